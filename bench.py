@@ -1,0 +1,354 @@
+"""Benchmark of the CCCS beam-dose engine (forward + adjoint beam-doses/s).
+
+Workload (one step): the batched candidate-beam set -- 200x200x160 voxel
+head-and-neck-like phantom at 2 mm, 1024 non-coplanar beams on a ~6 degree
+4-pi grid, per-beam fluence maps of 8^2..40^2 beamlets of 2.5 mm with U(0,1)
+weights, 8x6 = 48 double-exponential collapsed cones, FP32.  One step is the
+forward dose of every beam plus the adjoint (fluence gradient) of every beam.
+Inputs are seeded synthetic data (no public dataset exists for this path).
+
+value : beam-doses/s with inputs resident in HBM (CUDA events on the engine
+        stream, L2 flushed between steps).
+e2e   : the same through the host-pointer C-ABI calls (pinned host fluence and
+        dose gradient in, dose and fluence gradient out).
+plain : one beam per call (the plain per-beam path), for the batched/plain ratio.
+
+``--impl reference`` times the CPU restatement of the reference algorithm
+(24-radius cumulative-kernel walk, FP32, OpenMP on all host cores) on a
+bounded sample of the same workload.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "beam-doses/s fwd+adjoint batched vs plain, 1 GB300, <=0.5% Dmax err; p50/p99 ms"
+UNIT = "beam-doses/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--beams", type=int, default=1024)
+    ap.add_argument("--plain-beams", type=int, default=32)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true")
+    return ap.parse_args()
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        backend = "nccl"
+        dist.init_process_group(backend)
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, ws):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{index}.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.3)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax = float(p[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_workload(n_beams, seed_offset=0):
+    from endtoend_gb300 import inputs
+    vol = inputs.head_neck_phantom(shape=(200, 200, 160), voxel_cm=0.2)
+    phys = inputs.make_physics(seed=0, spacing_cm=0.2)
+    beams = inputs.candidate_beams(n_beams, seed=3 + seed_offset)
+    return vol, phys, beams
+
+
+def cpu_reference_sample(vol, phys, beams, steps=1, warmup=0, nthreads=None):
+    """FP32 OpenMP restatement of the reference chain (table kernel) on one
+    beam: forward dose + adjoint.  Returns seconds per beam-dose."""
+    from oracle.oracle import Oracle
+    o = Oracle(vol, phys, kernel_mode=0, precision=32, nthreads=nthreads)
+    g = np.random.default_rng(7).standard_normal(vol.density.shape).astype(np.float32)
+    times = []
+    for i in range(warmup + steps):
+        b = beams[i % len(beams)]
+        t0 = time.perf_counter()
+        o.beam_dose(b)
+        o.beam_dose_adjoint(b, g)
+        dt = time.perf_counter() - t0
+        if i >= warmup:
+            times.append(dt)
+    return float(np.mean(times)), o.setup.nthreads
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    vol, phys, beams = make_workload(8)
+    # bounded sample: one beam forward + adjoint per step
+    t_step, cores = cpu_reference_sample(vol, phys, beams, steps=args.steps, warmup=min(args.warmup, 1))
+    v = 1.0 / t_step
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)", "impl": "reference",
+            "config": {"workload": "batched candidate beams: 200x200x160 @2mm head-neck phantom, 48 cones, "
+                                   "fluence 8^2-40^2 beamlets @2.5mm; sample = 1 beam fwd+adjoint per step",
+                       "kernel": "reference 24-radius cumulative table walk (O(L^2) per line)",
+                       "l2": "n/a (CPU)"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": "1 beam forward + adjoint of the batched candidate workload per step"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def algorithmic_bytes(infos):
+    """Per-solve algorithmic bytes: 392 * V_beam per beam (TERMA 8 B/voxel,
+    each of 24 cone directions 8 B/voxel read + 8 B/voxel dose RMW)."""
+    vb = sum(i["v_beam"] for i in infos)
+    return 392.0 * vb, vb
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+        return
+    import torch
+    from endtoend_gb300 import engine, metrics
+
+    torch.cuda.set_device(local)
+    vol, phys, beams = make_workload(args.beams, seed_offset=rank)
+    eng = engine.Engine(local)
+    eng.set_volume(vol)
+    eng.set_physics(phys, mode="exp")
+    stream = torch.cuda.ExternalStream(eng.stream)
+    nfull = vol.nvoxels
+    fl_host = engine.concat_fluence(beams)
+    d_fl = torch.from_numpy(fl_host).cuda()
+    d_dose = torch.zeros(nfull, dtype=torch.float32, device="cuda")
+    rng = np.random.default_rng(11)
+    grad_host = rng.standard_normal(nfull).astype(np.float32)
+    d_grad = torch.from_numpy(grad_host).cuda()
+    d_fgrad = torch.zeros_like(d_fl)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+
+    def step_device():
+        eng.beam_dose_device(beams, d_fl.data_ptr(), d_dose.data_ptr(), engine.DOSE_SUM)
+        eng.beam_dose_adjoint_device(beams, d_fl.data_ptr(), d_grad.data_ptr(), d_fgrad.data_ptr())
+
+    for _ in range(args.warmup):
+        step_device()
+    eng.synchronize()
+    # one profiled step (untimed): per-stage device time + launches
+    eng.set_profiling(True)
+    eng.read_profile()
+    step_device()
+    eng.synchronize()
+    prof = eng.read_profile()
+    eng.set_profiling(False)
+    infos = [eng.beam_info(i) for i in range(len(beams))]
+
+    clocks = ClockSampler(local)
+    barrier(ws)
+    torch.cuda.synchronize()
+    clocks.start()
+    step_ms = []
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        step_device()
+        b.record(stream)
+        b.synchronize()
+        step_ms.append(a.elapsed_time(b))
+    torch.cuda.synchronize()
+    barrier(ws)
+    clk = clocks.stop()
+    t_dev = max_over_ranks(sum(step_ms) / 1e3, ws)
+    value = ws * len(beams) * args.steps / t_dev
+
+    # e2e through host pointers (pinned host memory)
+    pin_fl = torch.from_numpy(fl_host).pin_memory().numpy()
+    pin_grad = torch.from_numpy(grad_host).pin_memory().numpy()
+    pin_dose = torch.zeros(nfull, dtype=torch.float32).pin_memory().numpy()
+    pin_fgrad = torch.zeros(fl_host.size, dtype=torch.float32).pin_memory().numpy()
+    import ctypes as C
+    eb = engine.to_ee_beams(beams)
+
+    def step_host():
+        eng._check(eng.lib.ee_beam_dose(eng.h, eb, len(beams), C.c_void_p(pin_fl.ctypes.data),
+                                        C.c_void_p(pin_dose.ctypes.data), engine.DOSE_SUM))
+        eng._check(eng.lib.ee_beam_dose_adjoint(eng.h, eb, len(beams), C.c_void_p(pin_fl.ctypes.data),
+                                                C.c_void_p(pin_grad.ctypes.data), C.c_void_p(pin_fgrad.ctypes.data)))
+
+    step_host()
+    barrier(ws)
+    torch.cuda.synchronize()
+    e2e_lat = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        step_host()
+        e2e_lat.append(time.perf_counter() - t0)
+    barrier(ws)
+    t_e2e = max_over_ranks(sum(e2e_lat), ws)
+    e2e = ws * len(beams) * args.steps / t_e2e
+    h2d = pin_fl.nbytes * 2 + pin_grad.nbytes
+    d2h = pin_dose.nbytes + pin_fgrad.nbytes
+
+    # plain per-beam path: one beam per call
+    npl = min(args.plain_beams, len(beams))
+    pb = beams[:npl]
+    offs = np.cumsum([0] + [b.fluence.size for b in pb])
+    torch.cuda.synchronize()
+    lat = []
+    t0 = time.perf_counter()
+    for i, b in enumerate(pb):
+        s0 = time.perf_counter()
+        eng.beam_dose_device([b], d_fl.data_ptr() + 4 * int(offs[i]), d_dose.data_ptr(), engine.DOSE_SUM)
+        eng.beam_dose_adjoint_device([b], d_fl.data_ptr() + 4 * int(offs[i]), d_grad.data_ptr(),
+                                     d_fgrad.data_ptr() + 4 * int(offs[i]))
+        eng.synchronize()
+        lat.append(time.perf_counter() - s0)
+    plain = npl / (time.perf_counter() - t0)
+
+    # roofline of the dominant stage (CUDA-event stage times of the profiled step)
+    dom = max(prof, key=lambda k: prof[k][0])
+    alg_bytes, vb = algorithmic_bytes(infos)
+    stage_bytes = {
+        "terma": 8.0 * vb, "cone": 24 * 12.0 * vb, "gather": 24 * 4.0 * vb + 4.0 * vb,
+        "gather_T": 24 * 4.0 * vb + 4.0 * vb, "cone_T": 24 * 12.0 * vb, "terma_T": 8.0 * vb, "geometry": 0.0,
+    }
+    import json as _json
+    peaks = {}
+    try:
+        peaks = _json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    dom_ms, dom_launches = prof[dom]
+    achieved = stage_bytes.get(dom, 0.0) / (dom_ms / 1e3) / 1e9 if dom_ms > 0 else 0.0
+    roof = {"bound": "hbm", "kernel": f"k_{dom}", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": None,
+            "peak_source": "measured" if peaks else "fallback",
+            "stage_ms": {k: round(v[0], 3) for k, v in prof.items()},
+            "chain_frac": (2 * alg_bytes / (sum(step_ms) / len(step_ms) / 1e3) / 1e9) / peak}
+    gpu_launches = int(sum(v[1] for v in prof.values())) * args.steps
+
+    # accuracy vs the reference discretisation on one beam (FP64 oracle,
+    # 24-radius table, texture 8-bit weights)
+    acc = None
+    if not args.no_accuracy and rank == 0:
+        from oracle.oracle import Oracle
+        b = beams[0]
+        d = eng.beam_dose([b])
+        ref, _ = Oracle(vol, phys, kernel_mode=0, tex_emulate=True).beam_dose(b)
+        ref64, _ = Oracle(vol, phys, kernel_mode=2).beam_dose(b)
+        acc = {"max_abs_diff_over_dmax_vs_reference_discretisation": metrics.max_rel_diff(d, ref),
+               "max_abs_diff_over_dmax_vs_fp64_oracle_same_kernel": metrics.max_rel_diff(d, ref64),
+               "beam": 0}
+
+    cpu = None
+    if not args.no_cpu_baseline and rank == 0:
+        t_cpu, cores = cpu_reference_sample(vol, phys, beams, steps=1, warmup=0)
+        cpu = {"value": 1.0 / t_cpu, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": "1 beam forward + adjoint (FP32 OpenMP restatement, 24-radius table walk)"}
+
+    lat_ms = np.array(lat) * 1e3
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_dev / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": "batched candidate beams: 200x200x160 @2mm head-neck phantom, "
+                                   f"{len(beams)} beams/GPU, 48 cones (8x6), fluence 8^2-40^2 @2.5mm; "
+                                   "step = forward + adjoint of every beam",
+                       "kernel": "double exponential, O(L) warp-scan", "parallelism": f"beams sharded x{ws}",
+                       "l2": "flushed (256 MB write) between timed steps"},
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+            "plain": {"value": plain, "unit": UNIT, "beams": npl, "p50_ms": float(np.percentile(lat_ms, 50)),
+                      "p99_ms": float(np.percentile(lat_ms, 99))},
+            "batched_over_plain": value / plain,
+            "gpu_launches": gpu_launches,
+            "roofline": roof,
+            "clocks": clk,
+            "accuracy": acc,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    eng.close()
+
+
+if __name__ == "__main__":
+    main()

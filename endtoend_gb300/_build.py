@@ -1,0 +1,72 @@
+"""In-tree build of the CUDA engine library ``endtoend_gb300/_lib/libee_cccs.so``.
+
+nvcc, one ``-gencode`` for sm_103a, the two translation units compiled in
+parallel, then linked as a shared library with the C ABI of include/ee_cccs.h.
+No torch, no cmake: the result loads with ctypes (or any C FFI).
+"""
+import os
+import shutil
+import subprocess
+import sys
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+OUT_DIR = os.path.join(PKG, "_lib")
+LIB = os.path.join(OUT_DIR, "libee_cccs.so")
+SOURCES = ["ee_kernels.cu", "ee_api.cpp"]
+HEADERS = ["ee_internal.h", os.path.join("..", "..", "include", "ee_cccs.h")]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def nvcc_path():
+    p = shutil.which("nvcc")
+    if p:
+        return p
+    cand = "/usr/local/cuda/bin/nvcc"
+    if os.path.exists(cand):
+        return cand
+    raise RuntimeError("nvcc not found: the CUDA toolkit is required to build the engine")
+
+
+def _stale():
+    if not os.path.exists(LIB):
+        return True
+    t = os.path.getmtime(LIB)
+    deps = [os.path.join(CSRC, s) for s in SOURCES] + [os.path.normpath(os.path.join(CSRC, h)) for h in HEADERS]
+    deps.append(os.path.abspath(__file__))
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def build(verbose=False, force=False):
+    """Compile (if stale) and return the library path."""
+    if not force and not _stale():
+        return LIB
+    nvcc = nvcc_path()
+    os.makedirs(OUT_DIR, exist_ok=True)
+    common = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "-I", os.path.join(ROOT, "include")]
+    procs, objs = [], []
+    for src in SOURCES:
+        obj = os.path.join(OUT_DIR, os.path.splitext(src)[0] + ".o")
+        objs.append(obj)
+        cmd = [nvcc] + common + ["-c", os.path.join(CSRC, src), "-o", obj]
+        if src.endswith(".cpp"):
+            cmd = [nvcc] + common + ["-x", "cu", "-c", os.path.join(CSRC, src), "-o", obj]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        procs.append(subprocess.Popen(cmd))
+    for p in procs:
+        if p.wait() != 0:
+            raise RuntimeError("nvcc compilation of the CCCS engine failed")
+    tmp = LIB + ".tmp"
+    cmd = [nvcc] + ARCH + ["-shared", "-cudart", "static", "-o", tmp] + objs
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    if subprocess.call(cmd) != 0:
+        raise RuntimeError("linking libee_cccs.so failed")
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(verbose=True, force="-f" in sys.argv))

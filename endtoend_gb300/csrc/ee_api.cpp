@@ -1,0 +1,685 @@
+// ee_api.cpp -- host side of the CCCS engine: context, device-resident
+// caches, beam geometry, the per-batch pipeline and the C ABI of ee_cccs.h.
+//
+// Pipeline of one batch of beams (the reference runs the same stages one
+// beam and one cone at a time, CCCS/dosecalc-beam/nvbbRayConvolve_host.cu:376-725):
+//   H2D beam specs -> k_geom_init -> k_terma (+crop-box reduction)
+//   -> k_geometry -> [one read-back of the per-beam geometry: REV arena
+//   offsets] -> k_cone (all cones of all beams) -> k_gather (all cones of all
+//   beams accumulated per voxel).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/ee_cccs.h"
+#include "ee_internal.h"
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define EE_CUDA(call)                                                                              \
+    do {                                                                                           \
+        cudaError_t _e = (call);                                                                   \
+        if (_e != cudaSuccess)                                                                     \
+            return fail(EE_ERR_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(_e), __FILE__, \
+                        __LINE__);                                                                 \
+    } while (0)
+
+// ----------------------------------------------------------- geometry ---
+// Double-precision restatement of CCCS/CudaUtilities/geometry.cu:46-145.
+struct d3 {
+    double x, y, z;
+};
+d3 rot_axis(d3 p, d3 r, double t) {
+    double s = std::sin(t), c = std::cos(t);
+    double d = -r.x * p.x - r.y * p.y - r.z * p.z;
+    return {(-r.x * d) * (1 - c) + p.x * c + (-r.z * p.y + r.y * p.z) * s,
+            (-r.y * d) * (1 - c) + p.y * c + (r.z * p.x - r.x * p.z) * s,
+            (-r.z * d) * (1 - c) + p.z * c + (-r.y * p.x + r.x * p.y) * s};
+}
+d3 rot_beam(d3 v, double az, double zen, double coll) {
+    d3 t = rot_axis(v, {std::sin(-zen), 0, std::cos(-zen)}, -az);
+    return rot_axis(t, {0, 1, 0}, zen + coll);
+}
+d3 inv_rot_beam(d3 v, double az, double zen, double coll) {
+    d3 t = rot_axis(v, {0, 1, 0}, -(zen + coll));
+    return rot_axis(t, {std::sin(-zen), 0, std::cos(-zen)}, az);
+}
+d3 rot_kern(d3 v, double th, double ph) {
+    d3 u = rot_axis(v, {std::cos(ph), 0, -std::sin(ph)}, -th);
+    return rot_axis(u, {0, 1, 0}, -ph);
+}
+d3 inv_rot_kern(d3 v, double th, double ph) {
+    d3 u = rot_axis(v, {0, 1, 0}, ph);
+    return rot_axis(u, {std::cos(ph), 0, -std::sin(ph)}, th);
+}
+template <class F>
+void matrix_of(F f, float* M) {
+    d3 c[3] = {f({1, 0, 0}), f({0, 1, 0}), f({0, 0, 1})};
+    for (int j = 0; j < 3; j++) {
+        M[0 * 3 + j] = (float)c[j].x;
+        M[1 * 3 + j] = (float)c[j].y;
+        M[2 * 3 + j] = (float)c[j].z;
+    }
+}
+
+const double kPi = 3.14159265358979323846;
+
+// BEAM::reconfigure, angle orientation (CCCS/DoseCalcIO/beam.cpp:300-321).
+void reconfigure(const ee_beam& b, double& az, double& zen, d3& src, d3& dir) {
+    az = std::fmod((double)b.azimuth, 2 * kPi);
+    zen = std::fmod((double)b.zenith, 2 * kPi);
+    auto close = [](double a, double c) { return std::fabs(c - a) <= 1e-6; };
+    if (!close(zen, 0.0) && (close(az, 0.0) || close(az, kPi))) zen = 0.0;
+    d3 s = inv_rot_beam({0, -(double)b.sad, 0}, az, zen, 0);
+    src = {s.x + b.isocenter[0], s.y + b.isocenter[1], s.z + b.isocenter[2]};
+    d3 d = {b.isocenter[0] - src.x, b.isocenter[1] - src.y, b.isocenter[2] - src.z};
+    double l = std::sqrt(d.x * d.x + d.y * d.y + d.z * d.z);
+    dir = {d.x / l, d.y / l, d.z / l};
+}
+
+template <class T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    cudaError_t ensure(size_t count) {
+        if (count <= n && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+        size_t want = std::max<size_t>(count, 1);
+        cudaError_t e = cudaMalloc((void**)&p, want * sizeof(T));
+        if (e == cudaSuccess) n = want;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+};
+
+template <class T>
+struct PinBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    cudaError_t ensure(size_t count) {
+        if (count <= n && p) return cudaSuccess;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        n = 0;
+        size_t want = std::max<size_t>(count, 1);
+        cudaError_t e = cudaMallocHost((void**)&p, want * sizeof(T));
+        if (e == cudaSuccess) n = want;
+        return e;
+    }
+    void release() {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        n = 0;
+    }
+};
+
+}  // namespace
+
+struct ee_context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::mutex mu;
+    bool have_volume = false, have_spectrum = false, have_table = false, have_exp = false;
+    EeParams P{};
+    ee_frame frame{};
+    ee_conv_params conv{};
+    std::vector<EeRayConst> rays;
+    DevBuf<float> density, cumkern, expp;
+    DevBuf<EeRayConst> d_rays;
+    // per-call scratch
+    DevBuf<EeBeamSpec> d_specs;
+    DevBuf<EeBeamGeom> d_geoms;
+    DevBuf<float> terma, unit, rev, rev_grad, terma_grad;
+    DevBuf<int> bl_idx;
+    DevBuf<float> io_fluence, io_dose, io_grad;
+    PinBuf<EeBeamSpec> h_specs;
+    PinBuf<EeBeamGeom> h_geoms;
+    std::vector<EeBeamGeom> last_geoms;
+    std::vector<EeBeamSpec> last_specs;
+    long long max_batch_bytes = 8ll << 30;  // scratch budget for one chunk of beams
+    // profiling
+    bool profiling = false;
+    struct Pending {
+        int stage;
+        cudaEvent_t a, b;
+    };
+    std::vector<Pending> pending;
+    std::vector<cudaEvent_t> event_pool;
+    double stage_ms[EE_NSTAGES] = {0};
+    long long stage_launches[EE_NSTAGES] = {0};
+};
+
+namespace {
+
+int check_ready(ee_context* c) {
+    if (!c) return fail(EE_ERR_INVALID_ARG, "null context");
+    if (!c->have_volume) return fail(EE_ERR_NOT_READY, "ee_set_volume has not been called");
+    if (!c->have_spectrum) return fail(EE_ERR_NOT_READY, "ee_set_spectrum has not been called");
+    if (!c->have_table) return fail(EE_ERR_NOT_READY, "ee_set_kernel_table has not been called");
+    if (c->P.mode == EE_KERNEL_EXP && !c->have_exp) return fail(EE_ERR_NOT_READY, "exp kernel mode without ee_set_kernel_exp");
+    return EE_OK;
+}
+
+int check_beams(const ee_beam* beams, int nbeams) {
+    if (!beams || nbeams <= 0) return fail(EE_ERR_INVALID_ARG, "no beams");
+    for (int b = 0; b < nbeams; b++) {
+        const ee_beam& B = beams[b];
+        if (B.fmap_size[0] <= 0 || B.fmap_size[1] <= 0 || !(B.beamlet_size[0] > 0) || !(B.beamlet_size[1] > 0) ||
+            !(B.sad > 0))
+            return fail(EE_ERR_INVALID_ARG, "beam %d: invalid fluence map / beamlet size / SAD", b);
+    }
+    return EE_OK;
+}
+
+void build_specs(const ee_beam* beams, int nbeams, long long fl_base, EeBeamSpec* out) {
+    long long off = fl_base;
+    for (int b = 0; b < nbeams; b++) {
+        const ee_beam& B = beams[b];
+        double az, zen;
+        d3 src, dir;
+        reconfigure(B, az, zen, src, dir);
+        EeBeamSpec& S = out[b];
+        std::memset(&S, 0, sizeof(S));
+        S.src[0] = (float)src.x; S.src[1] = (float)src.y; S.src[2] = (float)src.z;
+        S.dir[0] = (float)dir.x; S.dir[1] = (float)dir.y; S.dir[2] = (float)dir.z;
+        for (int a = 0; a < 3; a++) S.iso[a] = B.isocenter[a];
+        S.az = (float)az; S.zen = (float)zen; S.coll = B.coll; S.sad = B.sad;
+        d3 id = {B.isocenter[0] - src.x, B.isocenter[1] - src.y, B.isocenter[2] - src.z};
+        S.isodist = (float)std::sqrt(id.x * id.x + id.y * id.y + id.z * id.z);
+        double coll = B.coll;
+        matrix_of([&](d3 v) { return rot_beam(v, az, zen, coll); }, S.MB);
+        matrix_of([&](d3 v) { return inv_rot_beam(v, az, zen, coll); }, S.MBi);
+        S.fmap[0] = B.fmap_size[0]; S.fmap[1] = B.fmap_size[1];
+        S.beamlet[0] = B.beamlet_size[0]; S.beamlet[1] = B.beamlet_size[1];
+        S.fl_off = off;
+        off += (long long)B.fmap_size[0] * B.fmap_size[1];
+    }
+}
+
+const char* status_text(int st) {
+    switch (st) {
+        case EE_ERR_CROPBOX: return "bev_cropbox_size error (no TERMA in the calc bbox, or crop box >= 1000 voxels)";
+        case EE_ERR_REV_SIZE: return "convolution array size exceeds the REV limit";
+        case EE_ERR_SIDDON_ITER: return "Siddon ray trace hit its iteration cap";
+        case EE_ERR_CAPACITY: return "REV arena too small";
+        default: return "geometry error";
+    }
+}
+
+cudaEvent_t take_event(ee_context* c) {
+    if (!c->event_pool.empty()) {
+        cudaEvent_t e = c->event_pool.back();
+        c->event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+// Resolve recorded event pairs into per-stage milliseconds.
+void drain_profile(ee_context* c) {
+    for (auto& p : c->pending) {
+        float ms = 0.f;
+        if (cudaEventSynchronize(p.b) == cudaSuccess && cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess)
+            c->stage_ms[p.stage] += ms;
+        c->event_pool.push_back(p.a);
+        c->event_pool.push_back(p.b);
+    }
+    c->pending.clear();
+}
+
+// Launch `fn` bracketed by profiling events when enabled; counts launches.
+template <class F>
+cudaError_t staged(ee_context* c, int stage, int nlaunch, F fn) {
+    c->stage_launches[stage] += nlaunch;
+    if (!c->profiling) return fn();
+    cudaEvent_t a = take_event(c), b = take_event(c);
+    cudaEventRecord(a, c->stream);
+    cudaError_t e = fn();
+    cudaEventRecord(b, c->stream);
+    c->pending.push_back({stage, a, b});
+    return e;
+}
+
+long long nbbox_of(const ee_context* c) { return (long long)c->P.bbs[0] * c->P.bbs[1] * c->P.bbs[2]; }
+long long nfull_of(const ee_context* c) { return (long long)c->P.size[0] * c->P.size[1] * c->P.size[2]; }
+
+// Beams per chunk so that TERMA (+unit/index for the adjoint) fits the budget.
+int chunk_beams(const ee_context* c, int nbeams, bool adjoint) {
+    long long per = nbbox_of(c) * (long long)sizeof(float) * (adjoint ? 4 : 1) + 64ll * 1024 * 1024;
+    long long k = std::max(1ll, c->max_batch_bytes / per);
+    return (int)std::min<long long>(nbeams, std::min<long long>(k, 4096));
+}
+
+// Stages 1-3 for a chunk: specs up, TERMA + crop box, geometry, read-back,
+// REV arena offsets.  On return h_geoms holds the chunk's geometry.
+int run_front(ee_context* c, const ee_beam* beams, int nb, const float* d_fluence, long long fl_base, bool adjoint,
+              long long& rev_total, int& max_line, int& max_lines) {
+    cudaStream_t s = c->stream;
+    const long long nbbox = nbbox_of(c);
+    EE_CUDA(c->h_specs.ensure(nb));
+    EE_CUDA(c->h_geoms.ensure(nb));
+    EE_CUDA(c->d_specs.ensure(nb));
+    EE_CUDA(c->d_geoms.ensure(nb));
+    build_specs(beams, nb, 0, c->h_specs.p);
+    (void)fl_base;
+    EE_CUDA(cudaMemcpyAsync(c->d_specs.p, c->h_specs.p, sizeof(EeBeamSpec) * nb, cudaMemcpyHostToDevice, s));
+    EE_CUDA(c->terma.ensure((size_t)nb * nbbox));
+    if (adjoint) {
+        EE_CUDA(c->unit.ensure((size_t)nb * nbbox));
+        EE_CUDA(c->bl_idx.ensure((size_t)nb * nbbox));
+    }
+    EE_CUDA(staged(c, EE_STAGE_GEOMETRY, 1, [&] { return ee_launch_geom_init(c->d_geoms.p, nb, s); }));
+    EE_CUDA(staged(c, EE_STAGE_TERMA, 1, [&] {
+        return ee_launch_terma(c->P, c->d_specs.p, c->d_geoms.p, d_fluence, c->terma.p, adjoint ? c->unit.p : nullptr,
+                               adjoint ? c->bl_idx.p : nullptr, nb, s);
+    }));
+    EE_CUDA(staged(c, EE_STAGE_GEOMETRY, 1, [&] { return ee_launch_geometry(c->P, c->d_specs.p, c->d_geoms.p, nb, s); }));
+    EE_CUDA(cudaMemcpyAsync(c->h_geoms.p, c->d_geoms.p, sizeof(EeBeamGeom) * nb, cudaMemcpyDeviceToHost, s));
+    EE_CUDA(cudaStreamSynchronize(s));
+    rev_total = 0;
+    max_line = 1;
+    max_lines = 1;
+    for (int b = 0; b < nb; b++) {
+        EeBeamGeom& G = c->h_geoms.p[b];
+        if (G.status != 0) return fail(G.status, "beam %d: %s", b, status_text(G.status));
+        G.arena_off = rev_total;
+        G.arena_cap = G.rev_total;
+        rev_total += G.rev_total;
+        max_line = std::max(max_line, G.max_line);
+        max_lines = std::max(max_lines, G.max_lines);
+    }
+    EE_CUDA(cudaMemcpyAsync(c->d_geoms.p, c->h_geoms.p, sizeof(EeBeamGeom) * nb, cudaMemcpyHostToDevice, s));
+    c->last_geoms.assign(c->h_geoms.p, c->h_geoms.p + nb);
+    c->last_specs.assign(c->h_specs.p, c->h_specs.p + nb);
+    return EE_OK;
+}
+
+int dose_device(ee_context* c, const ee_beam* beams, int nbeams, const float* d_fluence, float* d_dose, int mode) {
+    int st = check_ready(c);
+    if (st) return st;
+    if ((st = check_beams(beams, nbeams))) return st;
+    if (!d_fluence || !d_dose) return fail(EE_ERR_INVALID_ARG, "null fluence/dose pointer");
+    if (mode < 0 || mode > 2) return fail(EE_ERR_INVALID_ARG, "bad dose mode %d", mode);
+    EE_CUDA(cudaSetDevice(c->device));
+    const long long nfull = nfull_of(c);
+    const int chunk = chunk_beams(c, nbeams, false);
+    long long fl_off = 0;
+    std::vector<EeBeamGeom> all;
+    std::vector<EeBeamSpec> allspec;
+    for (int b0 = 0; b0 < nbeams; b0 += chunk) {
+        int nb = std::min(chunk, nbeams - b0);
+        long long rev_total;
+        int max_line, max_lines;
+        st = run_front(c, beams + b0, nb, d_fluence + fl_off, fl_off, false, rev_total, max_line, max_lines);
+        if (st) return st;
+        EE_CUDA(c->rev.ensure((size_t)rev_total));
+        EE_CUDA(staged(c, EE_STAGE_CONE, 1, [&] { return ee_launch_cone(c->P, c->d_geoms.p, c->terma.p, c->rev.p, nb, max_lines, max_line, c->stream); }));
+        int m = mode;
+        float* out = d_dose;
+        if (mode == EE_DOSE_SUM && b0 > 0) m = EE_DOSE_ACCUMULATE;
+        if (mode == EE_DOSE_PER_BEAM) out = d_dose + (long long)b0 * nfull;
+        EE_CUDA(staged(c, EE_STAGE_GATHER, 1, [&] { return ee_launch_gather(c->P, c->d_specs.p, c->d_geoms.p, c->rev.p, out, nb, m, c->stream); }));
+        for (int b = 0; b < nb; b++) fl_off += (long long)beams[b0 + b].fmap_size[0] * beams[b0 + b].fmap_size[1];
+        all.insert(all.end(), c->last_geoms.begin(), c->last_geoms.end());
+        allspec.insert(allspec.end(), c->last_specs.begin(), c->last_specs.end());
+        if (b0 + nb < nbeams) EE_CUDA(cudaStreamSynchronize(c->stream));  // scratch reuse
+    }
+    c->last_geoms.swap(all);
+    c->last_specs.swap(allspec);
+    return EE_OK;
+}
+
+int adjoint_device(ee_context* c, const ee_beam* beams, int nbeams, const float* d_fluence, const float* d_grad,
+                   float* d_fgrad) {
+    int st = check_ready(c);
+    if (st) return st;
+    if ((st = check_beams(beams, nbeams))) return st;
+    if (!d_fluence || !d_grad || !d_fgrad) return fail(EE_ERR_INVALID_ARG, "null pointer");
+    EE_CUDA(cudaSetDevice(c->device));
+    const long long nbbox = nbbox_of(c);
+    const int chunk = chunk_beams(c, nbeams, true);
+    long long fl_off = 0;
+    for (int b0 = 0; b0 < nbeams; b0 += chunk) {
+        int nb = std::min(chunk, nbeams - b0);
+        long long rev_total;
+        int max_line, max_lines;
+        st = run_front(c, beams + b0, nb, d_fluence + fl_off, fl_off, true, rev_total, max_line, max_lines);
+        if (st) return st;
+        long long nfl = 0;
+        for (int b = 0; b < nb; b++) nfl += (long long)beams[b0 + b].fmap_size[0] * beams[b0 + b].fmap_size[1];
+        EE_CUDA(c->rev_grad.ensure((size_t)rev_total));
+        EE_CUDA(c->terma_grad.ensure((size_t)nb * nbbox));
+        EE_CUDA(cudaMemsetAsync(c->rev_grad.p, 0, sizeof(float) * rev_total, c->stream));
+        EE_CUDA(cudaMemsetAsync(c->terma_grad.p, 0, sizeof(float) * nb * nbbox, c->stream));
+        EE_CUDA(cudaMemsetAsync(d_fgrad + fl_off, 0, sizeof(float) * nfl, c->stream));
+        EE_CUDA(staged(c, EE_STAGE_GATHER_T, 1, [&] { return ee_launch_gather_T(c->P, c->d_specs.p, c->d_geoms.p, d_grad, c->rev_grad.p, nb, c->stream); }));
+        EE_CUDA(staged(c, EE_STAGE_CONE_T, 1, [&] { return ee_launch_cone_T(c->P, c->d_geoms.p, c->rev_grad.p, c->terma_grad.p, nb, max_lines, max_line, c->stream); }));
+        EE_CUDA(staged(c, EE_STAGE_TERMA_T, 1, [&] {
+            return ee_launch_terma_T(c->P, c->d_specs.p, c->d_geoms.p, c->unit.p, c->bl_idx.p, c->terma_grad.p,
+                                     d_fgrad + fl_off, nb, c->stream);
+        }));
+        fl_off += nfl;
+        if (b0 + nb < nbeams) EE_CUDA(cudaStreamSynchronize(c->stream));
+    }
+    return EE_OK;
+}
+
+// max_rev_size as initCudaConstandTex derives it when the caller gives none
+// (host.cu:248-258, REV_PAD = 0).
+void derive_max_rev(ee_context* c) {
+    EeParams& P = c->P;
+    for (int a = 0; a < 3; a++) P.max_rev[a] = c->conv.max_rev_size[a];
+    if (!c->have_volume || c->conv.max_rev_size[0] > 0 || !(c->conv.rev_latspacing > 0)) return;
+    double mvs = std::min(c->conv.rev_latspacing, c->conv.rev_longspacing);
+    double bl = std::sqrt((double)P.bbs[0] * P.bbs[0] + (double)P.bbs[1] * P.bbs[1] + (double)P.bbs[2] * P.bbs[2]);
+    unsigned diag = (unsigned)std::ceil((float)bl * P.voxel[0] / (float)mvs);
+    unsigned m = diag + (unsigned)(2 * (c->conv.penumbra / mvs)) + 100;
+    for (int a = 0; a < 3; a++) P.max_rev[a] = (int)m;
+}
+
+long long total_fluence(const ee_beam* beams, int nbeams) {
+    long long n = 0;
+    for (int b = 0; b < nbeams; b++) n += (long long)beams[b].fmap_size[0] * beams[b].fmap_size[1];
+    return n;
+}
+
+}  // namespace
+
+// ======================================================================= ABI
+extern "C" {
+
+const char* ee_last_error(void) { return g_err.c_str(); }
+int ee_abi_version(void) { return EE_ABI_VERSION; }
+
+int ee_create(int device, ee_context** out) {
+    if (!out) return fail(EE_ERR_INVALID_ARG, "null output pointer");
+    *out = nullptr;
+    int n = 0;
+    EE_CUDA(cudaGetDeviceCount(&n));
+    if (device < 0 || device >= n) return fail(EE_ERR_INVALID_ARG, "device %d out of range (%d devices)", device, n);
+    EE_CUDA(cudaSetDevice(device));
+    ee_context* c = new ee_context();
+    c->device = device;
+    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete c;
+        return fail(EE_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
+    }
+    c->P.mode = EE_KERNEL_TABLE;
+    *out = c;
+    return EE_OK;
+}
+
+int ee_destroy(ee_context* c) {
+    if (!c) return EE_OK;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    c->density.release(); c->cumkern.release(); c->expp.release(); c->d_rays.release();
+    c->d_specs.release(); c->d_geoms.release(); c->terma.release(); c->unit.release(); c->rev.release();
+    c->rev_grad.release(); c->terma_grad.release(); c->bl_idx.release();
+    c->io_fluence.release(); c->io_dose.release(); c->io_grad.release();
+    c->h_specs.release(); c->h_geoms.release();
+    drain_profile(c);
+    for (auto e : c->event_pool) cudaEventDestroy(e);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return EE_OK;
+}
+
+int ee_set_volume(ee_context* c, const ee_frame* f, const float* density) {
+    if (!c || !f || !density) return fail(EE_ERR_INVALID_ARG, "null argument");
+    std::lock_guard<std::mutex> lk(c->mu);
+    ee_frame fr = *f;
+    for (int a = 0; a < 3; a++) {
+        if (fr.size[a] <= 0 || !(fr.voxel[a] > 0)) return fail(EE_ERR_INVALID_ARG, "bad volume size/voxel");
+        // enforce a valid bbox as load_omni_header does (calc_header.cpp:127-133)
+        if (fr.bbox_start[a] < 0 || fr.bbox_start[a] >= fr.size[a]) fr.bbox_start[a] = 0;
+        if (fr.bbox_size[a] <= 0 || fr.bbox_size[a] + fr.bbox_start[a] > fr.size[a]) fr.bbox_size[a] = fr.size[a] - fr.bbox_start[a];
+    }
+    EE_CUDA(cudaSetDevice(c->device));
+    size_t n = (size_t)fr.size[0] * fr.size[1] * fr.size[2];
+    EE_CUDA(c->density.ensure(n));
+    EE_CUDA(cudaMemcpyAsync(c->density.p, density, n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    EE_CUDA(cudaStreamSynchronize(c->stream));
+    c->frame = fr;
+    for (int a = 0; a < 3; a++) {
+        c->P.size[a] = fr.size[a]; c->P.voxel[a] = fr.voxel[a]; c->P.start[a] = fr.start[a];
+        c->P.bb0[a] = fr.bbox_start[a]; c->P.bbs[a] = fr.bbox_size[a];
+    }
+    c->P.density = c->density.p;
+    c->have_volume = true;
+    derive_max_rev(c);
+    return EE_OK;
+}
+
+int ee_set_spectrum(ee_context* c, int nE, const float* energy, const float* fluence, const float* mu, const float* mu_en) {
+    if (!c || !energy || !fluence || !mu) return fail(EE_ERR_INVALID_ARG, "null argument");
+    if (nE <= 0 || nE > EE_MAX_E) return fail(EE_ERR_INVALID_ARG, "nE must be in [1, %d]", EE_MAX_E);
+    (void)mu_en;  // beam-hardening correction is fixed to 1 (host.cu:204)
+    std::lock_guard<std::mutex> lk(c->mu);
+    double sum = 0;
+    for (int e = 0; e < nE; e++) sum += fluence[e];
+    if (!(sum > 0)) return fail(EE_ERR_INVALID_ARG, "spectrum fluence sums to zero");
+    c->P.nE = nE;
+    for (int e = 0; e < nE; e++) {
+        // fluence normalised to unit sum as read_spectrum_file does (spectra.cpp:56-58)
+        c->P.sp_fluence[e] = (float)(fluence[e] / sum);
+        c->P.sp_energy[e] = energy[e];
+        c->P.sp_mu[e] = mu[e];
+    }
+    c->have_spectrum = true;
+    return EE_OK;
+}
+
+int ee_set_kernel_table(ee_context* c, const ee_conv_params* cv, const float* radii, const float* cumkern,
+                        const float* theta_deg, const float* phi_deg) {
+    if (!c || !cv || !radii || !cumkern || !theta_deg || !phi_deg) return fail(EE_ERR_INVALID_ARG, "null argument");
+    if (cv->ntheta <= 0 || cv->ntheta > EE_MAX_THETA || (cv->ntheta & 1))
+        return fail(EE_ERR_INVALID_ARG, "ntheta must be even and <= %d", EE_MAX_THETA);
+    int nrays = cv->nphi * (cv->ntheta / 2);
+    if (cv->nphi <= 0 || nrays > EE_MAX_RAYS) return fail(EE_ERR_INVALID_ARG, "nphi*ntheta/2 must be in [1, %d]", EE_MAX_RAYS);
+    if (cv->nradii <= 0 || cv->nradii > EE_MAX_RADII) return fail(EE_ERR_INVALID_ARG, "nradii must be in [1, %d]", EE_MAX_RADII);
+    if (!(cv->rev_latspacing > 0) || !(cv->rev_longspacing > 0) || !(cv->penumbra >= 0))
+        return fail(EE_ERR_INVALID_ARG, "bad convolution spacing/penumbra");
+    std::lock_guard<std::mutex> lk(c->mu);
+    EE_CUDA(cudaSetDevice(c->device));
+    c->conv = *cv;
+    EeParams& P = c->P;
+    P.ntheta = cv->ntheta; P.nphi = cv->nphi; P.nradii = cv->nradii; P.nrays = nrays;
+    for (int r = 0; r < cv->nradii; r++) P.radii[r] = radii[r];
+    P.lat = cv->rev_latspacing; P.lng = cv->rev_longspacing; P.penumbra = cv->penumbra;
+    for (int a = 0; a < 3; a++) P.max_rev[a] = cv->max_rev_size[a];
+    derive_max_rev(c);
+    size_t nk = (size_t)cv->ntheta * cv->nradii;
+    EE_CUDA(c->cumkern.ensure(nk));
+    EE_CUDA(cudaMemcpy(c->cumkern.p, cumkern, nk * sizeof(float), cudaMemcpyHostToDevice));
+    P.cumkern = c->cumkern.p;
+    c->rays.resize(nrays);
+    for (int r = 0; r < nrays; r++) {
+        EeRayConst& R = c->rays[r];
+        double th = (double)theta_deg[r] * kPi / 180.0, ph = (double)phi_deg[r] * kPi / 180.0;
+        R.th = (float)th; R.ph = (float)ph;
+        R.row_fwd = r % (cv->ntheta / 2);
+        R.row_rev = cv->ntheta - 1 - R.row_fwd;
+        matrix_of([&](d3 v) { return rot_kern(v, th, ph); }, R.MK);
+        matrix_of([&](d3 v) { return inv_rot_kern(v, th, ph); }, R.MKi);
+    }
+    EE_CUDA(c->d_rays.ensure(nrays));
+    EE_CUDA(cudaMemcpy(c->d_rays.p, c->rays.data(), sizeof(EeRayConst) * nrays, cudaMemcpyHostToDevice));
+    P.rays = c->d_rays.p;
+    c->have_table = true;
+    return EE_OK;
+}
+
+int ee_set_kernel_exp(ee_context* c, const float* params) {
+    if (!c || !params) return fail(EE_ERR_INVALID_ARG, "null argument");
+    if (!c->have_table) return fail(EE_ERR_NOT_READY, "call ee_set_kernel_table first (cone angles, radii)");
+    std::lock_guard<std::mutex> lk(c->mu);
+    for (int t = 0; t < c->P.ntheta; t++)
+        if (!(params[4 * t + 1] > 0) || !(params[4 * t + 3] > 0))
+            return fail(EE_ERR_INVALID_ARG, "exp kernel attenuation coefficients must be > 0");
+    EE_CUDA(cudaSetDevice(c->device));
+    EE_CUDA(c->expp.ensure((size_t)4 * c->P.ntheta));
+    EE_CUDA(cudaMemcpy(c->expp.p, params, sizeof(float) * 4 * c->P.ntheta, cudaMemcpyHostToDevice));
+    c->P.expp = c->expp.p;
+    c->have_exp = true;
+    c->P.mode = EE_KERNEL_EXP;
+    return EE_OK;
+}
+
+int ee_set_kernel_mode(ee_context* c, int mode) {
+    if (!c) return fail(EE_ERR_INVALID_ARG, "null context");
+    if (mode != EE_KERNEL_TABLE && mode != EE_KERNEL_EXP) return fail(EE_ERR_INVALID_ARG, "bad kernel mode %d", mode);
+    if (mode == EE_KERNEL_EXP && !c->have_exp) return fail(EE_ERR_NOT_READY, "ee_set_kernel_exp has not been called");
+    c->P.mode = mode;
+    return EE_OK;
+}
+
+int ee_beam_dose_device(ee_context* c, const ee_beam* beams, int nbeams, const float* d_fluence, float* d_dose,
+                        int dose_mode) {
+    if (!c) return fail(EE_ERR_INVALID_ARG, "null context");
+    std::lock_guard<std::mutex> lk(c->mu);
+    return dose_device(c, beams, nbeams, d_fluence, d_dose, dose_mode);
+}
+
+int ee_beam_dose(ee_context* c, const ee_beam* beams, int nbeams, const float* fluence, float* dose, int dose_mode) {
+    if (!c) return fail(EE_ERR_INVALID_ARG, "null context");
+    int st = check_ready(c);
+    if (st) return st;
+    if ((st = check_beams(beams, nbeams))) return st;
+    if (!fluence || !dose) return fail(EE_ERR_INVALID_ARG, "null fluence/dose pointer");
+    std::lock_guard<std::mutex> lk(c->mu);
+    EE_CUDA(cudaSetDevice(c->device));
+    long long nfl = total_fluence(beams, nbeams);
+    long long nout = nfull_of(c) * (dose_mode == EE_DOSE_PER_BEAM ? nbeams : 1);
+    EE_CUDA(c->io_fluence.ensure(nfl));
+    EE_CUDA(c->io_dose.ensure(nout));
+    EE_CUDA(cudaMemcpyAsync(c->io_fluence.p, fluence, sizeof(float) * nfl, cudaMemcpyHostToDevice, c->stream));
+    if (dose_mode == EE_DOSE_ACCUMULATE)
+        EE_CUDA(cudaMemcpyAsync(c->io_dose.p, dose, sizeof(float) * nout, cudaMemcpyHostToDevice, c->stream));
+    st = dose_device(c, beams, nbeams, c->io_fluence.p, c->io_dose.p, dose_mode);
+    if (st) return st;
+    EE_CUDA(cudaMemcpyAsync(dose, c->io_dose.p, sizeof(float) * nout, cudaMemcpyDeviceToHost, c->stream));
+    EE_CUDA(cudaStreamSynchronize(c->stream));
+    return EE_OK;
+}
+
+int ee_beam_dose_adjoint_device(ee_context* c, const ee_beam* beams, int nbeams, const float* d_fluence,
+                                const float* d_grad, float* d_fgrad) {
+    if (!c) return fail(EE_ERR_INVALID_ARG, "null context");
+    std::lock_guard<std::mutex> lk(c->mu);
+    return adjoint_device(c, beams, nbeams, d_fluence, d_grad, d_fgrad);
+}
+
+int ee_beam_dose_adjoint(ee_context* c, const ee_beam* beams, int nbeams, const float* fluence, const float* grad,
+                         float* fgrad) {
+    if (!c) return fail(EE_ERR_INVALID_ARG, "null context");
+    int st = check_ready(c);
+    if (st) return st;
+    if ((st = check_beams(beams, nbeams))) return st;
+    if (!fluence || !grad || !fgrad) return fail(EE_ERR_INVALID_ARG, "null pointer");
+    std::lock_guard<std::mutex> lk(c->mu);
+    EE_CUDA(cudaSetDevice(c->device));
+    long long nfl = total_fluence(beams, nbeams);
+    long long nfull = nfull_of(c);
+    EE_CUDA(c->io_fluence.ensure(nfl));
+    EE_CUDA(c->io_grad.ensure(nfull + nfl));
+    EE_CUDA(cudaMemcpyAsync(c->io_fluence.p, fluence, sizeof(float) * nfl, cudaMemcpyHostToDevice, c->stream));
+    EE_CUDA(cudaMemcpyAsync(c->io_grad.p, grad, sizeof(float) * nfull, cudaMemcpyHostToDevice, c->stream));
+    st = adjoint_device(c, beams, nbeams, c->io_fluence.p, c->io_grad.p, c->io_grad.p + nfull);
+    if (st) return st;
+    EE_CUDA(cudaMemcpyAsync(fgrad, c->io_grad.p + nfull, sizeof(float) * nfl, cudaMemcpyDeviceToHost, c->stream));
+    EE_CUDA(cudaStreamSynchronize(c->stream));
+    return EE_OK;
+}
+
+int ee_get_beam_info(ee_context* c, int i, ee_beam_info* info) {
+    if (!c || !info) return fail(EE_ERR_INVALID_ARG, "null argument");
+    if (i < 0 || i >= (int)c->last_geoms.size()) return fail(EE_ERR_INVALID_ARG, "beam index %d out of range", i);
+    const EeBeamGeom& G = c->last_geoms[i];
+    const EeBeamSpec& S = c->last_specs[i];
+    std::memset(info, 0, sizeof(*info));
+    for (int a = 0; a < 3; a++) {
+        info->source[a] = S.src[a];
+        info->direction[a] = S.dir[a];
+        info->b_min[a] = G.bmin[a];
+        info->bev_size[a] = G.bev[a];
+        info->lim_min[a] = G.lim_min[a];
+    }
+    info->v_beam = G.v_beam;
+    info->rev_samples = G.rev_total;
+    info->terma_nonzero = G.nnz;
+    info->max_line = G.max_line;
+    info->status = G.status;
+    return EE_OK;
+}
+
+int ee_synchronize(ee_context* c) {
+    if (!c) return fail(EE_ERR_INVALID_ARG, "null context");
+    EE_CUDA(cudaStreamSynchronize(c->stream));
+    return EE_OK;
+}
+
+void* ee_get_stream(ee_context* c) { return c ? (void*)c->stream : nullptr; }
+
+int ee_set_profiling(ee_context* c, int enable) {
+    if (!c) return fail(EE_ERR_INVALID_ARG, "null context");
+    std::lock_guard<std::mutex> lk(c->mu);
+    drain_profile(c);
+    c->profiling = enable != 0;
+    return EE_OK;
+}
+
+int ee_read_profile(ee_context* c, double* ms, long long* launches, int n) {
+    if (!c) return fail(EE_ERR_INVALID_ARG, "null context");
+    std::lock_guard<std::mutex> lk(c->mu);
+    drain_profile(c);
+    for (int i = 0; i < n && i < EE_NSTAGES; i++) {
+        if (ms) ms[i] = c->stage_ms[i];
+        if (launches) launches[i] = c->stage_launches[i];
+    }
+    for (int i = 0; i < EE_NSTAGES; i++) {
+        c->stage_ms[i] = 0;
+        c->stage_launches[i] = 0;
+    }
+    return EE_OK;
+}
+
+int ee_beam_source(const ee_beam* b, float source[3], float direction[3]) {
+    if (!b || !source || !direction) return fail(EE_ERR_INVALID_ARG, "null argument");
+    double az, zen;
+    d3 s, d;
+    reconfigure(*b, az, zen, s, d);
+    source[0] = (float)s.x; source[1] = (float)s.y; source[2] = (float)s.z;
+    direction[0] = (float)d.x; direction[1] = (float)d.y; direction[2] = (float)d.z;
+    return EE_OK;
+}
+
+}  // extern "C"

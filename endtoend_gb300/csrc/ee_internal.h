@@ -1,0 +1,106 @@
+// Internal structures shared by the CCCS host code (ee_api.cpp) and the
+// sm_103a kernels (ee_kernels.cu).  POD only, identical on host and device.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#define EE_MAX_RAYS 64
+#define EE_MAX_E 32
+#define EE_MAX_RADII 32
+#define EE_MAX_THETA 48
+#define EE_MAX_LINE 1024  // longest convolution line (reference limit, host.cu:567)
+
+// Per-context constants, passed by value to every kernel.
+struct EeParams {
+    int size[3];
+    float voxel[3];
+    float start[3];
+    int bb0[3];
+    int bbs[3];
+    const float* density;  // full grid
+    int nE;
+    float sp_fluence[EE_MAX_E];
+    float sp_energy[EE_MAX_E];
+    float sp_mu[EE_MAX_E];
+    int ntheta, nphi, nradii, nrays;
+    float radii[EE_MAX_RADII];
+    float lat, lng, penumbra;
+    int max_rev[3];
+    int mode;                   // ee_kernel_mode
+    const float* cumkern;       // [ntheta][nradii]
+    const float* expp;          // [ntheta][4]
+    const struct EeRayConst* rays;  // [nrays]
+};
+
+// Per-cone constants (angles and rotations), built on the host.
+struct EeRayConst {
+    float th, ph;
+    int row_fwd, row_rev;  // kernel rows for the two walk directions
+    float MK[9];           // BEV -> REV   (rotateKernelAtOriginRHS), row-major
+    float MKi[9];          // REV -> BEV   (inverseRotateKernelAtOriginRHS)
+};
+
+// Per-beam constants built on the host.
+struct EeBeamSpec {
+    float src[3];
+    float dir[3];          // unit
+    float iso[3];
+    float az, zen, coll, sad;
+    float isodist;         // |iso - src|
+    float MB[9];           // RCS -> BEV (rotateBeamAtOriginRHS)
+    float MBi[9];          // BEV -> RCS
+    int fmap[2];
+    float beamlet[2];
+    long long fl_off;      // offset of this beam's fluence map
+};
+
+// Per-cone geometry of one beam, computed on the device.
+struct EeRayGeom {
+    int rev[3];            // (along-line, lateral-1, lateral-2) sizes
+    int nlines;            // rev[1]*rev[2]
+    long long offset;      // element offset in the beam's REV arena
+    float q0[3];           // rev_min / spacing (reference vector order)
+    float G0[3], Gx[3], Gy[3], Gz[3];  // REV (tX,tY,tZ) -> patient voxel index
+    float B0[3], Bx[3], By[3], Bz[3];  // REV (tX,tY,tZ) -> BEV crop-box index
+    float M[9];            // BEV -> REV (copy of MK for the gather)
+};
+
+// Per-beam geometry computed on the device (crop box + REV frames).
+struct EeBeamGeom {
+    int key_min[3];        // ordered-int keys for atomic min/max
+    int key_max[3];
+    unsigned int nnz;
+    int status;
+    float bmin[3];
+    int bev[3];
+    float lim_off[3];      // (lim_min - start)/voxel
+    float lim_min[3];
+    long long v_beam;
+    long long rev_total;
+    int max_line;
+    int max_lines;
+    long long arena_off;   // element offset of this beam's REV arena
+    long long arena_cap;   // elements available to this beam
+    EeRayGeom ray[EE_MAX_RAYS];
+};
+
+// Launch wrappers implemented in ee_kernels.cu.  All enqueue on `s`.
+cudaError_t ee_launch_geom_init(EeBeamGeom* g, int nbeams, cudaStream_t s);
+// unit/beamlet_idx (both optional) receive TERMA per unit fluence of every
+// in-field voxel and its beamlet index (adjoint).
+cudaError_t ee_launch_terma(const EeParams& P, const EeBeamSpec* specs, EeBeamGeom* geoms, const float* fluence,
+                            float* terma, float* unit, int* beamlet_idx, int nbeams, cudaStream_t s);
+cudaError_t ee_launch_geometry(const EeParams& P, const EeBeamSpec* specs, EeBeamGeom* geoms, int nbeams,
+                               cudaStream_t s);
+cudaError_t ee_launch_cone(const EeParams& P, const EeBeamGeom* geoms, const float* terma, float* rev,
+                           int nbeams, int max_lines, int max_line, cudaStream_t s);
+cudaError_t ee_launch_gather(const EeParams& P, const EeBeamSpec* specs, const EeBeamGeom* geoms, const float* rev,
+                             float* dose, int nbeams, int dose_mode, cudaStream_t s);
+// adjoint
+cudaError_t ee_launch_gather_T(const EeParams& P, const EeBeamSpec* specs, const EeBeamGeom* geoms,
+                               const float* dose_grad, float* rev_grad, int nbeams, cudaStream_t s);
+cudaError_t ee_launch_cone_T(const EeParams& P, const EeBeamGeom* geoms, const float* rev_grad, float* terma_grad,
+                             int nbeams, int max_lines, int max_line, cudaStream_t s);
+cudaError_t ee_launch_terma_T(const EeParams& P, const EeBeamSpec* specs, const EeBeamGeom* geoms,
+                              const float* unit_terma, const int* beamlet_idx, const float* terma_grad,
+                              float* fluence_grad, int nbeams, cudaStream_t s);

@@ -1,0 +1,833 @@
+// ee_kernels.cu -- sm_103a kernels of the CCCS beam-dose engine.
+//
+// Stages per beam (forward):
+//   k_terma     Siddon radiological path + polyenergetic TERMA, one thread per
+//               calc-bbox voxel, fused with the crop-box min/max reduction.
+//               Restates CCCS/DoseCalcAlgo/cudaSiddon.cu:20-308 and the host
+//               extent scan CCCS/dosecalc-beam/nvbbRayConvolve_host.cu:429-499.
+//   k_geometry  crop box -> BEV box, findREV for every cone, affine maps
+//               (host.cu:460-499, :75-155).
+//   k_cone_*    one warp per collapsed-cone line: trilinear gather of density
+//               and TERMA along the rotated line into shared memory
+//               (nvbbRayConvolve_device.cu:11-80), then the bidirectional line
+//               convolution (device.cu:87-218): EE_KERNEL_EXP as two warp-shuffle
+//               affine scans, EE_KERNEL_TABLE as the reference walk.
+//   k_gather    patient voxel <- sum over cones of the trilinear REV dose
+//               (device.cu:222-261), all cones of all beams of the batch in
+//               registers, one write per voxel.
+// Adjoint: k_gather_T (scatter), k_cone_T (reverse scans + TERMA scatter),
+// k_terma_T (per-beamlet reduction).
+#include "ee_internal.h"
+#include <cfloat>
+
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+
+__device__ __forceinline__ int f2key(float f) {
+    int i = __float_as_int(f);
+    return i >= 0 ? i : (i ^ 0x7fffffff);
+}
+__device__ __forceinline__ float key2f(int k) { return __int_as_float(k >= 0 ? k : (k ^ 0x7fffffff)); }
+
+struct f3 {
+    float x, y, z;
+};
+__device__ __forceinline__ f3 mk(float x, float y, float z) { return {x, y, z}; }
+__device__ __forceinline__ f3 operator+(f3 a, f3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ f3 operator-(f3 a, f3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ f3 operator*(f3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ float dot(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ f3 ld3(const float* p) { return {p[0], p[1], p[2]}; }
+__device__ __forceinline__ f3 mv(const float* M, f3 v) {
+    return {M[0] * v.x + M[1] * v.y + M[2] * v.z, M[3] * v.x + M[4] * v.y + M[5] * v.z,
+            M[6] * v.x + M[7] * v.y + M[8] * v.z};
+}
+
+// tex3D<float> with linear filtering, unnormalised coordinates and border
+// addressing, written as an explicit FP32 trilinear gather.  (x,y,z) are
+// texel-space coordinates after the -0.5 texel-centre shift.
+__device__ __forceinline__ float tri_border(const float* __restrict__ v, int nx, int ny, int nz, float x, float y,
+                                            float z) {
+    float fx = floorf(x), fy = floorf(y), fz = floorf(z);
+    int i = (int)fx, j = (int)fy, k = (int)fz;
+    float ax = x - fx, ay = y - fy, az = z - fz;
+    long long sxy = (long long)nx * ny;
+    if (i >= 0 && j >= 0 && k >= 0 && i + 1 < nx && j + 1 < ny && k + 1 < nz) {
+        const float* p = v + i + (long long)nx * j + sxy * k;
+        float c000 = __ldg(p), c100 = __ldg(p + 1), c010 = __ldg(p + nx), c110 = __ldg(p + nx + 1);
+        float c001 = __ldg(p + sxy), c101 = __ldg(p + sxy + 1), c011 = __ldg(p + sxy + nx), c111 = __ldg(p + sxy + nx + 1);
+        float c00 = c000 + ax * (c100 - c000), c10 = c010 + ax * (c110 - c010);
+        float c01 = c001 + ax * (c101 - c001), c11 = c011 + ax * (c111 - c011);
+        float c0 = c00 + ay * (c10 - c00), c1 = c01 + ay * (c11 - c01);
+        return c0 + az * (c1 - c0);
+    }
+    float acc = 0.f;
+#pragma unroll
+    for (int dk = 0; dk < 2; dk++) {
+        int kk = k + dk;
+        if (kk < 0 || kk >= nz) continue;
+        float wz = dk ? az : 1.f - az;
+#pragma unroll
+        for (int dj = 0; dj < 2; dj++) {
+            int jj = j + dj;
+            if (jj < 0 || jj >= ny) continue;
+            float wy = dj ? ay : 1.f - ay;
+#pragma unroll
+            for (int di = 0; di < 2; di++) {
+                int ii = i + di;
+                if (ii < 0 || ii >= nx) continue;
+                float wx = di ? ax : 1.f - ax;
+                acc += wx * wy * wz * __ldg(v + ii + (long long)nx * jj + sxy * kk);
+            }
+        }
+    }
+    return acc;
+}
+
+// Transpose of tri_border: atomically scatter g with the trilinear weights.
+__device__ __forceinline__ void tri_border_scatter(float* v, int nx, int ny, int nz, float x, float y, float z, float g) {
+    float fx = floorf(x), fy = floorf(y), fz = floorf(z);
+    int i = (int)fx, j = (int)fy, k = (int)fz;
+    float ax = x - fx, ay = y - fy, az = z - fz;
+    long long sxy = (long long)nx * ny;
+#pragma unroll
+    for (int dk = 0; dk < 2; dk++) {
+        int kk = k + dk;
+        if (kk < 0 || kk >= nz) continue;
+        float wz = dk ? az : 1.f - az;
+#pragma unroll
+        for (int dj = 0; dj < 2; dj++) {
+            int jj = j + dj;
+            if (jj < 0 || jj >= ny) continue;
+            float wy = dj ? ay : 1.f - ay;
+#pragma unroll
+            for (int di = 0; di < 2; di++) {
+                int ii = i + di;
+                if (ii < 0 || ii >= nx) continue;
+                float wx = di ? ax : 1.f - ax;
+                atomicAdd(v + ii + (long long)nx * jj + sxy * kk, wx * wy * wz * g);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------- TERMA --
+// Radiological path of the ray source -> voxel centre (cudaSiddon.cu:20-115):
+// plane crossings advanced from a common a_min, midpoint density samples of
+// the border-mode trilinear density at (pos-start)/voxel, segments shorter
+// than 1e-3 cm skipped, 5000-iteration cap.
+__device__ float siddon_rpl(const EeParams& P, f3 vox, f3 src, bool& iter_cap) {
+    const f3 start = mk(P.start[0], P.start[1], P.start[2]);
+    const f3 voxel = mk(P.voxel[0], P.voxel[1], P.voxel[2]);
+    const f3 end = mk(start.x + P.size[0] * voxel.x, start.y + P.size[1] * voxel.y, start.z + P.size[2] * voxel.z);
+    f3 diff = vox - src, sd = start - src, ed = end - src;
+    float afx = (sd.x - 0.5f * voxel.x) / diff.x, afy = (sd.y - 0.5f * voxel.y) / diff.y,
+          afz = (sd.z - 0.5f * voxel.z) / diff.z;
+    float alx = (ed.x + 0.5f * voxel.x) / diff.x, aly = (ed.y + 0.5f * voxel.y) / diff.y,
+          alz = (ed.z + 0.5f * voxel.z) / diff.z;
+    float a_min = fmaxf(0.f, fmaxf(fmaxf(fminf(afx, alx), fminf(afy, aly)), fminf(afz, alz)));
+    float a_max = fminf(1.f, fminf(fminf(fmaxf(afx, alx), fmaxf(afy, aly)), fmaxf(afz, alz)));
+    float rpl = 0.f;
+    if (!(a_min >= a_max)) {
+        float d12 = sqrtf(dot(diff, diff));
+        float stx = fabsf(voxel.x / diff.x), sty = fabsf(voxel.y / diff.y), stz = fabsf(voxel.z / diff.z);
+        float alpha = a_min, ax = a_min, ay = a_min, az = a_min, next = 0.f;
+        const float ivx = 1.f / voxel.x, ivy = 1.f / voxel.y, ivz = 1.f / voxel.z;
+        int iter = 0;
+        while (alpha < a_max && ++iter < 5000) {
+            bool vx = (ax >= 0.f && ax < 1.f), vy = (ay >= 0.f && ay < 1.f), vz = (az >= 0.f && az < 1.f);
+            if (!(vx || vy || vz)) break;
+            if (vx && (!vy || ax <= ay) && (!vz || ax <= az)) { next = ax; ax += stx; }
+            if (vy && (!vx || ay <= ax) && (!vz || ay <= az)) { next = ay; ay += sty; }
+            if (vz && (!vx || az <= ax) && (!vy || az <= ay)) { next = az; az += stz; }
+            float isect = fabsf(d12 * (next - alpha));
+            if (isect >= 0.001f) {
+                float mid = (next + alpha) * 0.5f;
+                float fx = (src.x + mid * diff.x - start.x) * ivx;
+                float fy = (src.y + mid * diff.y - start.y) * ivy;
+                float fz = (src.z + mid * diff.z - start.z) * ivz;
+                rpl += isect * tri_border(P.density, P.size[0], P.size[1], P.size[2], fx - 0.5f, fy - 0.5f, fz - 0.5f);
+            }
+            alpha = next;
+        }
+        if (iter >= 5000) iter_cap = true;
+    }
+    return rpl;
+}
+
+// Beamlet under this voxel (cudaSiddon.cu:143-165), -1 if none.
+__device__ __forceinline__ int beamlet_of(const EeBeamSpec& S, f3 vox) {
+    f3 src = ld3(S.src), nd = ld3(S.dir);
+    f3 diff = vox - src;
+    float pl = dot(diff, nd);
+    f3 proj = nd * pl;
+    f3 rej = diff - proj;
+    float rl = sqrtf(dot(rej, rej));
+    if (!(rl > 0.f)) return -1;  // normalize(0) is NaN in the reference: no fluence
+    float trad = rl * fabsf(S.isodist / sqrtf(dot(proj, proj)));
+    f3 pf = rej * (trad / rl);
+    f3 pb = mv(S.MB, pf);
+    float fx = pb.x / S.beamlet[0] + S.fmap[0] * 0.5f;
+    float fz = pb.z / S.beamlet[1] + S.fmap[1] * 0.5f;
+    if (!(fx >= 0.f && fx < (float)S.fmap[0] && fz >= 0.f && fz < (float)S.fmap[1])) return -1;
+    int idx = (int)floorf(fx) + S.fmap[0] * (int)floorf(fz);
+    if (idx < 0 || idx >= S.fmap[0] * S.fmap[1]) return -1;
+    return idx;
+}
+
+__device__ __forceinline__ float terma_per_fluence(const EeParams& P, float rpl, f3 vox, f3 src, float sad) {
+    float tsum = 0.f;
+    for (int e = 0; e < P.nE; e++) {
+        float mu = P.sp_mu[e];
+        tsum += P.sp_fluence[e] * P.sp_energy[e] * mu * expf(-mu * rpl);
+    }
+    f3 d = vox - src;
+    return tsum * (sad * sad) / dot(d, d);
+}
+
+__global__ void __launch_bounds__(256) k_terma(EeParams P, const EeBeamSpec* __restrict__ specs,
+                                               EeBeamGeom* __restrict__ geoms, const float* __restrict__ fluence,
+                                               float* __restrict__ terma, float* __restrict__ unit, int* __restrict__ bl_idx,
+                                               long long nbbox) {
+    const int b = blockIdx.z;
+    const EeBeamSpec& S = specs[b];
+    long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    bool nz = false, cap = false;
+    f3 bi = mk(0.f, 0.f, 0.f);
+    if (v < nbbox) {
+        int x = (int)(v % P.bbs[0]);
+        int y = (int)((v / P.bbs[0]) % P.bbs[1]);
+        int z = (int)(v / ((long long)P.bbs[0] * P.bbs[1]));
+        f3 vox = mk(P.start[0] + (P.bb0[0] + x) * P.voxel[0], P.start[1] + (P.bb0[1] + y) * P.voxel[1],
+                    P.start[2] + (P.bb0[2] + z) * P.voxel[2]);
+        f3 src = ld3(S.src);
+        int bl = beamlet_of(S, vox);
+        float t = 0.f, u = 0.f;
+        if (bl >= 0) {
+            float fl = __ldg(fluence + S.fl_off + bl);
+            if (fl > 0.f || unit) {
+                float rpl = siddon_rpl(P, vox, src, cap);
+                u = terma_per_fluence(P, rpl, vox, src, S.sad);
+                if (fl > 0.f) t = fl * u;
+            }
+        }
+        terma[(long long)b * nbbox + v] = t;
+        if (unit) unit[(long long)b * nbbox + v] = u;
+        if (bl_idx) bl_idx[(long long)b * nbbox + v] = bl;
+        if (t != 0.f) {
+            nz = true;
+            bi = mv(S.MB, mk((float)x, (float)y, (float)z));
+        }
+    }
+    // crop-box reduction (host.cu:442-459): min/max of BEV indices of voxels
+    // with non-zero TERMA, as ordered-int keys.
+    int kmin0 = nz ? f2key(bi.x) : INT_MAX, kmin1 = nz ? f2key(bi.y) : INT_MAX, kmin2 = nz ? f2key(bi.z) : INT_MAX;
+    int kmax0 = nz ? f2key(bi.x) : INT_MIN, kmax1 = nz ? f2key(bi.y) : INT_MIN, kmax2 = nz ? f2key(bi.z) : INT_MIN;
+    unsigned cnt = __popc(__ballot_sync(FULL, nz));
+    bool anycap = __any_sync(FULL, cap);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        kmin0 = min(kmin0, __shfl_xor_sync(FULL, kmin0, o));
+        kmin1 = min(kmin1, __shfl_xor_sync(FULL, kmin1, o));
+        kmin2 = min(kmin2, __shfl_xor_sync(FULL, kmin2, o));
+        kmax0 = max(kmax0, __shfl_xor_sync(FULL, kmax0, o));
+        kmax1 = max(kmax1, __shfl_xor_sync(FULL, kmax1, o));
+        kmax2 = max(kmax2, __shfl_xor_sync(FULL, kmax2, o));
+    }
+    __shared__ int sred[8][8];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) {
+        sred[w][0] = kmin0; sred[w][1] = kmin1; sred[w][2] = kmin2;
+        sred[w][3] = kmax0; sred[w][4] = kmax1; sred[w][5] = kmax2;
+        sred[w][6] = (int)cnt; sred[w][7] = anycap ? 1 : 0;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int r[8] = {INT_MAX, INT_MAX, INT_MAX, INT_MIN, INT_MIN, INT_MIN, 0, 0};
+        for (int i = 0; i < (int)(blockDim.x >> 5); i++) {
+            for (int a = 0; a < 3; a++) { r[a] = min(r[a], sred[i][a]); r[3 + a] = max(r[3 + a], sred[i][3 + a]); }
+            r[6] += sred[i][6];
+            r[7] |= sred[i][7];
+        }
+        EeBeamGeom& G = geoms[b];
+        if (r[6] > 0) {
+            for (int a = 0; a < 3; a++) { atomicMin(&G.key_min[a], r[a]); atomicMax(&G.key_max[a], r[3 + a]); }
+            atomicAdd(&G.nnz, (unsigned)r[6]);
+        }
+        if (r[7]) atomicExch(&G.status, 7 /* EE_ERR_SIDDON_ITER */);
+    }
+}
+
+__global__ void k_geom_init(EeBeamGeom* g, int n) {
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= n) return;
+    for (int a = 0; a < 3; a++) { g[b].key_min[a] = f2key(FLT_MAX); g[b].key_max[a] = f2key(FLT_MIN); }
+    g[b].nnz = 0;
+    g[b].status = 0;
+}
+
+// ------------------------------------------------------------- geometry --
+// Crop box (host.cu:460-499) and findREV (host.cu:75-155) for every cone.
+__global__ void k_geometry(EeParams P, const EeBeamSpec* __restrict__ specs, EeBeamGeom* __restrict__ geoms) {
+    const int b = blockIdx.x;
+    EeBeamGeom& G = geoms[b];
+    const EeBeamSpec& S = specs[b];
+    __shared__ int s_ok;
+    if (threadIdx.x == 0) {
+        int ok = (G.status == 0);
+        if (ok && G.nnz == 0) { G.status = 3; ok = 0; }
+        if (ok) {
+            float pl = P.penumbra / P.lat, plg = P.penumbra / P.lng;
+            float mn[3], mx[3];
+            for (int a = 0; a < 3; a++) { mn[a] = key2f(G.key_min[a]); mx[a] = key2f(G.key_max[a]); }
+            mn[0] -= pl; mn[1] -= plg; mn[2] -= pl;
+            mx[0] += pl; mx[1] += plg; mx[2] += pl;
+            for (int a = 0; a < 3; a++) {
+                float s = ceilf(fabsf(mx[a] - mn[a]));
+                if (!(s > 0.f) || s >= 1000.f) { ok = 0; }
+                G.bev[a] = ok ? (int)s : 0;
+                G.bmin[a] = mn[a];
+            }
+            if (!ok) G.status = 3;
+            f3 tmn = mv(S.MBi, mk(mn[0], mn[1], mn[2]));
+            G.lim_min[0] = P.start[0] + (tmn.x + P.bb0[0]) * P.voxel[0];
+            G.lim_min[1] = P.start[1] + (tmn.y + P.bb0[1]) * P.voxel[1];
+            G.lim_min[2] = P.start[2] + (tmn.z + P.bb0[2]) * P.voxel[2];
+            for (int a = 0; a < 3; a++) G.lim_off[a] = (G.lim_min[a] - P.start[a]) / P.voxel[a];
+            G.v_beam = (long long)G.bev[0] * G.bev[1] * G.bev[2];
+        }
+        s_ok = ok;
+    }
+    __syncthreads();
+    if (!s_ok) return;
+    const f3 bd = mk(G.bev[0] * P.lat, G.bev[1] * P.lng, G.bev[2] * P.lat);
+    for (int r = threadIdx.x; r < P.nrays; r += blockDim.x) {
+        const EeRayConst& RC = P.rays[r];
+        EeRayGeom& R = G.ray[r];
+        float mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, mx[3] = {FLT_MIN, FLT_MIN, FLT_MIN};
+        for (int c = 0; c < 8; c++) {
+            f3 o = mv(RC.MK, mk(bd.x * (c & 1), bd.y * ((c >> 1) & 1), bd.z * ((c >> 2) & 1)));
+            mn[0] = fminf(mn[0], o.x); mn[1] = fminf(mn[1], o.y); mn[2] = fminf(mn[2], o.z);
+            mx[0] = fmaxf(mx[0], o.x); mx[1] = fmaxf(mx[1], o.y); mx[2] = fmaxf(mx[2], o.z);
+        }
+        int sz[3] = {(int)ceilf(fabsf(mx[1] - mn[1]) / P.lng), (int)ceilf(fabsf(mx[2] - mn[2]) / P.lat),
+                     (int)ceilf(fabsf(mx[0] - mn[0]) / P.lat)};
+        bool bad = false;
+        for (int a = 0; a < 3; a++) {
+            if (P.max_rev[a] > 0 && sz[a] > P.max_rev[a]) bad = true;
+            R.rev[a] = sz[a];
+        }
+        if (sz[0] > EE_MAX_LINE || sz[0] <= 0 || sz[1] <= 0 || sz[2] <= 0) bad = true;
+        if (bad) atomicExch(&G.status, 4);
+        R.nlines = sz[1] * sz[2];
+        f3 q0 = mk(mn[0] / P.lat, mn[1] / P.lng, mn[2] / P.lat);
+        R.q0[0] = q0.x; R.q0[1] = q0.y; R.q0[2] = q0.z;
+        // REV vector (tZ, tX, tY) + q0 -> BEV (inverseRotateKernel)
+        f3 B0 = mv(RC.MKi, q0);
+        f3 Bx = mk(RC.MKi[1], RC.MKi[4], RC.MKi[7]);  // column for tX (REV y)
+        f3 By = mk(RC.MKi[2], RC.MKi[5], RC.MKi[8]);  // column for tY (REV z)
+        f3 Bz = mk(RC.MKi[0], RC.MKi[3], RC.MKi[6]);  // column for tZ (REV x)
+        f3 lo = mk(G.lim_off[0], G.lim_off[1], G.lim_off[2]);
+        f3 G0 = lo + mv(S.MBi, B0), Gx = mv(S.MBi, Bx), Gy = mv(S.MBi, By), Gz = mv(S.MBi, Bz);
+        R.B0[0] = B0.x; R.B0[1] = B0.y; R.B0[2] = B0.z;
+        R.Bx[0] = Bx.x; R.Bx[1] = Bx.y; R.Bx[2] = Bx.z;
+        R.By[0] = By.x; R.By[1] = By.y; R.By[2] = By.z;
+        R.Bz[0] = Bz.x; R.Bz[1] = Bz.y; R.Bz[2] = Bz.z;
+        R.G0[0] = G0.x; R.G0[1] = G0.y; R.G0[2] = G0.z;
+        R.Gx[0] = Gx.x; R.Gx[1] = Gx.y; R.Gx[2] = Gx.z;
+        R.Gy[0] = Gy.x; R.Gy[1] = Gy.y; R.Gy[2] = Gy.z;
+        R.Gz[0] = Gz.x; R.Gz[1] = Gz.y; R.Gz[2] = Gz.z;
+        for (int i = 0; i < 9; i++) R.M[i] = RC.MK[i];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && G.status == 0) {
+        long long off = 0;
+        int ml = 0, mls = 0;
+        for (int r = 0; r < P.nrays; r++) {
+            G.ray[r].offset = off;
+            off += (long long)G.ray[r].rev[0] * G.ray[r].nlines;
+            ml = max(ml, G.ray[r].rev[0]);
+            mls = max(mls, G.ray[r].nlines);
+        }
+        G.rev_total = off;
+        G.max_line = ml;
+        G.max_lines = mls;
+        if (G.arena_cap > 0 && off > G.arena_cap) G.status = 8;
+    }
+}
+
+
+// ------------------------------------------------------- cone: gather ----
+// REV resample of one line into shared memory (device.cu:47-79): density
+// sentinel -3 outside the BEV crop box, -2 outside the calc bbox; TERMA is
+// zero at sentinel samples (never written by the reference).
+__device__ __forceinline__ void gather_line(const EeParams& P, const EeBeamGeom& G, const EeRayGeom& R,
+                                            const float* __restrict__ terma_b, int tY, int tZ, int L, int lane,
+                                            float* rho, float* T) {
+    const f3 bl = ld3(R.B0) + ld3(R.By) * (float)tY + ld3(R.Bz) * (float)tZ;
+    const f3 gl = ld3(R.G0) + ld3(R.Gy) * (float)tY + ld3(R.Gz) * (float)tZ;
+    const f3 bx = ld3(R.Bx), gx = ld3(R.Gx);
+    const float bsx = (float)G.bev[0], bsy = (float)G.bev[1], bsz = (float)G.bev[2];
+    const float b0x = (float)P.bb0[0], b0y = (float)P.bb0[1], b0z = (float)P.bb0[2];
+    const float b1x = (float)(P.bb0[0] + P.bbs[0]), b1y = (float)(P.bb0[1] + P.bbs[1]), b1z = (float)(P.bb0[2] + P.bbs[2]);
+    for (int i = lane; i < L; i += 32) {
+        f3 bev = bl + bx * (float)i;
+        float r = -3.f, t = 0.f;
+        if (!(bev.x < 0.f || bev.y < 0.f || bev.z < 0.f || bev.x >= bsx || bev.y >= bsy || bev.z >= bsz)) {
+            f3 g = gl + gx * (float)i;
+            if (g.x < b0x || g.x >= b1x || g.y < b0y || g.y >= b1y || g.z < b0z || g.z >= b1z) {
+                r = -2.f;
+            } else {
+                r = tri_border(P.density, P.size[0], P.size[1], P.size[2], g.x, g.y, g.z);
+                if (terma_b) t = tri_border(terma_b, P.bbs[0], P.bbs[1], P.bbs[2], g.x - b0x, g.y - b0y, g.z - b0z);
+            }
+        }
+        rho[i] = r;
+        if (T) T[i] = t;
+    }
+}
+
+// --------------------------------------------------- cone: exp scans -----
+// Collapsed-cone line convolution with K(r) = A/a (1-e^{-ar}) + B/b (1-e^{-br})
+// on the reference discretisation (device.cu:140-211: no self term, radii
+// measured from the receiving voxel's boundary to the source voxel's centre):
+//   D_i = sum_c A_c/a_c [ Y_i + T_{i-1} (1 - h_{i-1}) ],
+//   Y_{i+1} = h_i^2 Y_i + T_{i-1} h_i (1 - h_{i-1} h_i),  h_j = e^{-a p_j/2},
+// evaluated as a warp-shuffle inclusive scan of the affine maps
+// Y -> F Y + U over 32-sample tiles with a carried Y.  p = delr*rho, p = T = 0
+// at sentinel samples.  FWD walks ascending i (contributions from k < i).
+template <bool FWD>
+__device__ __forceinline__ void line_scan(const float* rho, const float* T, int L, int lane, float delr,
+                                          const float* prm, float* D, float* out, float inv_nphi) {
+    const float A1 = prm[0], a1 = prm[1], A2 = prm[2], a2 = prm[3];
+    const float c1 = A1 / a1, c2 = A2 / a2;
+    float Y1 = 0.f, Y2 = 0.f;
+    const int ntiles = (L + 31) >> 5;
+    for (int tile = 0; tile < ntiles; tile++) {
+        const int n = (tile << 5) + lane;
+        const int i = FWD ? n : (L - 1 - n);
+        const int im = FWD ? i - 1 : i + 1;  // previous sample in walk order
+        float p = 0.f, t = 0.f, pm = 0.f, tm = 0.f;
+        bool valid = false;
+        if (n < L) {
+            float r = rho[i];
+            valid = r >= 0.f;
+            if (valid) { p = delr * r; t = T[i]; }
+            if (n > 0) {
+                float rm = rho[im];
+                if (rm >= 0.f) { pm = delr * rm; tm = T[im]; }
+            }
+        }
+        float h1 = __expf(-0.5f * a1 * p), hm1 = __expf(-0.5f * a1 * pm);
+        float h2 = __expf(-0.5f * a2 * p), hm2 = __expf(-0.5f * a2 * pm);
+        float F1 = h1 * h1, U1 = tm * h1 * (1.f - hm1 * h1);
+        float F2 = h2 * h2, U2 = tm * h2 * (1.f - hm2 * h2);
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            float fF1 = __shfl_up_sync(FULL, F1, off), fU1 = __shfl_up_sync(FULL, U1, off);
+            float fF2 = __shfl_up_sync(FULL, F2, off), fU2 = __shfl_up_sync(FULL, U2, off);
+            if (lane >= off) {
+                U1 = fmaf(F1, fU1, U1); F1 *= fF1;
+                U2 = fmaf(F2, fU2, U2); F2 *= fF2;
+            }
+        }
+        float Ya1 = fmaf(F1, Y1, U1), Ya2 = fmaf(F2, Y2, U2);
+        float Yb1 = __shfl_up_sync(FULL, Ya1, 1), Yb2 = __shfl_up_sync(FULL, Ya2, 1);
+        if (lane == 0) { Yb1 = Y1; Yb2 = Y2; }
+        float d = c1 * (Yb1 + tm * (1.f - hm1)) + c2 * (Yb2 + tm * (1.f - hm2));
+        if (n < L) {
+            if (FWD) D[i] = d;
+            else out[i] = valid ? (D[i] + d) * inv_nphi : 0.f;
+        }
+        Y1 = __shfl_sync(FULL, Ya1, 31);
+        Y2 = __shfl_sync(FULL, Ya2, 31);
+    }
+}
+
+// Transpose of line_scan<FWD> for the terma adjoint: with g_i the incoming
+// REV-dose gradient (already / nphi, zero at sentinels),
+//   Z_i = c g_i + h_i^2 Z_{i+1}   (walking opposite to FWD),
+//   Tbar_{i-1} += c g_i (1 - h_{i-1}) + Z_{i+1} h_i (1 - h_{i-1} h_i).
+template <bool FWD>
+__device__ __forceinline__ void line_scan_T(const float* rho, const float* g, int L, int lane, float delr,
+                                            const float* prm, float* Tb) {
+    const float A1 = prm[0], a1 = prm[1], A2 = prm[2], a2 = prm[3];
+    const float c1 = A1 / a1, c2 = A2 / a2;
+    float Z1 = 0.f, Z2 = 0.f;
+    const int ntiles = (L + 31) >> 5;
+    for (int tile = 0; tile < ntiles; tile++) {
+        const int n = (tile << 5) + lane;
+        // adjoint walk runs opposite to the forward walk
+        const int i = FWD ? (L - 1 - n) : n;
+        const int im = FWD ? i - 1 : i + 1;  // the forward walk's previous sample
+        float p = 0.f, gi = 0.f, pm = 0.f;
+        bool has_m = false;
+        if (n < L) {
+            float r = rho[i];
+            if (r >= 0.f) { p = delr * r; gi = g[i]; }
+            if (im >= 0 && im < L) {
+                float rm = rho[im];
+                if (rm >= 0.f) { pm = delr * rm; has_m = true; }
+            }
+        }
+        float h1 = __expf(-0.5f * a1 * p), hm1 = __expf(-0.5f * a1 * pm);
+        float h2 = __expf(-0.5f * a2 * p), hm2 = __expf(-0.5f * a2 * pm);
+        float F1 = h1 * h1, U1 = c1 * gi;
+        float F2 = h2 * h2, U2 = c2 * gi;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            float fF1 = __shfl_up_sync(FULL, F1, off), fU1 = __shfl_up_sync(FULL, U1, off);
+            float fF2 = __shfl_up_sync(FULL, F2, off), fU2 = __shfl_up_sync(FULL, U2, off);
+            if (lane >= off) {
+                U1 = fmaf(F1, fU1, U1); F1 *= fF1;
+                U2 = fmaf(F2, fU2, U2); F2 *= fF2;
+            }
+        }
+        float Za1 = fmaf(F1, Z1, U1), Za2 = fmaf(F2, Z2, U2);  // Z_i
+        float Zb1 = __shfl_up_sync(FULL, Za1, 1), Zb2 = __shfl_up_sync(FULL, Za2, 1);  // Z_{i+1}
+        if (lane == 0) { Zb1 = Z1; Zb2 = Z2; }
+        if (n < L && has_m) {
+            float v = c1 * gi * (1.f - hm1) + Zb1 * h1 * (1.f - hm1 * h1) + c2 * gi * (1.f - hm2) +
+                      Zb2 * h2 * (1.f - hm2 * h2);
+            Tb[im] += v;  // unique im per lane within a pass
+        }
+        Z1 = __shfl_sync(FULL, Za1, 31);
+        Z2 = __shfl_sync(FULL, Za2, 31);
+    }
+}
+
+// --------------------------------------------------- cone: table walk ----
+// RowConvolve walk (device.cu:126-211) over shared memory with exact FP32
+// linear interpolation of the cumulative kernel between radial boundaries.
+// coef == nullptr: returns sum_k w_k T_k; otherwise adds w_k * gscale into
+// coef[k] with shared-memory atomics (adjoint).
+__device__ __forceinline__ float table_walk(const float* rho, const float* T, int L, int i, int step, const float* K,
+                                            const float* RAD, int nr, float delr, float* coef, float gscale) {
+    float sum = 0.f, r_eff = 0.f, cumval = 0.f, last_cumval = 0.f, last_rad = 0.f, next_rad = RAD[0];
+    int rad_start = 0, k1 = i;
+    do {
+        k1 += step;
+        if (k1 < 0 || k1 >= L) break;
+        float de = delr * rho[k1];
+        r_eff += 0.5f * de;
+        if (r_eff > RAD[nr - 1]) break;
+        while (next_rad < r_eff) {
+            if (rad_start == nr - 1) break;
+            last_rad = next_rad;
+            next_rad = RAD[++rad_start];
+        }
+        float interp = (r_eff - last_rad) / (next_rad - last_rad);
+        if (rad_start == 0) cumval = interp * K[0];
+        else cumval = K[rad_start - 1] + interp * (K[rad_start] - K[rad_start - 1]);
+        float w = cumval - last_cumval;
+        if (coef) atomicAdd(coef + k1, w * gscale);
+        else sum += w * T[k1];
+        last_cumval = cumval;
+        r_eff += 0.5f * de;
+    } while (rad_start < nr - 1);
+    return sum;
+}
+
+// ------------------------------------------------------- cone kernels ----
+constexpr int CONE_WARPS = 4;
+
+__global__ void __launch_bounds__(CONE_WARPS * 32) k_cone(EeParams P, const EeBeamGeom* __restrict__ geoms,
+                                                          const float* __restrict__ terma, float* __restrict__ rev,
+                                                          long long nbbox, int maxL) {
+    extern __shared__ float sm[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int ray = blockIdx.y, b = blockIdx.z;
+    const EeBeamGeom& G = geoms[b];
+    float* tabK = sm + (size_t)CONE_WARPS * 3 * maxL;  // [2][nradii] kernel rows + radii
+    float* tabR = tabK + 2 * EE_MAX_RADII;
+    if (P.mode == 0) {
+        const EeRayConst& RC = P.rays[ray];
+        for (int k = threadIdx.x; k < P.nradii; k += blockDim.x) {
+            tabK[k] = P.cumkern[RC.row_fwd * P.nradii + k];
+            tabK[EE_MAX_RADII + k] = P.cumkern[RC.row_rev * P.nradii + k];
+            tabR[k] = P.radii[k];
+        }
+        __syncthreads();
+    }
+    if (G.status != 0) return;
+    const EeRayGeom& R = G.ray[ray];
+    const int line = blockIdx.x * CONE_WARPS + warp;
+    if (line >= R.nlines) return;
+    const int L = R.rev[0];
+    const int tY = line % R.rev[1], tZ = line / R.rev[1];
+    float* rho = sm + (size_t)warp * 3 * maxL;
+    float* T = rho + maxL;
+    float* D = T + maxL;
+    gather_line(P, G, R, terma + (long long)b * nbbox, tY, tZ, L, lane, rho, T);
+    __syncwarp();
+    float* out = rev + G.arena_off + R.offset + (long long)line * L;
+    const float inv_nphi = 1.f / (float)P.nphi;
+    const EeRayConst& RC = P.rays[ray];
+    if (P.mode == 1) {
+        line_scan<true>(rho, T, L, lane, P.lng, P.expp + 4 * RC.row_fwd, D, out, inv_nphi);
+        __syncwarp();
+        line_scan<false>(rho, T, L, lane, P.lng, P.expp + 4 * RC.row_rev, D, out, inv_nphi);
+    } else {
+        for (int i = lane; i < L; i += 32) {
+            float v = 0.f;
+            if (rho[i] >= 0.f) {
+                v = table_walk(rho, T, L, i, -1, tabK, tabR, P.nradii, P.lng, nullptr, 0.f);
+                v += table_walk(rho, T, L, i, +1, tabK + EE_MAX_RADII, tabR, P.nradii, P.lng, nullptr, 0.f);
+                v = __fdiv_rn(v, (float)P.nphi);
+            }
+            out[i] = v;
+        }
+    }
+}
+
+// Adjoint of k_cone followed by the transpose of the REV TERMA resample:
+// terma_grad (bbox grid) += R_T^T C^T rev_grad.
+__global__ void __launch_bounds__(CONE_WARPS * 32) k_cone_T(EeParams P, const EeBeamGeom* __restrict__ geoms,
+                                                            const float* __restrict__ rev_grad,
+                                                            float* __restrict__ terma_grad, long long nbbox, int maxL) {
+    extern __shared__ float sm[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int ray = blockIdx.y, b = blockIdx.z;
+    const EeBeamGeom& G = geoms[b];
+    float* tabK = sm + (size_t)CONE_WARPS * 3 * maxL;
+    float* tabR = tabK + 2 * EE_MAX_RADII;
+    if (P.mode == 0) {
+        const EeRayConst& RC = P.rays[ray];
+        for (int k = threadIdx.x; k < P.nradii; k += blockDim.x) {
+            tabK[k] = P.cumkern[RC.row_fwd * P.nradii + k];
+            tabK[EE_MAX_RADII + k] = P.cumkern[RC.row_rev * P.nradii + k];
+            tabR[k] = P.radii[k];
+        }
+        __syncthreads();
+    }
+    if (G.status != 0) return;
+    const EeRayGeom& R = G.ray[ray];
+    const int line = blockIdx.x * CONE_WARPS + warp;
+    if (line >= R.nlines) return;
+    const int L = R.rev[0];
+    const int tY = line % R.rev[1], tZ = line / R.rev[1];
+    float* rho = sm + (size_t)warp * 3 * maxL;
+    float* g = rho + maxL;
+    float* Tb = g + maxL;
+    gather_line(P, G, R, nullptr, tY, tZ, L, lane, rho, nullptr);
+    const float* gin = rev_grad + G.arena_off + R.offset + (long long)line * L;
+    const float inv_nphi = 1.f / (float)P.nphi;
+    for (int i = lane; i < L; i += 32) {
+        g[i] = rho[i] >= 0.f ? gin[i] * inv_nphi : 0.f;
+        Tb[i] = 0.f;
+    }
+    __syncwarp();
+    const EeRayConst& RC = P.rays[ray];
+    if (P.mode == 1) {
+        line_scan_T<true>(rho, g, L, lane, P.lng, P.expp + 4 * RC.row_fwd, Tb);
+        __syncwarp();
+        line_scan_T<false>(rho, g, L, lane, P.lng, P.expp + 4 * RC.row_rev, Tb);
+    } else {
+        for (int i = lane; i < L; i += 32) {
+            if (rho[i] >= 0.f && g[i] != 0.f) {
+                table_walk(rho, nullptr, L, i, -1, tabK, tabR, P.nradii, P.lng, Tb, g[i]);
+                table_walk(rho, nullptr, L, i, +1, tabK + EE_MAX_RADII, tabR, P.nradii, P.lng, Tb, g[i]);
+            }
+        }
+    }
+    __syncwarp();
+    // transpose of the REV TERMA resample
+    const f3 gl = ld3(R.G0) + ld3(R.Gy) * (float)tY + ld3(R.Gz) * (float)tZ;
+    const f3 gx = ld3(R.Gx);
+    float* tg = terma_grad + (long long)b * nbbox;
+    for (int i = lane; i < L; i += 32) {
+        float v = Tb[i];
+        if (rho[i] < 0.f || v == 0.f) continue;
+        f3 gp = gl + gx * (float)i;
+        tri_border_scatter(tg, P.bbs[0], P.bbs[1], P.bbs[2], gp.x - P.bb0[0], gp.y - P.bb0[1], gp.z - P.bb0[2], v);
+    }
+}
+
+// ------------------------------------------------------------- gather ----
+// REV2XYZdose (device.cu:222-261) for all cones at once.  The patient
+// voxel's BEV index b = MB (t - lim_off) is formed once per beam; voxels more
+// than 2 BEV voxels outside the crop box see only zero REV samples and skip
+// the cone loop.
+__device__ __forceinline__ float beam_voxel_dose(const EeParams& P, const EeBeamSpec& S, const EeBeamGeom& G,
+                                                 const float* __restrict__ rev, int x, int y, int z) {
+    f3 d = mk((float)x - G.lim_off[0], (float)y - G.lim_off[1], (float)z - G.lim_off[2]);
+    f3 bi = mv(S.MB, d);
+    if (bi.x < -2.f || bi.y < -2.f || bi.z < -2.f || bi.x > G.bev[0] + 2.f || bi.y > G.bev[1] + 2.f ||
+        bi.z > G.bev[2] + 2.f)
+        return 0.f;
+    float acc = 0.f;
+    const float* base = rev + G.arena_off;
+    for (int r = 0; r < P.nrays; r++) {
+        const EeRayGeom& R = G.ray[r];
+        f3 q = mv(R.M, bi) - ld3(R.q0);
+        // q.y along the line (rev[0]), q.z -> rev[1], q.x -> rev[2]
+        if (q.y >= (float)R.rev[0] || q.z >= (float)R.rev[1] || q.x >= (float)R.rev[2] || q.x < 0.f || q.y < 0.f ||
+            q.z < 0.f)
+            continue;
+        acc += tri_border(base + R.offset, R.rev[0], R.rev[1], R.rev[2], q.y, q.z, q.x);
+    }
+    return acc;
+}
+
+__global__ void __launch_bounds__(256) k_gather(EeParams P, const EeBeamSpec* __restrict__ specs,
+                                                const EeBeamGeom* __restrict__ geoms, const float* __restrict__ rev,
+                                                float* __restrict__ dose, int nbeams, int mode, long long nfull) {
+    long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nfull) return;
+    int x = (int)(v % P.size[0]);
+    int y = (int)((v / P.size[0]) % P.size[1]);
+    int z = (int)(v / ((long long)P.size[0] * P.size[1]));
+    bool inbb = x >= P.bb0[0] && x < P.bb0[0] + P.bbs[0] && y >= P.bb0[1] && y < P.bb0[1] + P.bbs[1] &&
+                z >= P.bb0[2] && z < P.bb0[2] + P.bbs[2];
+    if (mode == 2) {
+        int b = blockIdx.z;
+        float acc = 0.f;
+        if (inbb && geoms[b].status == 0) acc = beam_voxel_dose(P, specs[b], geoms[b], rev, x, y, z);
+        dose[(long long)b * nfull + v] = acc;
+        return;
+    }
+    float acc = 0.f;
+    if (inbb)
+        for (int b = 0; b < nbeams; b++)
+            if (geoms[b].status == 0) acc += beam_voxel_dose(P, specs[b], geoms[b], rev, x, y, z);
+    if (mode == 1) dose[v] += acc;
+    else dose[v] = acc;
+}
+
+// Transpose of beam_voxel_dose: rev_grad += S^T dose_grad (atomic scatter).
+__global__ void __launch_bounds__(256) k_gather_T(EeParams P, const EeBeamSpec* __restrict__ specs,
+                                                  const EeBeamGeom* __restrict__ geoms,
+                                                  const float* __restrict__ dose_grad, float* __restrict__ rev_grad,
+                                                  long long nbbox) {
+    long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int b = blockIdx.z;
+    if (v >= nbbox) return;
+    const EeBeamGeom& G = geoms[b];
+    if (G.status != 0) return;
+    int x = P.bb0[0] + (int)(v % P.bbs[0]);
+    int y = P.bb0[1] + (int)((v / P.bbs[0]) % P.bbs[1]);
+    int z = P.bb0[2] + (int)(v / ((long long)P.bbs[0] * P.bbs[1]));
+    float gd = dose_grad[x + (long long)P.size[0] * (y + (long long)P.size[1] * z)];
+    if (gd == 0.f) return;
+    const EeBeamSpec& S = specs[b];
+    f3 d = mk((float)x - G.lim_off[0], (float)y - G.lim_off[1], (float)z - G.lim_off[2]);
+    f3 bi = mv(S.MB, d);
+    if (bi.x < -2.f || bi.y < -2.f || bi.z < -2.f || bi.x > G.bev[0] + 2.f || bi.y > G.bev[1] + 2.f ||
+        bi.z > G.bev[2] + 2.f)
+        return;
+    float* base = rev_grad + G.arena_off;
+    for (int r = 0; r < P.nrays; r++) {
+        const EeRayGeom& R = G.ray[r];
+        f3 q = mv(R.M, bi) - ld3(R.q0);
+        if (q.y >= (float)R.rev[0] || q.z >= (float)R.rev[1] || q.x >= (float)R.rev[2] || q.x < 0.f || q.y < 0.f ||
+            q.z < 0.f)
+            continue;
+        tri_border_scatter(base + R.offset, R.rev[0], R.rev[1], R.rev[2], q.y, q.z, q.x, gd);
+    }
+}
+
+// TERMA adjoint: fluence_grad[beamlet(v)] += G_v * terma_grad[v], warp-
+// aggregated per beamlet index before the atomic.
+__global__ void __launch_bounds__(256) k_terma_T(EeParams P, const EeBeamSpec* __restrict__ specs,
+                                                 const float* __restrict__ unit, const int* __restrict__ bl_idx,
+                                                 const float* __restrict__ terma_grad, float* __restrict__ fluence_grad,
+                                                 long long nbbox) {
+    long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int b = blockIdx.z;
+    int bl = -1;
+    float val = 0.f;
+    if (v < nbbox) {
+        long long o = (long long)b * nbbox + v;
+        bl = bl_idx[o];
+        if (bl >= 0) val = unit[o] * terma_grad[o];
+    }
+    unsigned peers = __match_any_sync(FULL, bl);
+    int leader = __ffs(peers) - 1;
+    // sum val over lanes sharing bl (segmented by match mask)
+    float sum = 0.f;
+    for (unsigned m = peers; m; m &= m - 1) {
+        int src = __ffs(m) - 1;
+        sum += __shfl_sync(peers, val, src);
+    }
+    if ((int)(threadIdx.x & 31) == leader && bl >= 0 && sum != 0.f) atomicAdd(fluence_grad + specs[b].fl_off + bl, sum);
+}
+
+}  // namespace
+
+// ----------------------------------------------------------- launchers ---
+static inline unsigned grid1(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+cudaError_t ee_launch_geom_init(EeBeamGeom* g, int nbeams, cudaStream_t s) {
+    k_geom_init<<<grid1(nbeams, 128), 128, 0, s>>>(g, nbeams);
+    return cudaGetLastError();
+}
+
+cudaError_t ee_launch_terma(const EeParams& P, const EeBeamSpec* specs, EeBeamGeom* geoms, const float* fluence,
+                            float* terma, float* unit, int* beamlet_idx, int nbeams, cudaStream_t s) {
+    long long nbbox = (long long)P.bbs[0] * P.bbs[1] * P.bbs[2];
+    dim3 grid(grid1(nbbox, 256), 1, nbeams);
+    k_terma<<<grid, 256, 0, s>>>(P, specs, geoms, fluence, terma, unit, beamlet_idx, nbbox);
+    return cudaGetLastError();
+}
+
+cudaError_t ee_launch_geometry(const EeParams& P, const EeBeamSpec* specs, EeBeamGeom* geoms, int nbeams,
+                               cudaStream_t s) {
+    k_geometry<<<nbeams, 64, 0, s>>>(P, specs, geoms);
+    return cudaGetLastError();
+}
+
+static size_t cone_smem(int maxL) { return sizeof(float) * ((size_t)CONE_WARPS * 3 * maxL + 2 * EE_MAX_RADII + EE_MAX_RADII); }
+
+static cudaError_t cone_attr(const void* fn, size_t smem) {
+    if (smem > 48 * 1024) return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    return cudaSuccess;
+}
+
+cudaError_t ee_launch_cone(const EeParams& P, const EeBeamGeom* geoms, const float* terma, float* rev, int nbeams,
+                           int max_lines, int max_line, cudaStream_t s) {
+    long long nbbox = (long long)P.bbs[0] * P.bbs[1] * P.bbs[2];
+    size_t smem = cone_smem(max_line);
+    cudaError_t e = cone_attr((const void*)k_cone, smem);
+    if (e != cudaSuccess) return e;
+    dim3 grid(grid1(max_lines, CONE_WARPS), P.nrays, nbeams);
+    k_cone<<<grid, CONE_WARPS * 32, smem, s>>>(P, geoms, terma, rev, nbbox, max_line);
+    return cudaGetLastError();
+}
+
+cudaError_t ee_launch_gather(const EeParams& P, const EeBeamSpec* specs, const EeBeamGeom* geoms, const float* rev,
+                             float* dose, int nbeams, int dose_mode, cudaStream_t s) {
+    long long nfull = (long long)P.size[0] * P.size[1] * P.size[2];
+    dim3 grid(grid1(nfull, 256), 1, dose_mode == 2 ? nbeams : 1);
+    k_gather<<<grid, 256, 0, s>>>(P, specs, geoms, rev, dose, nbeams, dose_mode, nfull);
+    return cudaGetLastError();
+}
+
+cudaError_t ee_launch_gather_T(const EeParams& P, const EeBeamSpec* specs, const EeBeamGeom* geoms,
+                               const float* dose_grad, float* rev_grad, int nbeams, cudaStream_t s) {
+    long long nbbox = (long long)P.bbs[0] * P.bbs[1] * P.bbs[2];
+    dim3 grid(grid1(nbbox, 256), 1, nbeams);
+    k_gather_T<<<grid, 256, 0, s>>>(P, specs, geoms, dose_grad, rev_grad, nbbox);
+    return cudaGetLastError();
+}
+
+cudaError_t ee_launch_cone_T(const EeParams& P, const EeBeamGeom* geoms, const float* rev_grad, float* terma_grad,
+                             int nbeams, int max_lines, int max_line, cudaStream_t s) {
+    long long nbbox = (long long)P.bbs[0] * P.bbs[1] * P.bbs[2];
+    size_t smem = cone_smem(max_line);
+    cudaError_t e = cone_attr((const void*)k_cone_T, smem);
+    if (e != cudaSuccess) return e;
+    dim3 grid(grid1(max_lines, CONE_WARPS), P.nrays, nbeams);
+    k_cone_T<<<grid, CONE_WARPS * 32, smem, s>>>(P, geoms, rev_grad, terma_grad, nbbox, max_line);
+    return cudaGetLastError();
+}
+
+cudaError_t ee_launch_terma_T(const EeParams& P, const EeBeamSpec* specs, const EeBeamGeom* geoms,
+                              const float* unit_terma, const int* beamlet_idx, const float* terma_grad,
+                              float* fluence_grad, int nbeams, cudaStream_t s) {
+    (void)geoms;
+    long long nbbox = (long long)P.bbs[0] * P.bbs[1] * P.bbs[2];
+    dim3 grid(grid1(nbbox, 256), 1, nbeams);
+    k_terma_T<<<grid, 256, 0, s>>>(P, specs, unit_terma, beamlet_idx, terma_grad, fluence_grad, nbbox);
+    return cudaGetLastError();
+}

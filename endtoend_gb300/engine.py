@@ -1,0 +1,307 @@
+"""Python host binding of the CCCS engine's C ABI (include/ee_cccs.h).
+
+This is a thin ctypes layer: every computation runs in
+``endtoend_gb300/_lib/libee_cccs.so`` (hand-written sm_103a kernels).  There
+is no CPU fallback; constructing an :class:`Engine` without the built
+library raises.
+
+Exceptions mirror the reference's error behaviour
+(CCCS/dosecalc-beam/nvbbRayConvolve_host.cu): :class:`ArraySizeError` for REV
+arrays over their limit (``ArraySizeError``, host.cu:71-74,148-154 and the
+rev.x > 1024 runtime_error, host.cu:567) and :class:`CropBoxError` for an
+empty or oversized crop box (runtime_error, host.cu:494-498).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import List, Sequence
+
+import numpy as np
+
+from . import _build
+
+EE_OK = 0
+EE_ERR_INVALID_ARG = 1
+EE_ERR_CUDA = 2
+EE_ERR_CROPBOX = 3
+EE_ERR_REV_SIZE = 4
+EE_ERR_NOMEM = 5
+EE_ERR_NOT_READY = 6
+EE_ERR_SIDDON_ITER = 7
+EE_ERR_CAPACITY = 8
+
+KERNEL_TABLE = 0
+KERNEL_EXP = 1
+
+DOSE_SUM = 0
+DOSE_ACCUMULATE = 1
+DOSE_PER_BEAM = 2
+
+
+class EEError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"[ee status {code}] {msg}")
+        self.code = code
+
+
+class ArraySizeError(EEError):
+    pass
+
+
+class CropBoxError(EEError):
+    pass
+
+
+class NotReadyError(EEError):
+    pass
+
+
+class Frame(C.Structure):
+    _fields_ = [("size", C.c_int * 3), ("voxel", C.c_float * 3), ("start", C.c_float * 3),
+                ("bbox_start", C.c_int * 3), ("bbox_size", C.c_int * 3)]
+
+
+class ConvParams(C.Structure):
+    _fields_ = [("ntheta", C.c_int), ("nphi", C.c_int), ("nradii", C.c_int),
+                ("rev_latspacing", C.c_float), ("rev_longspacing", C.c_float), ("penumbra", C.c_float),
+                ("max_rev_size", C.c_int * 3)]
+
+
+class EEBeam(C.Structure):
+    _fields_ = [("azimuth", C.c_float), ("zenith", C.c_float), ("coll", C.c_float),
+                ("isocenter", C.c_float * 3), ("sad", C.c_float),
+                ("fmap_size", C.c_int * 2), ("beamlet_size", C.c_float * 2)]
+
+
+class BeamInfo(C.Structure):
+    _fields_ = [("source", C.c_float * 3), ("direction", C.c_float * 3), ("b_min", C.c_float * 3),
+                ("bev_size", C.c_int * 3), ("lim_min", C.c_float * 3), ("v_beam", C.c_longlong),
+                ("rev_samples", C.c_longlong), ("terma_nonzero", C.c_longlong), ("max_line", C.c_int),
+                ("status", C.c_int)]
+
+
+# every symbol include/ee_cccs.h declares, with its ctypes signature
+_SIGS = {
+    "ee_create": (C.c_int, [C.c_int, C.POINTER(C.c_void_p)]),
+    "ee_destroy": (C.c_int, [C.c_void_p]),
+    "ee_last_error": (C.c_char_p, []),
+    "ee_abi_version": (C.c_int, []),
+    "ee_set_volume": (C.c_int, [C.c_void_p, C.POINTER(Frame), C.c_void_p]),
+    "ee_set_spectrum": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "ee_set_kernel_table": (C.c_int, [C.c_void_p, C.POINTER(ConvParams), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "ee_set_kernel_exp": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "ee_set_kernel_mode": (C.c_int, [C.c_void_p, C.c_int]),
+    "ee_beam_dose": (C.c_int, [C.c_void_p, C.POINTER(EEBeam), C.c_int, C.c_void_p, C.c_void_p, C.c_int]),
+    "ee_beam_dose_device": (C.c_int, [C.c_void_p, C.POINTER(EEBeam), C.c_int, C.c_void_p, C.c_void_p, C.c_int]),
+    "ee_beam_dose_adjoint": (C.c_int, [C.c_void_p, C.POINTER(EEBeam), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "ee_beam_dose_adjoint_device": (C.c_int, [C.c_void_p, C.POINTER(EEBeam), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "ee_get_beam_info": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(BeamInfo)]),
+    "ee_synchronize": (C.c_int, [C.c_void_p]),
+    "ee_get_stream": (C.c_void_p, [C.c_void_p]),
+    "ee_beam_source": (C.c_int, [C.POINTER(EEBeam), C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "ee_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
+    "ee_read_profile": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_longlong), C.c_int]),
+}
+
+STAGES = ["terma", "geometry", "cone", "gather", "gather_T", "cone_T", "terma_T"]
+
+_LIB = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load_library(build_if_missing: bool = False):
+    """Load libee_cccs.so (raises if it is not built)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = _build.LIB
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise ImportError(f"CCCS engine library not built ({path}); run endtoend_gb300._build.build()")
+        _build.build()
+    lib = C.CDLL(path)
+    for name, (res, args) in _SIGS.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _LIB = lib
+    return lib
+
+
+def _ptr(a: np.ndarray):
+    return C.c_void_p(a.ctypes.data)
+
+
+def to_ee_beams(beams) -> "C.Array":
+    arr = (EEBeam * len(beams))()
+    for i, b in enumerate(beams):
+        e = arr[i]
+        e.azimuth, e.zenith, e.coll = float(b.azimuth), float(b.zenith), float(b.coll)
+        e.isocenter[:] = [float(v) for v in b.isocenter]
+        e.sad = float(b.sad)
+        e.fmap_size[:] = [int(v) for v in b.fmap_size]
+        e.beamlet_size[:] = [float(v) for v in b.beamlet_size]
+    return arr
+
+
+def concat_fluence(beams) -> np.ndarray:
+    return np.ascontiguousarray(np.concatenate([np.asarray(b.fluence, np.float32).ravel() for b in beams]))
+
+
+class Engine:
+    """One engine context on one GPU (device-resident density, spectrum and
+    kernel; reusable scratch).  Mirrors the reference call sequence
+    initCudaConstandTex -> radconvolveTexture -> cuda_sum_device_float_dose
+    -> freeCudaTexture as set_* -> beam_dose -> close."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load_library()
+        h = C.c_void_p()
+        self._check(self.lib.ee_create(int(device), C.byref(h)))
+        self.h = h
+        self.vol = None
+        self.phys = None
+
+    # -- errors
+    def _check(self, st):
+        if st == EE_OK:
+            return
+        msg = self.lib.ee_last_error().decode(errors="replace")
+        cls = {EE_ERR_REV_SIZE: ArraySizeError, EE_ERR_CROPBOX: CropBoxError,
+               EE_ERR_NOT_READY: NotReadyError}.get(st, EEError)
+        raise cls(st, msg)
+
+    # -- set-up
+    def set_volume(self, vol):
+        f = Frame()
+        f.size[:] = [int(v) for v in vol.size]
+        f.voxel[:] = [float(v) for v in vol.voxel]
+        f.start[:] = [float(v) for v in vol.start]
+        f.bbox_start[:] = [int(v) for v in vol.bbox_start]
+        f.bbox_size[:] = [int(v) for v in vol.bbox_size]
+        d = np.ascontiguousarray(vol.density, dtype=np.float32)
+        self._check(self.lib.ee_set_volume(self.h, C.byref(f), _ptr(d)))
+        self.vol = vol
+
+    def set_physics(self, phys, mode: str = "exp", max_rev_size=(0, 0, 0)):
+        f32 = lambda a: np.ascontiguousarray(np.asarray(a, dtype=np.float32))
+        E, fl, mu, muen = f32(phys.energy), f32(phys.fluence), f32(phys.mu), f32(phys.mu_en)
+        self._check(self.lib.ee_set_spectrum(self.h, len(E), _ptr(E), _ptr(fl), _ptr(mu), _ptr(muen)))
+        cp = ConvParams()
+        cp.ntheta, cp.nphi, cp.nradii = phys.ntheta, phys.nphi, phys.nradii
+        cp.rev_latspacing, cp.rev_longspacing, cp.penumbra = phys.rev_latspacing, phys.rev_longspacing, phys.penumbra
+        cp.max_rev_size[:] = list(max_rev_size)
+        radii, ck, th, ph = f32(phys.radii), f32(phys.cumkern), f32(phys.theta_deg), f32(phys.phi_deg)
+        self._check(self.lib.ee_set_kernel_table(self.h, C.byref(cp), _ptr(radii), _ptr(ck), _ptr(th), _ptr(ph)))
+        ep = f32(phys.exp_params)
+        self._check(self.lib.ee_set_kernel_exp(self.h, _ptr(ep)))
+        self.set_mode(mode)
+        self.phys = phys
+
+    def set_mode(self, mode: str):
+        self._check(self.lib.ee_set_kernel_mode(self.h, KERNEL_EXP if mode == "exp" else KERNEL_TABLE))
+
+    # -- forward dose
+    def beam_dose(self, beams: Sequence, per_beam: bool = False, accumulate_into: np.ndarray = None) -> np.ndarray:
+        """Host buffers in and out (the end-to-end path)."""
+        nz, ny, nx = self.vol.density.shape
+        eb = to_ee_beams(beams)
+        fl = concat_fluence(beams)
+        if per_beam:
+            out = np.zeros((len(beams), nz, ny, nx), np.float32)
+            mode = DOSE_PER_BEAM
+        elif accumulate_into is not None:
+            out = accumulate_into
+            assert out.dtype == np.float32 and out.flags.c_contiguous and out.shape == (nz, ny, nx)
+            mode = DOSE_ACCUMULATE
+        else:
+            out = np.zeros((nz, ny, nx), np.float32)
+            mode = DOSE_SUM
+        self._check(self.lib.ee_beam_dose(self.h, eb, len(beams), _ptr(fl), _ptr(out), mode))
+        return out
+
+    def beam_dose_device(self, beams: Sequence, d_fluence: int, d_dose: int, mode: int = DOSE_SUM):
+        """Device pointers (e.g. torch tensor .data_ptr()); enqueued on the
+        engine stream (the call returns after the per-batch geometry read-back)."""
+        eb = to_ee_beams(beams)
+        self._check(self.lib.ee_beam_dose_device(self.h, eb, len(beams), C.c_void_p(d_fluence), C.c_void_p(d_dose), mode))
+
+    # -- adjoint
+    def beam_dose_adjoint(self, beams: Sequence, dose_grad: np.ndarray) -> List[np.ndarray]:
+        eb = to_ee_beams(beams)
+        fl = concat_fluence(beams)
+        g = np.ascontiguousarray(dose_grad, dtype=np.float32)
+        assert g.shape == self.vol.density.shape
+        out = np.zeros(fl.size, np.float32)
+        self._check(self.lib.ee_beam_dose_adjoint(self.h, eb, len(beams), _ptr(fl), _ptr(g), _ptr(out)))
+        res, o = [], 0
+        for b in beams:
+            n = int(b.fmap_size[0] * b.fmap_size[1])
+            res.append(out[o:o + n].reshape(b.fmap_size[1], b.fmap_size[0]))
+            o += n
+        return res
+
+    def beam_dose_adjoint_device(self, beams: Sequence, d_fluence: int, d_dose_grad: int, d_fluence_grad: int):
+        eb = to_ee_beams(beams)
+        self._check(self.lib.ee_beam_dose_adjoint_device(self.h, eb, len(beams), C.c_void_p(d_fluence),
+                                                         C.c_void_p(d_dose_grad), C.c_void_p(d_fluence_grad)))
+
+    # -- diagnostics
+    def beam_info(self, i: int) -> dict:
+        bi = BeamInfo()
+        self._check(self.lib.ee_get_beam_info(self.h, int(i), C.byref(bi)))
+        return {"source": list(bi.source), "direction": list(bi.direction), "b_min": list(bi.b_min),
+                "bev_size": list(bi.bev_size), "lim_min": list(bi.lim_min), "v_beam": bi.v_beam,
+                "rev_samples": bi.rev_samples, "terma_nonzero": bi.terma_nonzero, "max_line": bi.max_line,
+                "status": bi.status}
+
+    def set_profiling(self, on: bool = True):
+        self._check(self.lib.ee_set_profiling(self.h, 1 if on else 0))
+
+    def read_profile(self) -> dict:
+        """{stage: (ms, launches)} accumulated since the last read."""
+        n = len(STAGES)
+        ms = (C.c_double * n)()
+        nl = (C.c_longlong * n)()
+        self._check(self.lib.ee_read_profile(self.h, ms, nl, n))
+        return {s: (ms[i], nl[i]) for i, s in enumerate(STAGES)}
+
+    def synchronize(self):
+        self._check(self.lib.ee_synchronize(self.h))
+
+    @property
+    def stream(self) -> int:
+        return int(self.lib.ee_get_stream(self.h) or 0)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.ee_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+def beam_source(beam):
+    """Source position and direction of a beam (BEAM::reconfigure)."""
+    lib = load_library()
+    eb = to_ee_beams([beam])
+    s = (C.c_float * 3)()
+    d = (C.c_float * 3)()
+    st = lib.ee_beam_source(eb, s, d)
+    if st:
+        raise EEError(st, lib.ee_last_error().decode())
+    return np.array(list(s)), np.array(list(d))

@@ -1,0 +1,183 @@
+/*
+ * ee_cccs.h -- C ABI of the GB300 collapsed-cone convolution/superposition
+ * (CCCS) beam-dose engine.
+ *
+ * Plain C types only: pointers, sizes, POD structs.  Every entry point
+ * returns an ee_status (0 = success); ee_last_error() gives the message of
+ * the calling thread's last failure.  Nothing here calls exit().
+ *
+ * Units: centimetres for lengths, radians for beam angles (VarianIEC:
+ * azimuth = gantry, zenith = couch, coll = collimator), degrees for the
+ * convolution-cone angles, g/cc for density.  Volumes are x-fastest
+ * [size[2]][size[1]][size[0]] float32 arrays; `start` is the centre of voxel
+ * (0,0,0).
+ *
+ * Reference interfaces replaced (paths within the reference checkout):
+ *   ee_create/ee_set_volume/ee_set_spectrum/ee_set_kernel_table/
+ *   ee_set_kernel_exp   <- initCudaConstandTex
+ *                          CCCS/dosecalc-beam/nvbbRayConvolve_host.cu:159
+ *   ee_beam_dose        <- radconvolveTexture + cuda_sum_device_float_dose
+ *                          CCCS/dosecalc-beam/nvbbRayConvolve_host.cu:297,775
+ *   ee_destroy          <- freeCudaTexture
+ *                          CCCS/dosecalc-beam/nvbbRayConvolve_host.cu:746
+ *   ee_beam_dose_adjoint, ee_loss_and_grad
+ *                       <- the EndtoEnd fluence-gradient call (README.md:15-22,
+ *                          source not in the reference snapshot)
+ */
+#ifndef EE_CCCS_H
+#define EE_CCCS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EE_ABI_VERSION 1
+
+typedef enum {
+    EE_OK = 0,
+    EE_ERR_INVALID_ARG = 1,   /* bad pointer / size / order of calls            */
+    EE_ERR_CUDA = 2,          /* a CUDA runtime call failed (message has it)    */
+    EE_ERR_CROPBOX = 3,       /* empty or oversized beam crop box
+                                 (reference: runtime_error, host.cu:494-498)    */
+    EE_ERR_REV_SIZE = 4,      /* REV array larger than allowed
+                                 (reference: ArraySizeError, host.cu:148-154,
+                                  runtime_error for rev.x > 1024, host.cu:567)  */
+    EE_ERR_NOMEM = 5,         /* device allocation failed / admission refused  */
+    EE_ERR_NOT_READY = 6,     /* volume, spectrum or kernel not set             */
+    EE_ERR_SIDDON_ITER = 7,   /* ray trace hit its iteration cap
+                                 (reference: assert, cudaSiddon.cu:112)         */
+    EE_ERR_CAPACITY = 8       /* caller-provided scratch too small              */
+} ee_status;
+
+/* line-convolution kernel representation */
+typedef enum {
+    EE_KERNEL_TABLE = 0,  /* cumulative kernel table, linear interpolation in
+                             radius: the reference's discretisation           */
+    EE_KERNEL_EXP = 1     /* double exponential A e^{-ar} + B e^{-br} per
+                             zenith bin: O(L) recurrence (fast path)          */
+} ee_kernel_mode;
+
+/* dose output modes for ee_beam_dose* */
+typedef enum {
+    EE_DOSE_SUM = 0,        /* dose = sum over the given beams (overwrite)   */
+    EE_DOSE_ACCUMULATE = 1, /* dose += sum over the given beams              */
+    EE_DOSE_PER_BEAM = 2    /* dose[b] = beam b's dose, nbeams full volumes  */
+} ee_dose_mode;
+
+typedef struct ee_context ee_context;
+
+/* Frame of reference and calculation bounding box (CONSTANTS fields size,
+ * voxel, start, calc_bbox_start, calc_bbox_size;
+ * CCCS/include/server/brain_defs.h:38-57). */
+typedef struct {
+    int   size[3];
+    float voxel[3];
+    float start[3];
+    int   bbox_start[3];
+    int   bbox_size[3];
+} ee_frame;
+
+/* Convolution parameters (CONSTANTS nphi, ntheta, nradii, rev_latspacing,
+ * rev_longspacing, penumbra, max_rev_size; brain_defs.h:14-52). */
+typedef struct {
+    int   ntheta;
+    int   nphi;
+    int   nradii;
+    float rev_latspacing;
+    float rev_longspacing;
+    float penumbra;
+    int   max_rev_size[3];  /* 0 = derive as the reference does (host.cu:248-258) */
+} ee_conv_params;
+
+/* One beam (BEAM, CCCS/DoseCalcIO/beam.h:35-50, angle orientation). */
+typedef struct {
+    float azimuth;
+    float zenith;
+    float coll;
+    float isocenter[3];
+    float sad;
+    int   fmap_size[2];
+    float beamlet_size[2];
+} ee_beam;
+
+/* Per-beam geometry of the last dose call (crop box and REV extents). */
+typedef struct {
+    float     source[3];
+    float     direction[3];
+    float     b_min[3];       /* crop box origin, BEV voxel units           */
+    int       bev_size[3];    /* crop box size (host.cu:469-473)            */
+    float     lim_min[3];     /* crop box origin in RCS cm (host.cu:478)    */
+    long long v_beam;         /* bev_size product                           */
+    long long rev_samples;    /* sum over cones of REV array sizes          */
+    long long terma_nonzero;
+    int       max_line;       /* longest convolution line (max rev.x)       */
+    int       status;
+} ee_beam_info;
+
+/* ---- context ---- */
+int         ee_create(int device, ee_context **ctx);
+int         ee_destroy(ee_context *ctx);
+const char *ee_last_error(void);
+int         ee_abi_version(void);
+
+/* ---- set-up (initCudaConstandTex) ---- */
+int ee_set_volume(ee_context *ctx, const ee_frame *frame, const float *density_host);
+int ee_set_spectrum(ee_context *ctx, int nE, const float *energy, const float *fluence,
+                    const float *mu, const float *mu_en);
+/* cumkern: [ntheta][nradii] cumulative kernel; theta_deg/phi_deg: per ray
+ * (nphi*ntheta/2) cone angles (convolution_{theta,phi}_angles.raw). */
+int ee_set_kernel_table(ee_context *ctx, const ee_conv_params *conv, const float *radii,
+                        const float *cumkern, const float *theta_deg, const float *phi_deg);
+/* params: [ntheta][4] = (A, a, B, b); selects EE_KERNEL_EXP. */
+int ee_set_kernel_exp(ee_context *ctx, const float *params);
+int ee_set_kernel_mode(ee_context *ctx, int mode);
+
+/* ---- forward dose (radconvolveTexture) ----
+ * fluence: concatenation of the beams' fmap_size[0]*fmap_size[1] maps.
+ * Host-pointer form: copies in, computes, copies dose out (synchronous). */
+int ee_beam_dose(ee_context *ctx, const ee_beam *beams, int nbeams, const float *fluence_host,
+                 float *dose_host, int dose_mode);
+/* Device-pointer form: d_fluence and d_dose are device buffers; runs on the
+ * context stream; returns after enqueueing unless the batch needs a
+ * geometry read-back (the plain path does one per batch). */
+int ee_beam_dose_device(ee_context *ctx, const ee_beam *beams, int nbeams, const float *d_fluence,
+                        float *d_dose, int dose_mode);
+
+/* ---- adjoint: fluence gradient of <dose_grad, dose(fluence)> ----
+ * Exact transpose of the forward chain with each beam's crop box held at
+ * the one its current fluence produces. */
+int ee_beam_dose_adjoint(ee_context *ctx, const ee_beam *beams, int nbeams, const float *fluence_host,
+                         const float *dose_grad_host, float *fluence_grad_host);
+int ee_beam_dose_adjoint_device(ee_context *ctx, const ee_beam *beams, int nbeams, const float *d_fluence,
+                                const float *d_dose_grad, float *d_fluence_grad);
+
+/* ---- diagnostics ---- */
+/* Stage ids for ee_read_profile. */
+#define EE_STAGE_TERMA 0     /* k_terma (+crop-box reduction)           */
+#define EE_STAGE_GEOMETRY 1  /* k_geom_init + k_geometry                */
+#define EE_STAGE_CONE 2      /* k_cone: REV resample + line convolution */
+#define EE_STAGE_GATHER 3    /* k_gather: REV -> patient accumulation   */
+#define EE_STAGE_GATHER_T 4  /* adjoint of k_gather                     */
+#define EE_STAGE_CONE_T 5    /* adjoint of k_cone + TERMA resample      */
+#define EE_STAGE_TERMA_T 6   /* adjoint of TERMA (per-beamlet reduce)   */
+#define EE_NSTAGES 7
+/* Per-stage device-time accounting with CUDA events on the context stream
+ * (off by default).  ee_read_profile returns the accumulated milliseconds
+ * and kernel-launch counts of the first n stages and resets them. */
+int ee_set_profiling(ee_context *ctx, int enable);
+int ee_read_profile(ee_context *ctx, double *ms, long long *launches, int n);
+int ee_get_beam_info(ee_context *ctx, int beam_index, ee_beam_info *info);
+int ee_synchronize(ee_context *ctx);
+/* CUDA stream (cudaStream_t) that the context enqueues on. */
+void *ee_get_stream(ee_context *ctx);
+/* Host-side beam geometry (BEAM::reconfigure, beam.cpp:300-321):
+ * source and unit direction for the given angles. */
+int ee_beam_source(const ee_beam *beam, float source[3], float direction[3]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* EE_CCCS_H */

@@ -1,0 +1,136 @@
+"""GPU parity of the sm_103a engine against the CPU oracle, through the C ABI.
+
+Tolerances (max |difference| / Dmax of the oracle dose):
+  * engine vs FP64 oracle of the SAME discretisation:          <= 1e-3
+    (FP32 arithmetic and FP32 affine geometry vs FP64)
+  * engine (exp kernel) vs the reference discretisation
+    (24-radius cumulative table, texture-unit 8-bit weights):  <= 5e-3
+    plus a 1%/1 mm gamma pass rate >= 99.5 %.
+"""
+import numpy as np
+import pytest
+
+from endtoend_gb300 import engine, inputs, metrics
+from oracle.oracle import Oracle
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def cfg0():
+    return inputs.config0()
+
+
+@pytest.fixture(scope="module")
+def eng(cfg0):
+    vol, phys, _ = cfg0
+    e = engine.Engine(0)
+    e.set_volume(vol)
+    e.set_physics(phys, mode="exp")
+    yield e
+    e.close()
+
+
+def _rel(a, ref):
+    return float(np.abs(a - ref).max() / np.abs(ref).max())
+
+
+def test_config0_exp_vs_fp64_oracle(cfg0, eng):
+    vol, phys, beams = cfg0
+    eng.set_mode("exp")
+    d = eng.beam_dose(beams)
+    ref, info = Oracle(vol, phys, kernel_mode=2).beam_dose(beams[0])
+    gi = eng.beam_info(0)
+    assert gi["bev_size"] == list(info.bev_size)
+    assert _rel(d, ref) <= 1e-3
+
+
+def test_config0_table_vs_fp64_oracle(cfg0, eng):
+    vol, phys, beams = cfg0
+    eng.set_mode("table")
+    try:
+        d = eng.beam_dose(beams)
+    finally:
+        eng.set_mode("exp")
+    ref, _ = Oracle(vol, phys, kernel_mode=0).beam_dose(beams[0])
+    assert _rel(d, ref) <= 1e-3
+
+
+def test_config0_exp_vs_reference_discretisation(cfg0, eng):
+    vol, phys, beams = cfg0
+    eng.set_mode("exp")
+    d = eng.beam_dose(beams)
+    ref, _ = Oracle(vol, phys, kernel_mode=0, tex_emulate=True).beam_dose(beams[0])
+    assert _rel(d, ref) <= 5e-3
+    pr = metrics.gamma_pass_rate(d, ref, voxel_mm=2.5, dose_tol=0.01, dist_mm=1.0)
+    assert pr >= 0.995, pr
+
+
+@pytest.mark.parametrize("gantry,couch,coll", [(30.0, 20.0, 0.0), (200.0, -35.0, 10.0), (90.0, 0.0, 0.0)])
+def test_oblique_beams(gantry, couch, coll):
+    vol = inputs.slab_phantom(40, 0.25)
+    phys = inputs.make_physics(seed=1, spacing_cm=0.25)
+    beam = inputs.single_beam(fmap=(10, 8), beamlet_cm=0.5, gantry_deg=gantry, couch_deg=couch, coll_deg=coll)
+    beam.fluence = np.random.default_rng(3).uniform(0.1, 1.0, beam.fluence.shape).astype(np.float32)
+    with engine.Engine(0) as e:
+        e.set_volume(vol)
+        e.set_physics(phys, mode="exp")
+        d = e.beam_dose([beam])
+        e.set_mode("table")
+        dt = e.beam_dose([beam])
+    ref2, _ = Oracle(vol, phys, kernel_mode=2).beam_dose(beam)
+    ref0, _ = Oracle(vol, phys, kernel_mode=0).beam_dose(beam)
+    assert _rel(d, ref2) <= 1e-3
+    assert _rel(dt, ref0) <= 1e-3
+
+
+def test_multi_beam_sum_and_per_beam(eng, cfg0):
+    vol, phys, _ = cfg0
+    beams = [inputs.single_beam(fmap=(8, 8), beamlet_cm=0.5, gantry_deg=g, couch_deg=c) for g, c in
+             [(0, 0), (72, 0), (144, 15), (216, -20)]]
+    for i, b in enumerate(beams):
+        b.fluence = np.random.default_rng(10 + i).uniform(0.0, 1.0, b.fluence.shape).astype(np.float32)
+    per = eng.beam_dose(beams, per_beam=True)
+    tot = eng.beam_dose(beams)
+    assert np.allclose(per.sum(0), tot, rtol=1e-5, atol=1e-6 * tot.max())
+    acc = np.zeros_like(tot)
+    eng.beam_dose(beams[:2], accumulate_into=acc)
+    eng.beam_dose(beams[2:], accumulate_into=acc)
+    assert np.allclose(acc, tot, rtol=1e-5, atol=1e-6 * tot.max())
+    # each beam alone equals its slot in the batch
+    one = eng.beam_dose([beams[2]])
+    assert np.allclose(one, per[2], rtol=1e-6, atol=1e-7 * one.max())
+
+
+@pytest.mark.parametrize("mode", ["exp", "table"])
+def test_adjoint_vs_oracle_and_dot_product(mode):
+    vol = inputs.slab_phantom(32, 0.25)
+    phys = inputs.make_physics(seed=2, spacing_cm=0.25)
+    beams = [inputs.single_beam(fmap=(8, 8), beamlet_cm=0.5, gantry_deg=g, couch_deg=c) for g, c in [(20, 0), (250, 30)]]
+    rng = np.random.default_rng(4)
+    for b in beams:
+        b.fluence = rng.uniform(0.2, 1.0, b.fluence.shape).astype(np.float32)
+    g = rng.standard_normal(vol.density.shape).astype(np.float32)
+    with engine.Engine(0) as e:
+        e.set_volume(vol)
+        e.set_physics(phys, mode=mode)
+        dose = e.beam_dose(beams)
+        fg = e.beam_dose_adjoint(beams, g)
+    # <A x, g> == <x, A^T g>
+    lhs = float(np.sum(dose.astype(np.float64) * g))
+    rhs = float(sum(np.sum(b.fluence.astype(np.float64) * f) for b, f in zip(beams, fg)))
+    assert abs(lhs - rhs) <= 2e-4 * abs(lhs) + 1e-6, (lhs, rhs)
+    o = Oracle(vol, phys, kernel_mode=2 if mode == "exp" else 0)
+    for b, f in zip(beams, fg):
+        ref, _ = o.beam_dose_adjoint(b, g)
+        assert _rel(f, ref) <= 2e-3
+
+
+def test_error_paths(eng, cfg0):
+    vol, phys, beams = cfg0
+    b = inputs.single_beam(fmap=(4, 4), beamlet_cm=0.5, iso=(100.0, 100.0, 100.0))
+    with pytest.raises(engine.CropBoxError):
+        eng.beam_dose([b])
+    # the context stays usable after an error
+    d = eng.beam_dose(beams)
+    assert d.max() > 0
