@@ -49,6 +49,8 @@ __device__ __forceinline__ f3 mv(const float* M, f3 v) {
 // texel-space coordinates after the -0.5 texel-centre shift.
 __device__ __forceinline__ float tri_border(const float* __restrict__ v, int nx, int ny, int nz, float x, float y,
                                             float z) {
+    // all eight texels outside (or a NaN coordinate): the border value 0
+    if (!(x > -1.f && x < (float)nx && y > -1.f && y < (float)ny && z > -1.f && z < (float)nz)) return 0.f;
     float fx = floorf(x), fy = floorf(y), fz = floorf(z);
     int i = (int)fx, j = (int)fy, k = (int)fz;
     float ax = x - fx, ay = y - fy, az = z - fz;
@@ -87,6 +89,7 @@ __device__ __forceinline__ float tri_border(const float* __restrict__ v, int nx,
 
 // Transpose of tri_border: atomically scatter g with the trilinear weights.
 __device__ __forceinline__ void tri_border_scatter(float* v, int nx, int ny, int nz, float x, float y, float z, float g) {
+    if (!(x > -1.f && x < (float)nx && y > -1.f && y < (float)ny && z > -1.f && z < (float)nz)) return;
     float fx = floorf(x), fy = floorf(y), fz = floorf(z);
     int i = (int)fx, j = (int)fy, k = (int)fz;
     float ax = x - fx, ay = y - fy, az = z - fz;
