@@ -30,6 +30,15 @@ __device__ __forceinline__ int f2key(float f) {
 }
 __device__ __forceinline__ float key2f(int k) { return __int_as_float(k >= 0 ? k : (k ^ 0x7fffffff)); }
 
+// ceil() with extents within 1e-3 of an integer snapped to it, so that
+// axis-aligned beams (exactly integer crop-box / REV extents) do not flip by
+// one voxel with the last bit of the FP32 rotation (the reference's plain
+// ceilf at host.cu:469-473, :111-114 is rounding-dependent there).
+__device__ __forceinline__ float snap_ceilf(float v) {
+    float r = rintf(v);
+    return fabsf(v - r) <= 1e-3f ? r : ceilf(v);
+}
+
 struct f3 {
     float x, y, z;
 };
@@ -287,7 +296,7 @@ __global__ void k_geometry(EeParams P, const EeBeamSpec* __restrict__ specs, EeB
             mn[0] -= pl; mn[1] -= plg; mn[2] -= pl;
             mx[0] += pl; mx[1] += plg; mx[2] += pl;
             for (int a = 0; a < 3; a++) {
-                float s = ceilf(fabsf(mx[a] - mn[a]));
+                float s = snap_ceilf(fabsf(mx[a] - mn[a]));
                 if (!(s > 0.f) || s >= 1000.f) { ok = 0; }
                 G.bev[a] = ok ? (int)s : 0;
                 G.bmin[a] = mn[a];
@@ -314,8 +323,8 @@ __global__ void k_geometry(EeParams P, const EeBeamSpec* __restrict__ specs, EeB
             mn[0] = fminf(mn[0], o.x); mn[1] = fminf(mn[1], o.y); mn[2] = fminf(mn[2], o.z);
             mx[0] = fmaxf(mx[0], o.x); mx[1] = fmaxf(mx[1], o.y); mx[2] = fmaxf(mx[2], o.z);
         }
-        int sz[3] = {(int)ceilf(fabsf(mx[1] - mn[1]) / P.lng), (int)ceilf(fabsf(mx[2] - mn[2]) / P.lat),
-                     (int)ceilf(fabsf(mx[0] - mn[0]) / P.lat)};
+        int sz[3] = {(int)snap_ceilf(fabsf(mx[1] - mn[1]) / P.lng), (int)snap_ceilf(fabsf(mx[2] - mn[2]) / P.lat),
+                     (int)snap_ceilf(fabsf(mx[0] - mn[0]) / P.lat)};
         bool bad = false;
         for (int a = 0; a < 3; a++) {
             if (P.max_rev[a] > 0 && sz[a] > P.max_rev[a]) bad = true;

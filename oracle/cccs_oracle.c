@@ -378,6 +378,19 @@ static void ray_angles(const orc_setup *S, int ray, real *th, real *ph) {
     *ph = (real)(S->phi_deg[ray] * ORC_PI / 180.0);
 }
 
+/* ceil() of a non-negative extent with values within 1e-3 of an integer
+ * snapped to that integer.  The reference takes a plain ceilf of FP32 rotated
+ * extents (host.cu:469-473, :111-114); for axis-aligned beams the exact
+ * extent is an integer and its ceil then depends on the last bit of the
+ * rotation, moving the crop-box face by one voxel (a dose discontinuity of a
+ * few % of Dmax at that face).  Snapping makes the result independent of
+ * the arithmetic precision; the engine does the same. */
+static double snap_ceil(double v) {
+    double r = floor(v + 0.5);
+    if (fabs(v - r) <= 1e-3) return r;
+    return ceil(v);
+}
+
 /* nvbbRayConvolve_host.cu:429-499 and findREV :75-155 (REV_PAD = 0). */
 static int compute_geometry(const orc_setup *S, const orc_beam *b, const real *terma, real az, real zen,
                             orc_beam_info *info) {
@@ -404,7 +417,7 @@ static int compute_geometry(const orc_setup *S, const orc_beam *b, const real *t
     for (int a = 0; a < 3; a++) {
         info->b_min[a] = mn[a];
         info->b_max[a] = mx[a];
-        double s = ceil(fabs(mx[a] - mn[a]));
+        double s = snap_ceil(fabs(mx[a] - mn[a]));
         if (!(s > 0) || s >= 1000.0) { info->status = ORC_ERR_CROPBOX; return ORC_ERR_CROPBOX; }
         info->bev_size[a] = (int)s;
     }
@@ -430,8 +443,8 @@ static int compute_geometry(const orc_setup *S, const orc_beam *b, const real *t
                     rmn[0] = fmin(rmn[0], o.x); rmn[1] = fmin(rmn[1], o.y); rmn[2] = fmin(rmn[2], o.z);
                     rmx[0] = fmax(rmx[0], o.x); rmx[1] = fmax(rmx[1], o.y); rmx[2] = fmax(rmx[2], o.z);
                 }
-        int sz[3] = {(int)ceil(fabs(rmx[1] - rmn[1]) / lng), (int)ceil(fabs(rmx[2] - rmn[2]) / lat),
-                     (int)ceil(fabs(rmx[0] - rmn[0]) / lat)};
+        int sz[3] = {(int)snap_ceil(fabs(rmx[1] - rmn[1]) / lng), (int)snap_ceil(fabs(rmx[2] - rmn[2]) / lat),
+                     (int)snap_ceil(fabs(rmx[0] - rmn[0]) / lat)};
         for (int a = 0; a < 3; a++) {
             if (S->max_rev_size[a] > 0 && sz[a] > S->max_rev_size[a]) { info->status = ORC_ERR_REVSIZE; return ORC_ERR_REVSIZE; }
             info->rev_size[ray][a] = sz[a];
