@@ -277,6 +277,8 @@ __global__ void k_geom_init(EeBeamGeom* g, int n) {
     for (int a = 0; a < 3; a++) { g[b].key_min[a] = f2key(FLT_MAX); g[b].key_max[a] = f2key(FLT_MIN); }
     g[b].nnz = 0;
     g[b].status = 0;
+    g[b].arena_off = 0;
+    g[b].arena_cap = 0;  // unbounded: the host sizes the arena after read-back
 }
 
 // ------------------------------------------------------------- geometry --
