@@ -41,6 +41,7 @@ def parse():
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--beams", type=int, default=1024)
     ap.add_argument("--plain-beams", type=int, default=32)
+    ap.add_argument("--scratch-gb", type=int, default=64)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
     return ap.parse_args()
@@ -190,6 +191,7 @@ def main():
     eng = engine.Engine(local)
     eng.set_volume(vol)
     eng.set_physics(phys, mode="exp")
+    eng.set_scratch_limit(args.scratch_gb << 30)
     stream = torch.cuda.ExternalStream(eng.stream)
     nfull = vol.nvoxels
     fl_host = engine.concat_fluence(beams)

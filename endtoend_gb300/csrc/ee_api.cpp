@@ -316,8 +316,8 @@ int run_front(ee_context* c, const ee_beam* beams, int nb, const float* d_fluenc
         max_lines = std::max(max_lines, G.max_lines);
     }
     EE_CUDA(cudaMemcpyAsync(c->d_geoms.p, c->h_geoms.p, sizeof(EeBeamGeom) * nb, cudaMemcpyHostToDevice, s));
-    c->last_geoms.assign(c->h_geoms.p, c->h_geoms.p + nb);
-    c->last_specs.assign(c->h_specs.p, c->h_specs.p + nb);
+    c->last_geoms.insert(c->last_geoms.end(), c->h_geoms.p, c->h_geoms.p + nb);
+    c->last_specs.insert(c->last_specs.end(), c->h_specs.p, c->h_specs.p + nb);
     return EE_OK;
 }
 
@@ -331,8 +331,8 @@ int dose_device(ee_context* c, const ee_beam* beams, int nbeams, const float* d_
     const long long nfull = nfull_of(c);
     const int chunk = chunk_beams(c, nbeams, false);
     long long fl_off = 0;
-    std::vector<EeBeamGeom> all;
-    std::vector<EeBeamSpec> allspec;
+    c->last_geoms.clear();
+    c->last_specs.clear();
     for (int b0 = 0; b0 < nbeams; b0 += chunk) {
         int nb = std::min(chunk, nbeams - b0);
         long long rev_total;
@@ -347,12 +347,8 @@ int dose_device(ee_context* c, const ee_beam* beams, int nbeams, const float* d_
         if (mode == EE_DOSE_PER_BEAM) out = d_dose + (long long)b0 * nfull;
         EE_CUDA(staged(c, EE_STAGE_GATHER, 1, [&] { return ee_launch_gather(c->P, c->d_specs.p, c->d_geoms.p, c->rev.p, out, nb, m, c->stream); }));
         for (int b = 0; b < nb; b++) fl_off += (long long)beams[b0 + b].fmap_size[0] * beams[b0 + b].fmap_size[1];
-        all.insert(all.end(), c->last_geoms.begin(), c->last_geoms.end());
-        allspec.insert(allspec.end(), c->last_specs.begin(), c->last_specs.end());
         if (b0 + nb < nbeams) EE_CUDA(cudaStreamSynchronize(c->stream));  // scratch reuse
     }
-    c->last_geoms.swap(all);
-    c->last_specs.swap(allspec);
     return EE_OK;
 }
 
@@ -366,6 +362,8 @@ int adjoint_device(ee_context* c, const ee_beam* beams, int nbeams, const float*
     const long long nbbox = nbbox_of(c);
     const int chunk = chunk_beams(c, nbeams, true);
     long long fl_off = 0;
+    c->last_geoms.clear();
+    c->last_specs.clear();
     for (int b0 = 0; b0 < nbeams; b0 += chunk) {
         int nb = std::min(chunk, nbeams - b0);
         long long rev_total;
@@ -648,6 +646,13 @@ int ee_synchronize(ee_context* c) {
 }
 
 void* ee_get_stream(ee_context* c) { return c ? (void*)c->stream : nullptr; }
+
+int ee_set_scratch_limit(ee_context* c, long long bytes) {
+    if (!c || bytes <= 0) return fail(EE_ERR_INVALID_ARG, "bad scratch limit");
+    std::lock_guard<std::mutex> lk(c->mu);
+    c->max_batch_bytes = bytes;
+    return EE_OK;
+}
 
 int ee_set_profiling(ee_context* c, int enable) {
     if (!c) return fail(EE_ERR_INVALID_ARG, "null context");

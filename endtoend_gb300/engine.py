@@ -101,6 +101,7 @@ _SIGS = {
     "ee_get_stream": (C.c_void_p, [C.c_void_p]),
     "ee_beam_source": (C.c_int, [C.POINTER(EEBeam), C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "ee_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
+    "ee_set_scratch_limit": (C.c_int, [C.c_void_p, C.c_longlong]),
     "ee_read_profile": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_longlong), C.c_int]),
 }
 
@@ -258,6 +259,9 @@ class Engine:
                 "bev_size": list(bi.bev_size), "lim_min": list(bi.lim_min), "v_beam": bi.v_beam,
                 "rev_samples": bi.rev_samples, "terma_nonzero": bi.terma_nonzero, "max_line": bi.max_line,
                 "status": bi.status}
+
+    def set_scratch_limit(self, nbytes: int):
+        self._check(self.lib.ee_set_scratch_limit(self.h, int(nbytes)))
 
     def set_profiling(self, on: bool = True):
         self._check(self.lib.ee_set_profiling(self.h, 1 if on else 0))

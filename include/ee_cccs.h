@@ -154,6 +154,10 @@ int ee_beam_dose_adjoint(ee_context *ctx, const ee_beam *beams, int nbeams, cons
 int ee_beam_dose_adjoint_device(ee_context *ctx, const ee_beam *beams, int nbeams, const float *d_fluence,
                                 const float *d_dose_grad, float *d_fluence_grad);
 
+/* Device scratch budget for one chunk of beams (TERMA and REV arenas);
+ * larger batches are processed in chunks that fit.  Default 8 GiB. */
+int ee_set_scratch_limit(ee_context *ctx, long long bytes);
+
 /* ---- diagnostics ---- */
 /* Stage ids for ee_read_profile. */
 #define EE_STAGE_TERMA 0     /* k_terma (+crop-box reduction)           */
