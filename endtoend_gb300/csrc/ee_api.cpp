@@ -196,8 +196,54 @@ int check_beams(const ee_beam* beams, int nbeams) {
     return EE_OK;
 }
 
-void build_specs(const ee_beam* beams, int nbeams, long long fl_base, EeBeamSpec* out) {
-    long long off = fl_base;
+// Axis-aligned patient-index box holding the beam's field frustum between the
+// calc bbox's nearest and farthest axial distances from the source (the
+// convex hull of 8 vertices), widened by one voxel and clipped to the bbox.
+// TERMA is zero outside it: a voxel gets TERMA only when its projection onto
+// the isocentre plane lands inside the fluence map (cudaSiddon.cu:143-165).
+void terma_box(const EeParams& P, const EeBeamSpec& S, int t0[3], int tn[3]) {
+    const d3 src = {S.src[0], S.src[1], S.src[2]}, dir = {S.dir[0], S.dir[1], S.dir[2]};
+    double dmin = 1e300, dmax = -1e300;
+    for (int c = 0; c < 8; c++) {
+        double p[3];
+        for (int a = 0; a < 3; a++) {
+            int idx = ((c >> a) & 1) ? P.bb0[a] + P.bbs[a] - 1 : P.bb0[a];
+            p[a] = P.start[a] + (double)idx * P.voxel[a];
+        }
+        double d = (p[0] - src.x) * dir.x + (p[1] - src.y) * dir.y + (p[2] - src.z) * dir.z;
+        dmin = std::min(dmin, d);
+        dmax = std::max(dmax, d);
+    }
+    for (int a = 0; a < 3; a++) { t0[a] = P.bb0[a]; tn[a] = 0; }
+    if (dmax <= 0) return;  // the bbox lies behind the source
+    dmin = std::max(dmin, 1e-6);
+    const double hu = 0.5 * S.fmap[0] * S.beamlet[0], hw = 0.5 * S.fmap[1] * S.beamlet[1];
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int c = 0; c < 8; c++) {
+        double u = (c & 1) ? hu : -hu, w = (c & 2) ? hw : -hw, d = (c & 4) ? dmax : dmin;
+        // point on the isocentre plane, BEV lateral offsets (u, 0, w)
+        double q[3];
+        for (int a = 0; a < 3; a++) q[a] = S.src[a] + S.dir[a] * S.isodist + S.MBi[3 * a] * u + S.MBi[3 * a + 2] * w;
+        double sc = d / S.isodist;
+        for (int a = 0; a < 3; a++) {
+            double pos = S.src[a] + (q[a] - S.src[a]) * sc;
+            double idx = (pos - P.start[a]) / P.voxel[a];
+            lo[a] = std::min(lo[a], idx);
+            hi[a] = std::max(hi[a], idx);
+        }
+    }
+    for (int a = 0; a < 3; a++) {
+        long long l = (long long)std::floor(lo[a]) - 1, h = (long long)std::ceil(hi[a]) + 1;
+        l = std::max<long long>(l, P.bb0[a]);
+        h = std::min<long long>(h, P.bb0[a] + P.bbs[a] - 1);
+        if (h < l) { for (int k = 0; k < 3; k++) tn[k] = 0; return; }
+        t0[a] = (int)l;
+        tn[a] = (int)(h - l + 1);
+    }
+}
+
+void build_specs(const EeParams& P, const ee_beam* beams, int nbeams, EeBeamSpec* out) {
+    long long off = 0, toff = 0;
     for (int b = 0; b < nbeams; b++) {
         const ee_beam& B = beams[b];
         double az, zen;
@@ -218,8 +264,13 @@ void build_specs(const ee_beam* beams, int nbeams, long long fl_base, EeBeamSpec
         S.beamlet[0] = B.beamlet_size[0]; S.beamlet[1] = B.beamlet_size[1];
         S.fl_off = off;
         off += (long long)B.fmap_size[0] * B.fmap_size[1];
+        terma_box(P, S, S.t0, S.tn);
+        S.t_off = toff;
+        toff += (long long)S.tn[0] * S.tn[1] * S.tn[2];
     }
 }
+
+long long tvol_of(const EeBeamSpec& S) { return (long long)S.tn[0] * S.tn[1] * S.tn[2]; }
 
 const char* status_text(int st) {
     switch (st) {
@@ -267,53 +318,76 @@ cudaError_t staged(ee_context* c, int stage, int nlaunch, F fn) {
     return e;
 }
 
-long long nbbox_of(const ee_context* c) { return (long long)c->P.bbs[0] * c->P.bbs[1] * c->P.bbs[2]; }
 long long nfull_of(const ee_context* c) { return (long long)c->P.size[0] * c->P.size[1] * c->P.size[2]; }
 
 // Beams per chunk so that TERMA (+unit/index for the adjoint) fits the budget.
-int chunk_beams(const ee_context* c, int nbeams, bool adjoint) {
-    long long per = nbbox_of(c) * (long long)sizeof(float) * (adjoint ? 4 : 1) + 64ll * 1024 * 1024;
-    long long k = std::max(1ll, c->max_batch_bytes / per);
-    return (int)std::min<long long>(nbeams, std::min<long long>(k, 4096));
+// Split the beams into chunks whose device scratch fits the budget: TERMA
+// box (x4 for the adjoint's unit TERMA, beamlet index and TERMA gradient)
+// plus an estimate of the REV arena (nrays x 4 x the TERMA box, x2 for the
+// adjoint's REV gradient).
+std::vector<int> plan_chunks(const ee_context* c, const EeBeamSpec* specs, int nbeams, bool adjoint) {
+    std::vector<int> starts;
+    long long acc = 0;
+    const long long per_vox = 4ll * ((adjoint ? 4 : 1) + (long long)c->P.nrays * 4 * (adjoint ? 2 : 1));
+    for (int b = 0; b < nbeams; b++) {
+        long long need = std::max(1ll, tvol_of(specs[b])) * per_vox + sizeof(EeBeamGeom);
+        if (starts.empty() || (acc + need > c->max_batch_bytes && acc > 0)) {
+            starts.push_back(b);
+            acc = 0;
+        }
+        acc += need;
+    }
+    starts.push_back(nbeams);
+    return starts;
 }
 
 // Stages 1-3 for a chunk: specs up, TERMA + crop box, geometry, read-back,
 // REV arena offsets.  On return h_geoms holds the chunk's geometry.
-int run_front(ee_context* c, const ee_beam* beams, int nb, const float* d_fluence, long long fl_base, bool adjoint,
-              long long& rev_total, int& max_line, int& max_lines) {
+struct ChunkDims {
+    long long rev_total = 0, tvol_total = 0, max_tvol = 1;
+    int max_line = 1, max_lines = 1, max_rows = 1;
+};
+
+int run_front(ee_context* c, const EeBeamSpec* specs_in, int nb, const float* d_fluence, bool adjoint, ChunkDims& D) {
     cudaStream_t s = c->stream;
-    const long long nbbox = nbbox_of(c);
     EE_CUDA(c->h_specs.ensure(nb));
     EE_CUDA(c->h_geoms.ensure(nb));
     EE_CUDA(c->d_specs.ensure(nb));
     EE_CUDA(c->d_geoms.ensure(nb));
-    build_specs(beams, nb, 0, c->h_specs.p);
-    (void)fl_base;
+    // re-base the chunk's fluence and TERMA offsets
+    D = ChunkDims();
+    const long long fl0 = specs_in[0].fl_off;
+    for (int b = 0; b < nb; b++) {
+        EeBeamSpec& S = c->h_specs.p[b];
+        S = specs_in[b];
+        S.fl_off -= fl0;
+        S.t_off = D.tvol_total;
+        D.tvol_total += tvol_of(S);
+        D.max_tvol = std::max(D.max_tvol, tvol_of(S));
+    }
     EE_CUDA(cudaMemcpyAsync(c->d_specs.p, c->h_specs.p, sizeof(EeBeamSpec) * nb, cudaMemcpyHostToDevice, s));
-    EE_CUDA(c->terma.ensure((size_t)nb * nbbox));
+    EE_CUDA(c->terma.ensure((size_t)D.tvol_total));
     if (adjoint) {
-        EE_CUDA(c->unit.ensure((size_t)nb * nbbox));
-        EE_CUDA(c->bl_idx.ensure((size_t)nb * nbbox));
+        EE_CUDA(c->unit.ensure((size_t)D.tvol_total));
+        EE_CUDA(c->bl_idx.ensure((size_t)D.tvol_total));
     }
     EE_CUDA(staged(c, EE_STAGE_GEOMETRY, 1, [&] { return ee_launch_geom_init(c->d_geoms.p, nb, s); }));
     EE_CUDA(staged(c, EE_STAGE_TERMA, 1, [&] {
         return ee_launch_terma(c->P, c->d_specs.p, c->d_geoms.p, d_fluence, c->terma.p, adjoint ? c->unit.p : nullptr,
-                               adjoint ? c->bl_idx.p : nullptr, nb, s);
+                               adjoint ? c->bl_idx.p : nullptr, nb, D.max_tvol, s);
     }));
     EE_CUDA(staged(c, EE_STAGE_GEOMETRY, 1, [&] { return ee_launch_geometry(c->P, c->d_specs.p, c->d_geoms.p, nb, s); }));
     EE_CUDA(cudaMemcpyAsync(c->h_geoms.p, c->d_geoms.p, sizeof(EeBeamGeom) * nb, cudaMemcpyDeviceToHost, s));
     EE_CUDA(cudaStreamSynchronize(s));
-    rev_total = 0;
-    max_line = 1;
-    max_lines = 1;
     for (int b = 0; b < nb; b++) {
         EeBeamGeom& G = c->h_geoms.p[b];
         if (G.status != 0) return fail(G.status, "beam %d: %s", b, status_text(G.status));
-        G.arena_off = rev_total;
+        G.arena_off = D.rev_total;
         G.arena_cap = G.rev_total;
-        rev_total += G.rev_total;
-        max_line = std::max(max_line, G.max_line);
-        max_lines = std::max(max_lines, G.max_lines);
+        D.rev_total += G.rev_total;
+        D.max_line = std::max(D.max_line, G.max_line);
+        D.max_lines = std::max(D.max_lines, G.max_lines);
+        D.max_rows = std::max(D.max_rows, G.rows);
     }
     EE_CUDA(cudaMemcpyAsync(c->d_geoms.p, c->h_geoms.p, sizeof(EeBeamGeom) * nb, cudaMemcpyHostToDevice, s));
     c->last_geoms.insert(c->last_geoms.end(), c->h_geoms.p, c->h_geoms.p + nb);
@@ -329,25 +403,30 @@ int dose_device(ee_context* c, const ee_beam* beams, int nbeams, const float* d_
     if (mode < 0 || mode > 2) return fail(EE_ERR_INVALID_ARG, "bad dose mode %d", mode);
     EE_CUDA(cudaSetDevice(c->device));
     const long long nfull = nfull_of(c);
-    const int chunk = chunk_beams(c, nbeams, false);
-    long long fl_off = 0;
+    std::vector<EeBeamSpec> specs(nbeams);
+    build_specs(c->P, beams, nbeams, specs.data());
+    std::vector<int> starts = plan_chunks(c, specs.data(), nbeams, false);
     c->last_geoms.clear();
     c->last_specs.clear();
-    for (int b0 = 0; b0 < nbeams; b0 += chunk) {
-        int nb = std::min(chunk, nbeams - b0);
-        long long rev_total;
-        int max_line, max_lines;
-        st = run_front(c, beams + b0, nb, d_fluence + fl_off, fl_off, false, rev_total, max_line, max_lines);
+    if (mode == EE_DOSE_SUM) EE_CUDA(cudaMemsetAsync(d_dose, 0, sizeof(float) * nfull, c->stream));
+    if (mode == EE_DOSE_PER_BEAM)
+        EE_CUDA(cudaMemsetAsync(d_dose, 0, sizeof(float) * nfull * nbeams, c->stream));
+    for (size_t k = 0; k + 1 < starts.size(); k++) {
+        const int b0 = starts[k], nb = starts[k + 1] - b0;
+        ChunkDims D;
+        st = run_front(c, specs.data() + b0, nb, d_fluence + specs[b0].fl_off, false, D);
         if (st) return st;
-        EE_CUDA(c->rev.ensure((size_t)rev_total));
-        EE_CUDA(staged(c, EE_STAGE_CONE, 1, [&] { return ee_launch_cone(c->P, c->d_geoms.p, c->terma.p, c->rev.p, nb, max_lines, max_line, c->stream); }));
-        int m = mode;
-        float* out = d_dose;
-        if (mode == EE_DOSE_SUM && b0 > 0) m = EE_DOSE_ACCUMULATE;
-        if (mode == EE_DOSE_PER_BEAM) out = d_dose + (long long)b0 * nfull;
-        EE_CUDA(staged(c, EE_STAGE_GATHER, 1, [&] { return ee_launch_gather(c->P, c->d_specs.p, c->d_geoms.p, c->rev.p, out, nb, m, c->stream); }));
-        for (int b = 0; b < nb; b++) fl_off += (long long)beams[b0 + b].fmap_size[0] * beams[b0 + b].fmap_size[1];
-        if (b0 + nb < nbeams) EE_CUDA(cudaStreamSynchronize(c->stream));  // scratch reuse
+        EE_CUDA(c->rev.ensure((size_t)D.rev_total));
+        EE_CUDA(staged(c, EE_STAGE_CONE, 1, [&] {
+            return ee_launch_cone(c->P, c->d_specs.p, c->d_geoms.p, c->terma.p, c->rev.p, nb, D.max_lines, D.max_line,
+                                  c->stream);
+        }));
+        float* out = mode == EE_DOSE_PER_BEAM ? d_dose + (long long)b0 * nfull : d_dose;
+        const int m = mode == EE_DOSE_PER_BEAM ? 2 : 1;
+        EE_CUDA(staged(c, EE_STAGE_GATHER, 1, [&] {
+            return ee_launch_gather(c->P, c->d_specs.p, c->d_geoms.p, c->rev.p, out, nb, m, D.max_rows, c->stream);
+        }));
+        if (k + 2 < starts.size()) EE_CUDA(cudaStreamSynchronize(c->stream));  // scratch reuse
     }
     return EE_OK;
 }
@@ -359,32 +438,36 @@ int adjoint_device(ee_context* c, const ee_beam* beams, int nbeams, const float*
     if ((st = check_beams(beams, nbeams))) return st;
     if (!d_fluence || !d_grad || !d_fgrad) return fail(EE_ERR_INVALID_ARG, "null pointer");
     EE_CUDA(cudaSetDevice(c->device));
-    const long long nbbox = nbbox_of(c);
-    const int chunk = chunk_beams(c, nbeams, true);
-    long long fl_off = 0;
+    std::vector<EeBeamSpec> specs(nbeams);
+    build_specs(c->P, beams, nbeams, specs.data());
+    std::vector<int> starts = plan_chunks(c, specs.data(), nbeams, true);
     c->last_geoms.clear();
     c->last_specs.clear();
-    for (int b0 = 0; b0 < nbeams; b0 += chunk) {
-        int nb = std::min(chunk, nbeams - b0);
-        long long rev_total;
-        int max_line, max_lines;
-        st = run_front(c, beams + b0, nb, d_fluence + fl_off, fl_off, true, rev_total, max_line, max_lines);
+    long long nfl_all = 0;
+    for (int b = 0; b < nbeams; b++) nfl_all += (long long)beams[b].fmap_size[0] * beams[b].fmap_size[1];
+    EE_CUDA(cudaMemsetAsync(d_fgrad, 0, sizeof(float) * nfl_all, c->stream));
+    for (size_t k = 0; k + 1 < starts.size(); k++) {
+        const int b0 = starts[k], nb = starts[k + 1] - b0;
+        const long long fl0 = specs[b0].fl_off;
+        ChunkDims D;
+        st = run_front(c, specs.data() + b0, nb, d_fluence + fl0, true, D);
         if (st) return st;
-        long long nfl = 0;
-        for (int b = 0; b < nb; b++) nfl += (long long)beams[b0 + b].fmap_size[0] * beams[b0 + b].fmap_size[1];
-        EE_CUDA(c->rev_grad.ensure((size_t)rev_total));
-        EE_CUDA(c->terma_grad.ensure((size_t)nb * nbbox));
-        EE_CUDA(cudaMemsetAsync(c->rev_grad.p, 0, sizeof(float) * rev_total, c->stream));
-        EE_CUDA(cudaMemsetAsync(c->terma_grad.p, 0, sizeof(float) * nb * nbbox, c->stream));
-        EE_CUDA(cudaMemsetAsync(d_fgrad + fl_off, 0, sizeof(float) * nfl, c->stream));
-        EE_CUDA(staged(c, EE_STAGE_GATHER_T, 1, [&] { return ee_launch_gather_T(c->P, c->d_specs.p, c->d_geoms.p, d_grad, c->rev_grad.p, nb, c->stream); }));
-        EE_CUDA(staged(c, EE_STAGE_CONE_T, 1, [&] { return ee_launch_cone_T(c->P, c->d_geoms.p, c->rev_grad.p, c->terma_grad.p, nb, max_lines, max_line, c->stream); }));
+        EE_CUDA(c->rev_grad.ensure((size_t)D.rev_total));
+        EE_CUDA(c->terma_grad.ensure((size_t)D.tvol_total));
+        EE_CUDA(cudaMemsetAsync(c->rev_grad.p, 0, sizeof(float) * D.rev_total, c->stream));
+        EE_CUDA(cudaMemsetAsync(c->terma_grad.p, 0, sizeof(float) * D.tvol_total, c->stream));
+        EE_CUDA(staged(c, EE_STAGE_GATHER_T, 1, [&] {
+            return ee_launch_gather_T(c->P, c->d_specs.p, c->d_geoms.p, d_grad, c->rev_grad.p, nb, D.max_rows, c->stream);
+        }));
+        EE_CUDA(staged(c, EE_STAGE_CONE_T, 1, [&] {
+            return ee_launch_cone_T(c->P, c->d_specs.p, c->d_geoms.p, c->rev_grad.p, c->terma_grad.p, nb, D.max_lines,
+                                    D.max_line, c->stream);
+        }));
         EE_CUDA(staged(c, EE_STAGE_TERMA_T, 1, [&] {
             return ee_launch_terma_T(c->P, c->d_specs.p, c->d_geoms.p, c->unit.p, c->bl_idx.p, c->terma_grad.p,
-                                     d_fgrad + fl_off, nb, c->stream);
+                                     d_fgrad + fl0, nb, D.max_tvol, c->stream);
         }));
-        fl_off += nfl;
-        if (b0 + nb < nbeams) EE_CUDA(cudaStreamSynchronize(c->stream));
+        if (k + 2 < starts.size()) EE_CUDA(cudaStreamSynchronize(c->stream));
     }
     return EE_OK;
 }

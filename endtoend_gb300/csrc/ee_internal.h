@@ -52,6 +52,11 @@ struct EeBeamSpec {
     int fmap[2];
     float beamlet[2];
     long long fl_off;      // offset of this beam's fluence map
+    // TERMA box: axis-aligned patient-index box holding the field frustum
+    // (clipped to the calc bbox); TERMA is identically zero outside it.
+    int t0[3];             // origin (full-grid voxel index)
+    int tn[3];             // size
+    long long t_off;       // element offset in the TERMA arena
 };
 
 // Per-cone geometry of one beam, computed on the device.
@@ -79,6 +84,10 @@ struct EeBeamGeom {
     long long rev_total;
     int max_line;
     int max_lines;
+    // patient rows (y,z) whose voxels can see this beam's REV dose: the AABB
+    // of the crop box dilated by 2 voxels, clipped to the calc bbox
+    int gy0, gz0, gny, gnz;
+    int rows;
     long long arena_off;   // element offset of this beam's REV arena
     long long arena_cap;   // elements available to this beam
     EeRayGeom ray[EE_MAX_RAYS];
@@ -89,18 +98,21 @@ cudaError_t ee_launch_geom_init(EeBeamGeom* g, int nbeams, cudaStream_t s);
 // unit/beamlet_idx (both optional) receive TERMA per unit fluence of every
 // in-field voxel and its beamlet index (adjoint).
 cudaError_t ee_launch_terma(const EeParams& P, const EeBeamSpec* specs, EeBeamGeom* geoms, const float* fluence,
-                            float* terma, float* unit, int* beamlet_idx, int nbeams, cudaStream_t s);
+                            float* terma, float* unit, int* beamlet_idx, int nbeams, long long max_tvol,
+                            cudaStream_t s);
 cudaError_t ee_launch_geometry(const EeParams& P, const EeBeamSpec* specs, EeBeamGeom* geoms, int nbeams,
                                cudaStream_t s);
-cudaError_t ee_launch_cone(const EeParams& P, const EeBeamGeom* geoms, const float* terma, float* rev,
-                           int nbeams, int max_lines, int max_line, cudaStream_t s);
+cudaError_t ee_launch_cone(const EeParams& P, const EeBeamSpec* specs, const EeBeamGeom* geoms, const float* terma,
+                           float* rev, int nbeams, int max_lines, int max_line, cudaStream_t s);
+// dose_mode 0/1 accumulate atomically into dose (the caller zeroes it for
+// mode 0); mode 2 writes dose[b] rows (the caller zeroes the volumes).
 cudaError_t ee_launch_gather(const EeParams& P, const EeBeamSpec* specs, const EeBeamGeom* geoms, const float* rev,
-                             float* dose, int nbeams, int dose_mode, cudaStream_t s);
+                             float* dose, int nbeams, int dose_mode, int max_rows, cudaStream_t s);
 // adjoint
 cudaError_t ee_launch_gather_T(const EeParams& P, const EeBeamSpec* specs, const EeBeamGeom* geoms,
-                               const float* dose_grad, float* rev_grad, int nbeams, cudaStream_t s);
-cudaError_t ee_launch_cone_T(const EeParams& P, const EeBeamGeom* geoms, const float* rev_grad, float* terma_grad,
-                             int nbeams, int max_lines, int max_line, cudaStream_t s);
+                               const float* dose_grad, float* rev_grad, int nbeams, int max_rows, cudaStream_t s);
+cudaError_t ee_launch_cone_T(const EeParams& P, const EeBeamSpec* specs, const EeBeamGeom* geoms, const float* rev_grad,
+                             float* terma_grad, int nbeams, int max_lines, int max_line, cudaStream_t s);
 cudaError_t ee_launch_terma_T(const EeParams& P, const EeBeamSpec* specs, const EeBeamGeom* geoms,
                               const float* unit_terma, const int* beamlet_idx, const float* terma_grad,
-                              float* fluence_grad, int nbeams, cudaStream_t s);
+                              float* fluence_grad, int nbeams, long long max_tvol, cudaStream_t s);

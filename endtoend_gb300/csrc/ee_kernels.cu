@@ -200,19 +200,19 @@ __device__ __forceinline__ float terma_per_fluence(const EeParams& P, float rpl,
 
 __global__ void __launch_bounds__(256) k_terma(EeParams P, const EeBeamSpec* __restrict__ specs,
                                                EeBeamGeom* __restrict__ geoms, const float* __restrict__ fluence,
-                                               float* __restrict__ terma, float* __restrict__ unit, int* __restrict__ bl_idx,
-                                               long long nbbox) {
+                                               float* __restrict__ terma, float* __restrict__ unit, int* __restrict__ bl_idx) {
     const int b = blockIdx.z;
     const EeBeamSpec& S = specs[b];
+    const long long tvol = (long long)S.tn[0] * S.tn[1] * S.tn[2];
     long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     bool nz = false, cap = false;
     f3 bi = mk(0.f, 0.f, 0.f);
-    if (v < nbbox) {
-        int x = (int)(v % P.bbs[0]);
-        int y = (int)((v / P.bbs[0]) % P.bbs[1]);
-        int z = (int)(v / ((long long)P.bbs[0] * P.bbs[1]));
-        f3 vox = mk(P.start[0] + (P.bb0[0] + x) * P.voxel[0], P.start[1] + (P.bb0[1] + y) * P.voxel[1],
-                    P.start[2] + (P.bb0[2] + z) * P.voxel[2]);
+    if (v < tvol) {
+        // full-grid voxel index of this TERMA-box voxel
+        int x = S.t0[0] + (int)(v % S.tn[0]);
+        int y = S.t0[1] + (int)((v / S.tn[0]) % S.tn[1]);
+        int z = S.t0[2] + (int)(v / ((long long)S.tn[0] * S.tn[1]));
+        f3 vox = mk(P.start[0] + x * P.voxel[0], P.start[1] + y * P.voxel[1], P.start[2] + z * P.voxel[2]);
         f3 src = ld3(S.src);
         int bl = beamlet_of(S, vox);
         float t = 0.f, u = 0.f;
@@ -224,12 +224,13 @@ __global__ void __launch_bounds__(256) k_terma(EeParams P, const EeBeamSpec* __r
                 if (fl > 0.f) t = fl * u;
             }
         }
-        terma[(long long)b * nbbox + v] = t;
-        if (unit) unit[(long long)b * nbbox + v] = u;
-        if (bl_idx) bl_idx[(long long)b * nbbox + v] = bl;
+        terma[S.t_off + v] = t;
+        if (unit) unit[S.t_off + v] = u;
+        if (bl_idx) bl_idx[S.t_off + v] = bl;
         if (t != 0.f) {
             nz = true;
-            bi = mv(S.MB, mk((float)x, (float)y, (float)z));
+            // crop box works on calc-bbox-relative indices (host.cu:445-448)
+            bi = mv(S.MB, mk((float)(x - P.bb0[0]), (float)(y - P.bb0[1]), (float)(z - P.bb0[2])));
         }
     }
     // crop-box reduction (host.cu:442-459): min/max of BEV indices of voxels
@@ -356,6 +357,20 @@ __global__ void k_geometry(EeParams P, const EeBeamSpec* __restrict__ specs, EeB
     }
     __syncthreads();
     if (threadIdx.x == 0 && G.status == 0) {
+        // patient-index AABB of the crop box dilated by 2 BEV voxels
+        float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+        for (int c = 0; c < 8; c++) {
+            f3 bc = mk((c & 1) ? G.bev[0] + 2.f : -2.f, ((c >> 1) & 1) ? G.bev[1] + 2.f : -2.f,
+                       ((c >> 2) & 1) ? G.bev[2] + 2.f : -2.f);
+            f3 t = mv(S.MBi, bc) + mk(G.lim_off[0], G.lim_off[1], G.lim_off[2]);
+            lo[0] = fminf(lo[0], t.x); lo[1] = fminf(lo[1], t.y); lo[2] = fminf(lo[2], t.z);
+            hi[0] = fmaxf(hi[0], t.x); hi[1] = fmaxf(hi[1], t.y); hi[2] = fmaxf(hi[2], t.z);
+        }
+        int y0 = max(P.bb0[1], (int)floorf(lo[1]) - 1), y1 = min(P.bb0[1] + P.bbs[1] - 1, (int)ceilf(hi[1]) + 1);
+        int z0 = max(P.bb0[2], (int)floorf(lo[2]) - 1), z1 = min(P.bb0[2] + P.bbs[2] - 1, (int)ceilf(hi[2]) + 1);
+        G.gy0 = y0; G.gz0 = z0;
+        G.gny = max(0, y1 - y0 + 1); G.gnz = max(0, z1 - z0 + 1);
+        G.rows = G.gny * G.gnz;
         long long off = 0;
         int ml = 0, mls = 0;
         for (int r = 0; r < P.nrays; r++) {
@@ -376,9 +391,9 @@ __global__ void k_geometry(EeParams P, const EeBeamSpec* __restrict__ specs, EeB
 // REV resample of one line into shared memory (device.cu:47-79): density
 // sentinel -3 outside the BEV crop box, -2 outside the calc bbox; TERMA is
 // zero at sentinel samples (never written by the reference).
-__device__ __forceinline__ void gather_line(const EeParams& P, const EeBeamGeom& G, const EeRayGeom& R,
-                                            const float* __restrict__ terma_b, int tY, int tZ, int L, int lane,
-                                            float* rho, float* T) {
+__device__ __forceinline__ void gather_line(const EeParams& P, const EeBeamSpec& S, const EeBeamGeom& G,
+                                            const EeRayGeom& R, const float* __restrict__ terma_b, int tY, int tZ,
+                                            int L, int lane, float* rho, float* T) {
     const f3 bl = ld3(R.B0) + ld3(R.By) * (float)tY + ld3(R.Bz) * (float)tZ;
     const f3 gl = ld3(R.G0) + ld3(R.Gy) * (float)tY + ld3(R.Gz) * (float)tZ;
     const f3 bx = ld3(R.Bx), gx = ld3(R.Gx);
@@ -394,7 +409,9 @@ __device__ __forceinline__ void gather_line(const EeParams& P, const EeBeamGeom&
                 r = -2.f;
             } else {
                 r = tri_border(P.density, P.size[0], P.size[1], P.size[2], g.x, g.y, g.z);
-                if (terma_b) t = tri_border(terma_b, P.bbs[0], P.bbs[1], P.bbs[2], g.x - b0x, g.y - b0y, g.z - b0z);
+                if (terma_b)
+                    t = tri_border(terma_b, S.tn[0], S.tn[1], S.tn[2], g.x - (float)S.t0[0], g.y - (float)S.t0[1],
+                                   g.z - (float)S.t0[2]);
             }
         }
         rho[i] = r;
@@ -546,9 +563,10 @@ __device__ __forceinline__ float table_walk(const float* rho, const float* T, in
 // ------------------------------------------------------- cone kernels ----
 constexpr int CONE_WARPS = 4;
 
-__global__ void __launch_bounds__(CONE_WARPS * 32) k_cone(EeParams P, const EeBeamGeom* __restrict__ geoms,
+__global__ void __launch_bounds__(CONE_WARPS * 32) k_cone(EeParams P, const EeBeamSpec* __restrict__ specs,
+                                                          const EeBeamGeom* __restrict__ geoms,
                                                           const float* __restrict__ terma, float* __restrict__ rev,
-                                                          long long nbbox, int maxL) {
+                                                          int maxL) {
     extern __shared__ float sm[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int ray = blockIdx.y, b = blockIdx.z;
@@ -573,7 +591,7 @@ __global__ void __launch_bounds__(CONE_WARPS * 32) k_cone(EeParams P, const EeBe
     float* rho = sm + (size_t)warp * 3 * maxL;
     float* T = rho + maxL;
     float* D = T + maxL;
-    gather_line(P, G, R, terma + (long long)b * nbbox, tY, tZ, L, lane, rho, T);
+    gather_line(P, specs[b], G, R, terma + specs[b].t_off, tY, tZ, L, lane, rho, T);
     __syncwarp();
     float* out = rev + G.arena_off + R.offset + (long long)line * L;
     const float inv_nphi = 1.f / (float)P.nphi;
@@ -597,9 +615,10 @@ __global__ void __launch_bounds__(CONE_WARPS * 32) k_cone(EeParams P, const EeBe
 
 // Adjoint of k_cone followed by the transpose of the REV TERMA resample:
 // terma_grad (bbox grid) += R_T^T C^T rev_grad.
-__global__ void __launch_bounds__(CONE_WARPS * 32) k_cone_T(EeParams P, const EeBeamGeom* __restrict__ geoms,
+__global__ void __launch_bounds__(CONE_WARPS * 32) k_cone_T(EeParams P, const EeBeamSpec* __restrict__ specs,
+                                                            const EeBeamGeom* __restrict__ geoms,
                                                             const float* __restrict__ rev_grad,
-                                                            float* __restrict__ terma_grad, long long nbbox, int maxL) {
+                                                            float* __restrict__ terma_grad, int maxL) {
     extern __shared__ float sm[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int ray = blockIdx.y, b = blockIdx.z;
@@ -624,7 +643,8 @@ __global__ void __launch_bounds__(CONE_WARPS * 32) k_cone_T(EeParams P, const Ee
     float* rho = sm + (size_t)warp * 3 * maxL;
     float* g = rho + maxL;
     float* Tb = g + maxL;
-    gather_line(P, G, R, nullptr, tY, tZ, L, lane, rho, nullptr);
+    const EeBeamSpec& S = specs[b];
+    gather_line(P, S, G, R, nullptr, tY, tZ, L, lane, rho, nullptr);
     const float* gin = rev_grad + G.arena_off + R.offset + (long long)line * L;
     const float inv_nphi = 1.f / (float)P.nphi;
     for (int i = lane; i < L; i += 32) {
@@ -649,12 +669,13 @@ __global__ void __launch_bounds__(CONE_WARPS * 32) k_cone_T(EeParams P, const Ee
     // transpose of the REV TERMA resample
     const f3 gl = ld3(R.G0) + ld3(R.Gy) * (float)tY + ld3(R.Gz) * (float)tZ;
     const f3 gx = ld3(R.Gx);
-    float* tg = terma_grad + (long long)b * nbbox;
+    float* tg = terma_grad + S.t_off;
     for (int i = lane; i < L; i += 32) {
         float v = Tb[i];
         if (rho[i] < 0.f || v == 0.f) continue;
         f3 gp = gl + gx * (float)i;
-        tri_border_scatter(tg, P.bbs[0], P.bbs[1], P.bbs[2], gp.x - P.bb0[0], gp.y - P.bb0[1], gp.z - P.bb0[2], v);
+        tri_border_scatter(tg, S.tn[0], S.tn[1], S.tn[2], gp.x - (float)S.t0[0], gp.y - (float)S.t0[1],
+                           gp.z - (float)S.t0[2], v);
     }
 }
 
@@ -684,60 +705,90 @@ __device__ __forceinline__ float beam_voxel_dose(const EeParams& P, const EeBeam
     return acc;
 }
 
-__global__ void __launch_bounds__(256) k_gather(EeParams P, const EeBeamSpec* __restrict__ specs,
-                                                const EeBeamGeom* __restrict__ geoms, const float* __restrict__ rev,
-                                                float* __restrict__ dose, int nbeams, int mode, long long nfull) {
-    long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= nfull) return;
-    int x = (int)(v % P.size[0]);
-    int y = (int)((v / P.size[0]) % P.size[1]);
-    int z = (int)(v / ((long long)P.size[0] * P.size[1]));
-    bool inbb = x >= P.bb0[0] && x < P.bb0[0] + P.bbs[0] && y >= P.bb0[1] && y < P.bb0[1] + P.bbs[1] &&
-                z >= P.bb0[2] && z < P.bb0[2] + P.bbs[2];
-    if (mode == 2) {
-        int b = blockIdx.z;
-        float acc = 0.f;
-        if (inbb && geoms[b].status == 0) acc = beam_voxel_dose(P, specs[b], geoms[b], rev, x, y, z);
-        dose[(long long)b * nfull + v] = acc;
-        return;
+// Voxel range [x0, x1] of patient row (y, z) whose BEV index lies within the
+// crop box dilated by 2 voxels (the BEV index is affine in x), widened by one
+// voxel for rounding and clipped to the calc bbox.
+__device__ __forceinline__ bool row_span(const EeParams& P, const EeBeamSpec& S, const EeBeamGeom& G, int y, int z,
+                                         int& x0, int& x1) {
+    float xa = (float)P.bb0[0], xb = (float)(P.bb0[0] + P.bbs[0] - 1);
+    const float dy = (float)y - G.lim_off[1], dz = (float)z - G.lim_off[2];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        float m = S.MB[3 * a];
+        float c = S.MB[3 * a + 1] * dy + S.MB[3 * a + 2] * dz - m * G.lim_off[0];
+        float lo = -2.f, hi = (float)G.bev[a] + 2.f;
+        if (fabsf(m) < 1e-6f) {
+            if (c < lo - 1e-3f || c > hi + 1e-3f) return false;
+        } else {
+            float t0 = (lo - c) / m, t1 = (hi - c) / m;
+            xa = fmaxf(xa, fminf(t0, t1));
+            xb = fminf(xb, fmaxf(t0, t1));
+        }
     }
-    float acc = 0.f;
-    if (inbb)
-        for (int b = 0; b < nbeams; b++)
-            if (geoms[b].status == 0) acc += beam_voxel_dose(P, specs[b], geoms[b], rev, x, y, z);
-    if (mode == 1) dose[v] += acc;
-    else dose[v] = acc;
+    if (!(xa <= xb + 2.f)) return false;
+    x0 = max(P.bb0[0], (int)floorf(xa) - 1);
+    x1 = min(P.bb0[0] + P.bbs[0] - 1, (int)ceilf(xb) + 1);
+    return x0 <= x1;
 }
 
-// Transpose of beam_voxel_dose: rev_grad += S^T dose_grad (atomic scatter).
-__global__ void __launch_bounds__(256) k_gather_T(EeParams P, const EeBeamSpec* __restrict__ specs,
-                                                  const EeBeamGeom* __restrict__ geoms,
-                                                  const float* __restrict__ dose_grad, float* __restrict__ rev_grad,
-                                                  long long nbbox) {
-    long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+constexpr int ROW_WARPS = 8;
+
+// One warp per patient row of one beam's AABB; lanes sweep the row's span.
+// mode 0/1: atomic accumulation into dose; mode 2: dose[b] written directly.
+__global__ void __launch_bounds__(ROW_WARPS * 32) k_gather(EeParams P, const EeBeamSpec* __restrict__ specs,
+                                                           const EeBeamGeom* __restrict__ geoms,
+                                                           const float* __restrict__ rev, float* __restrict__ dose,
+                                                           int mode, long long nfull) {
     const int b = blockIdx.z;
-    if (v >= nbbox) return;
     const EeBeamGeom& G = geoms[b];
     if (G.status != 0) return;
-    int x = P.bb0[0] + (int)(v % P.bbs[0]);
-    int y = P.bb0[1] + (int)((v / P.bbs[0]) % P.bbs[1]);
-    int z = P.bb0[2] + (int)(v / ((long long)P.bbs[0] * P.bbs[1]));
-    float gd = dose_grad[x + (long long)P.size[0] * (y + (long long)P.size[1] * z)];
-    if (gd == 0.f) return;
+    const int row = blockIdx.x * ROW_WARPS + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (row >= G.rows) return;
+    const int y = G.gy0 + row % G.gny, z = G.gz0 + row / G.gny;
     const EeBeamSpec& S = specs[b];
-    f3 d = mk((float)x - G.lim_off[0], (float)y - G.lim_off[1], (float)z - G.lim_off[2]);
-    f3 bi = mv(S.MB, d);
-    if (bi.x < -2.f || bi.y < -2.f || bi.z < -2.f || bi.x > G.bev[0] + 2.f || bi.y > G.bev[1] + 2.f ||
-        bi.z > G.bev[2] + 2.f)
-        return;
+    int x0, x1;
+    if (!row_span(P, S, G, y, z, x0, x1)) return;
+    float* out = dose + (mode == 2 ? (long long)b * nfull : 0ll);
+    const long long rbase = (long long)P.size[0] * (y + (long long)P.size[1] * z);
+    for (int x = x0 + lane; x <= x1; x += 32) {
+        float acc = beam_voxel_dose(P, S, G, rev, x, y, z);
+        if (mode == 2) out[rbase + x] = acc;
+        else if (acc != 0.f) atomicAdd(out + rbase + x, acc);
+    }
+}
+
+// Transpose of beam_voxel_dose over the same rows: rev_grad += S^T dose_grad.
+__global__ void __launch_bounds__(ROW_WARPS * 32) k_gather_T(EeParams P, const EeBeamSpec* __restrict__ specs,
+                                                             const EeBeamGeom* __restrict__ geoms,
+                                                             const float* __restrict__ dose_grad,
+                                                             float* __restrict__ rev_grad) {
+    const int b = blockIdx.z;
+    const EeBeamGeom& G = geoms[b];
+    if (G.status != 0) return;
+    const int row = blockIdx.x * ROW_WARPS + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (row >= G.rows) return;
+    const int y = G.gy0 + row % G.gny, z = G.gz0 + row / G.gny;
+    const EeBeamSpec& S = specs[b];
+    int x0, x1;
+    if (!row_span(P, S, G, y, z, x0, x1)) return;
+    const long long rbase = (long long)P.size[0] * (y + (long long)P.size[1] * z);
     float* base = rev_grad + G.arena_off;
-    for (int r = 0; r < P.nrays; r++) {
-        const EeRayGeom& R = G.ray[r];
-        f3 q = mv(R.M, bi) - ld3(R.q0);
-        if (q.y >= (float)R.rev[0] || q.z >= (float)R.rev[1] || q.x >= (float)R.rev[2] || q.x < 0.f || q.y < 0.f ||
-            q.z < 0.f)
+    for (int x = x0 + lane; x <= x1; x += 32) {
+        float gd = __ldg(dose_grad + rbase + x);
+        if (gd == 0.f) continue;
+        f3 d = mk((float)x - G.lim_off[0], (float)y - G.lim_off[1], (float)z - G.lim_off[2]);
+        f3 bi = mv(S.MB, d);
+        if (bi.x < -2.f || bi.y < -2.f || bi.z < -2.f || bi.x > G.bev[0] + 2.f || bi.y > G.bev[1] + 2.f ||
+            bi.z > G.bev[2] + 2.f)
             continue;
-        tri_border_scatter(base + R.offset, R.rev[0], R.rev[1], R.rev[2], q.y, q.z, q.x, gd);
+        for (int r = 0; r < P.nrays; r++) {
+            const EeRayGeom& R = G.ray[r];
+            f3 q = mv(R.M, bi) - ld3(R.q0);
+            if (q.y >= (float)R.rev[0] || q.z >= (float)R.rev[1] || q.x >= (float)R.rev[2] || q.x < 0.f ||
+                q.y < 0.f || q.z < 0.f)
+                continue;
+            tri_border_scatter(base + R.offset, R.rev[0], R.rev[1], R.rev[2], q.y, q.z, q.x, gd);
+        }
     }
 }
 
@@ -745,14 +796,15 @@ __global__ void __launch_bounds__(256) k_gather_T(EeParams P, const EeBeamSpec* 
 // aggregated per beamlet index before the atomic.
 __global__ void __launch_bounds__(256) k_terma_T(EeParams P, const EeBeamSpec* __restrict__ specs,
                                                  const float* __restrict__ unit, const int* __restrict__ bl_idx,
-                                                 const float* __restrict__ terma_grad, float* __restrict__ fluence_grad,
-                                                 long long nbbox) {
-    long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+                                                 const float* __restrict__ terma_grad, float* __restrict__ fluence_grad) {
     const int b = blockIdx.z;
+    const EeBeamSpec& S = specs[b];
+    const long long tvol = (long long)S.tn[0] * S.tn[1] * S.tn[2];
+    long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     int bl = -1;
     float val = 0.f;
-    if (v < nbbox) {
-        long long o = (long long)b * nbbox + v;
+    if (v < tvol) {
+        long long o = S.t_off + v;
         bl = bl_idx[o];
         if (bl >= 0) val = unit[o] * terma_grad[o];
     }
@@ -778,10 +830,10 @@ cudaError_t ee_launch_geom_init(EeBeamGeom* g, int nbeams, cudaStream_t s) {
 }
 
 cudaError_t ee_launch_terma(const EeParams& P, const EeBeamSpec* specs, EeBeamGeom* geoms, const float* fluence,
-                            float* terma, float* unit, int* beamlet_idx, int nbeams, cudaStream_t s) {
-    long long nbbox = (long long)P.bbs[0] * P.bbs[1] * P.bbs[2];
-    dim3 grid(grid1(nbbox, 256), 1, nbeams);
-    k_terma<<<grid, 256, 0, s>>>(P, specs, geoms, fluence, terma, unit, beamlet_idx, nbbox);
+                            float* terma, float* unit, int* beamlet_idx, int nbeams, long long max_tvol,
+                            cudaStream_t s) {
+    dim3 grid(grid1(max_tvol, 256), 1, nbeams);
+    k_terma<<<grid, 256, 0, s>>>(P, specs, geoms, fluence, terma, unit, beamlet_idx);
     return cudaGetLastError();
 }
 
@@ -798,50 +850,46 @@ static cudaError_t cone_attr(const void* fn, size_t smem) {
     return cudaSuccess;
 }
 
-cudaError_t ee_launch_cone(const EeParams& P, const EeBeamGeom* geoms, const float* terma, float* rev, int nbeams,
-                           int max_lines, int max_line, cudaStream_t s) {
-    long long nbbox = (long long)P.bbs[0] * P.bbs[1] * P.bbs[2];
+cudaError_t ee_launch_cone(const EeParams& P, const EeBeamSpec* specs, const EeBeamGeom* geoms, const float* terma,
+                           float* rev, int nbeams, int max_lines, int max_line, cudaStream_t s) {
     size_t smem = cone_smem(max_line);
     cudaError_t e = cone_attr((const void*)k_cone, smem);
     if (e != cudaSuccess) return e;
     dim3 grid(grid1(max_lines, CONE_WARPS), P.nrays, nbeams);
-    k_cone<<<grid, CONE_WARPS * 32, smem, s>>>(P, geoms, terma, rev, nbbox, max_line);
+    k_cone<<<grid, CONE_WARPS * 32, smem, s>>>(P, specs, geoms, terma, rev, max_line);
     return cudaGetLastError();
 }
 
 cudaError_t ee_launch_gather(const EeParams& P, const EeBeamSpec* specs, const EeBeamGeom* geoms, const float* rev,
-                             float* dose, int nbeams, int dose_mode, cudaStream_t s) {
+                             float* dose, int nbeams, int dose_mode, int max_rows, cudaStream_t s) {
     long long nfull = (long long)P.size[0] * P.size[1] * P.size[2];
-    dim3 grid(grid1(nfull, 256), 1, dose_mode == 2 ? nbeams : 1);
-    k_gather<<<grid, 256, 0, s>>>(P, specs, geoms, rev, dose, nbeams, dose_mode, nfull);
+    dim3 grid(grid1(max_rows, ROW_WARPS), 1, nbeams);
+    k_gather<<<grid, ROW_WARPS * 32, 0, s>>>(P, specs, geoms, rev, dose, dose_mode, nfull);
     return cudaGetLastError();
 }
 
 cudaError_t ee_launch_gather_T(const EeParams& P, const EeBeamSpec* specs, const EeBeamGeom* geoms,
-                               const float* dose_grad, float* rev_grad, int nbeams, cudaStream_t s) {
-    long long nbbox = (long long)P.bbs[0] * P.bbs[1] * P.bbs[2];
-    dim3 grid(grid1(nbbox, 256), 1, nbeams);
-    k_gather_T<<<grid, 256, 0, s>>>(P, specs, geoms, dose_grad, rev_grad, nbbox);
+                               const float* dose_grad, float* rev_grad, int nbeams, int max_rows, cudaStream_t s) {
+    dim3 grid(grid1(max_rows, ROW_WARPS), 1, nbeams);
+    k_gather_T<<<grid, ROW_WARPS * 32, 0, s>>>(P, specs, geoms, dose_grad, rev_grad);
     return cudaGetLastError();
 }
 
-cudaError_t ee_launch_cone_T(const EeParams& P, const EeBeamGeom* geoms, const float* rev_grad, float* terma_grad,
-                             int nbeams, int max_lines, int max_line, cudaStream_t s) {
-    long long nbbox = (long long)P.bbs[0] * P.bbs[1] * P.bbs[2];
+cudaError_t ee_launch_cone_T(const EeParams& P, const EeBeamSpec* specs, const EeBeamGeom* geoms, const float* rev_grad,
+                             float* terma_grad, int nbeams, int max_lines, int max_line, cudaStream_t s) {
     size_t smem = cone_smem(max_line);
     cudaError_t e = cone_attr((const void*)k_cone_T, smem);
     if (e != cudaSuccess) return e;
     dim3 grid(grid1(max_lines, CONE_WARPS), P.nrays, nbeams);
-    k_cone_T<<<grid, CONE_WARPS * 32, smem, s>>>(P, geoms, rev_grad, terma_grad, nbbox, max_line);
+    k_cone_T<<<grid, CONE_WARPS * 32, smem, s>>>(P, specs, geoms, rev_grad, terma_grad, max_line);
     return cudaGetLastError();
 }
 
 cudaError_t ee_launch_terma_T(const EeParams& P, const EeBeamSpec* specs, const EeBeamGeom* geoms,
                               const float* unit_terma, const int* beamlet_idx, const float* terma_grad,
-                              float* fluence_grad, int nbeams, cudaStream_t s) {
+                              float* fluence_grad, int nbeams, long long max_tvol, cudaStream_t s) {
     (void)geoms;
-    long long nbbox = (long long)P.bbs[0] * P.bbs[1] * P.bbs[2];
-    dim3 grid(grid1(nbbox, 256), 1, nbeams);
-    k_terma_T<<<grid, 256, 0, s>>>(P, specs, unit_terma, beamlet_idx, terma_grad, fluence_grad, nbbox);
+    dim3 grid(grid1(max_tvol, 256), 1, nbeams);
+    k_terma_T<<<grid, 256, 0, s>>>(P, specs, unit_terma, beamlet_idx, terma_grad, fluence_grad);
     return cudaGetLastError();
 }
