@@ -205,8 +205,7 @@ def main():
     torch.cuda.synchronize()
 
     def step_device():
-        eng.beam_dose_device(beams, d_fl.data_ptr(), d_dose.data_ptr(), engine.DOSE_SUM)
-        eng.beam_dose_adjoint_device(beams, d_fl.data_ptr(), d_grad.data_ptr(), d_fgrad.data_ptr())
+        eng.dose_and_adjoint_device(beams, d_fl.data_ptr(), d_dose.data_ptr(), d_grad.data_ptr(), d_fgrad.data_ptr())
 
     for _ in range(args.warmup):
         step_device()
@@ -250,10 +249,9 @@ def main():
     eb = engine.to_ee_beams(beams)
 
     def step_host():
-        eng._check(eng.lib.ee_beam_dose(eng.h, eb, len(beams), C.c_void_p(pin_fl.ctypes.data),
-                                        C.c_void_p(pin_dose.ctypes.data), engine.DOSE_SUM))
-        eng._check(eng.lib.ee_beam_dose_adjoint(eng.h, eb, len(beams), C.c_void_p(pin_fl.ctypes.data),
-                                                C.c_void_p(pin_grad.ctypes.data), C.c_void_p(pin_fgrad.ctypes.data)))
+        eng._check(eng.lib.ee_dose_and_adjoint(eng.h, eb, len(beams), C.c_void_p(pin_fl.ctypes.data),
+                                               C.c_void_p(pin_dose.ctypes.data), engine.DOSE_SUM,
+                                               C.c_void_p(pin_grad.ctypes.data), C.c_void_p(pin_fgrad.ctypes.data)))
 
     step_host()
     barrier(ws)
@@ -266,7 +264,7 @@ def main():
     barrier(ws)
     t_e2e = max_over_ranks(sum(e2e_lat), ws)
     e2e = ws * len(beams) * args.steps / t_e2e
-    h2d = pin_fl.nbytes * 2 + pin_grad.nbytes
+    h2d = pin_fl.nbytes + pin_grad.nbytes
     d2h = pin_dose.nbytes + pin_fgrad.nbytes
 
     # plain per-beam path: one beam per call
@@ -278,9 +276,8 @@ def main():
     t0 = time.perf_counter()
     for i, b in enumerate(pb):
         s0 = time.perf_counter()
-        eng.beam_dose_device([b], d_fl.data_ptr() + 4 * int(offs[i]), d_dose.data_ptr(), engine.DOSE_SUM)
-        eng.beam_dose_adjoint_device([b], d_fl.data_ptr() + 4 * int(offs[i]), d_grad.data_ptr(),
-                                     d_fgrad.data_ptr() + 4 * int(offs[i]))
+        eng.dose_and_adjoint_device([b], d_fl.data_ptr() + 4 * int(offs[i]), d_dose.data_ptr(), d_grad.data_ptr(),
+                                    d_fgrad.data_ptr() + 4 * int(offs[i]))
         eng.synchronize()
         lat.append(time.perf_counter() - s0)
     plain = npl / (time.perf_counter() - t0)

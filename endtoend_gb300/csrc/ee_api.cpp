@@ -157,6 +157,8 @@ struct ee_context {
     DevBuf<float> terma, unit, rev, rev_grad, terma_grad;
     DevBuf<int> bl_idx;
     DevBuf<float> io_fluence, io_dose, io_grad;
+    DevBuf<float> xf, xg, spread_w;
+    DevBuf<double> acc;
     PinBuf<EeBeamSpec> h_specs;
     PinBuf<EeBeamGeom> h_geoms;
     std::vector<EeBeamGeom> last_geoms;
@@ -321,16 +323,16 @@ cudaError_t staged(ee_context* c, int stage, int nlaunch, F fn) {
 long long nfull_of(const ee_context* c) { return (long long)c->P.size[0] * c->P.size[1] * c->P.size[2]; }
 
 // Beams per chunk so that TERMA (+unit/index for the adjoint) fits the budget.
-// Split the beams into chunks whose device scratch fits the budget: TERMA
-// box (x4 for the adjoint's unit TERMA, beamlet index and TERMA gradient)
-// plus an estimate of the REV arena (nrays x 4 x the TERMA box, x2 for the
-// adjoint's REV gradient).
+// Split the beams into chunks whose REV arena fits the scratch budget
+// (estimate: nrays x 4 x the TERMA box per beam, x2 with the adjoint's REV
+// gradient).  TERMA boxes of all beams stay resident for the whole call so
+// the adjoint reuses the forward's TERMA, crop boxes and REV frames.
 std::vector<int> plan_chunks(const ee_context* c, const EeBeamSpec* specs, int nbeams, bool adjoint) {
     std::vector<int> starts;
     long long acc = 0;
-    const long long per_vox = 4ll * ((adjoint ? 4 : 1) + (long long)c->P.nrays * 4 * (adjoint ? 2 : 1));
+    const long long per_vox = 4ll * (long long)c->P.nrays * 4 * (adjoint ? 2 : 1);
     for (int b = 0; b < nbeams; b++) {
-        long long need = std::max(1ll, tvol_of(specs[b])) * per_vox + sizeof(EeBeamGeom);
+        long long need = std::max(1ll, tvol_of(specs[b])) * per_vox;
         if (starts.empty() || (acc + need > c->max_batch_bytes && acc > 0)) {
             starts.push_back(b);
             acc = 0;
@@ -341,135 +343,162 @@ std::vector<int> plan_chunks(const ee_context* c, const EeBeamSpec* specs, int n
     return starts;
 }
 
-// Stages 1-3 for a chunk: specs up, TERMA + crop box, geometry, read-back,
-// REV arena offsets.  On return h_geoms holds the chunk's geometry.
 struct ChunkDims {
-    long long rev_total = 0, tvol_total = 0, max_tvol = 1;
+    long long rev_total = 0, max_tvol = 1;
     int max_line = 1, max_lines = 1, max_rows = 1;
 };
 
-int run_front(ee_context* c, const EeBeamSpec* specs_in, int nb, const float* d_fluence, bool adjoint, ChunkDims& D) {
+// Device buffer growth: a freed buffer may still be read by queued kernels,
+// so drain the stream first when a buffer has to grow.
+template <class T>
+cudaError_t grow(ee_context* c, DevBuf<T>& b, size_t n) {
+    if (n <= b.n && b.p) return cudaSuccess;
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return e;
+    return b.ensure(n);
+}
+
+struct PipeArgs {
+    const ee_beam* beams = nullptr;
+    int nbeams = 0;
+    const float* d_fluence = nullptr;  // fluence the dose engine sees
+    float* d_dose = nullptr;           // forward output (nullptr: no forward dose)
+    int dose_mode = EE_DOSE_SUM;
+    const float* d_dose_grad = nullptr;  // adjoint input given by the caller
+    const ee_loss* loss = nullptr;       // or: gradient of the EndtoEnd dose terms
+    float* d_fgrad = nullptr;            // adjoint output (nullptr: no adjoint)
+    double* loss_acc = nullptr;          // device accumulator [3] for loss terms
+};
+
+// One call of the CCCS chain over a list of beams:
+//   geometry pass per chunk (TERMA + crop box + REV frames, one read-back)
+//   with the forward dose (REV cones + gather) when requested, then the loss
+//   gradient, then the adjoint per chunk reusing the resident TERMA/geometry.
+int pipeline(ee_context* c, const PipeArgs& A) {
+    int st = check_ready(c);
+    if (st) return st;
+    if ((st = check_beams(A.beams, A.nbeams))) return st;
+    if (!A.d_fluence) return fail(EE_ERR_INVALID_ARG, "null fluence pointer");
+    if (A.dose_mode < 0 || A.dose_mode > 2) return fail(EE_ERR_INVALID_ARG, "bad dose mode %d", A.dose_mode);
+    const bool fwd = A.d_dose != nullptr;
+    const bool adj = A.d_fgrad != nullptr;
+    if (adj && !A.d_dose_grad && !A.loss) return fail(EE_ERR_INVALID_ARG, "adjoint needs a dose gradient or a loss");
+    if (A.loss && (!fwd || A.dose_mode != EE_DOSE_SUM)) return fail(EE_ERR_INVALID_ARG, "loss needs the summed dose");
+    EE_CUDA(cudaSetDevice(c->device));
     cudaStream_t s = c->stream;
-    EE_CUDA(c->h_specs.ensure(nb));
-    EE_CUDA(c->h_geoms.ensure(nb));
-    EE_CUDA(c->d_specs.ensure(nb));
-    EE_CUDA(c->d_geoms.ensure(nb));
-    // re-base the chunk's fluence and TERMA offsets
-    D = ChunkDims();
-    const long long fl0 = specs_in[0].fl_off;
-    for (int b = 0; b < nb; b++) {
-        EeBeamSpec& S = c->h_specs.p[b];
-        S = specs_in[b];
-        S.fl_off -= fl0;
-        S.t_off = D.tvol_total;
-        D.tvol_total += tvol_of(S);
-        D.max_tvol = std::max(D.max_tvol, tvol_of(S));
+    const int n = A.nbeams;
+    const long long nfull = nfull_of(c);
+    EE_CUDA(c->h_specs.ensure(n));
+    EE_CUDA(c->h_geoms.ensure(n));
+    build_specs(c->P, A.beams, n, c->h_specs.p);
+    long long tvol_total = 0;
+    for (int b = 0; b < n; b++) tvol_total += tvol_of(c->h_specs.p[b]);
+    EE_CUDA(grow(c, c->d_specs, n));
+    EE_CUDA(grow(c, c->d_geoms, n));
+    EE_CUDA(grow(c, c->terma, tvol_total));
+    if (adj) {
+        EE_CUDA(grow(c, c->unit, tvol_total));
+        EE_CUDA(grow(c, c->bl_idx, tvol_total));
+        EE_CUDA(grow(c, c->terma_grad, tvol_total));
     }
-    EE_CUDA(cudaMemcpyAsync(c->d_specs.p, c->h_specs.p, sizeof(EeBeamSpec) * nb, cudaMemcpyHostToDevice, s));
-    EE_CUDA(c->terma.ensure((size_t)D.tvol_total));
-    if (adjoint) {
-        EE_CUDA(c->unit.ensure((size_t)D.tvol_total));
-        EE_CUDA(c->bl_idx.ensure((size_t)D.tvol_total));
+    EE_CUDA(cudaMemcpyAsync(c->d_specs.p, c->h_specs.p, sizeof(EeBeamSpec) * n, cudaMemcpyHostToDevice, s));
+    std::vector<int> starts = plan_chunks(c, c->h_specs.p, n, adj);
+    const int nchunks = (int)starts.size() - 1;
+    std::vector<ChunkDims> dims(nchunks);
+    c->last_geoms.clear();
+    c->last_specs.assign(c->h_specs.p, c->h_specs.p + n);
+    if (fwd && A.dose_mode == EE_DOSE_SUM) EE_CUDA(cudaMemsetAsync(A.d_dose, 0, sizeof(float) * nfull, s));
+    if (fwd && A.dose_mode == EE_DOSE_PER_BEAM) EE_CUDA(cudaMemsetAsync(A.d_dose, 0, sizeof(float) * nfull * n, s));
+
+    // ---- geometry + forward, chunk by chunk
+    for (int k = 0; k < nchunks; k++) {
+        const int b0 = starts[k], nb = starts[k + 1] - b0;
+        EeBeamSpec* dsp = c->d_specs.p + b0;
+        EeBeamGeom* dge = c->d_geoms.p + b0;
+        ChunkDims& D = dims[k];
+        for (int b = b0; b < b0 + nb; b++) D.max_tvol = std::max(D.max_tvol, tvol_of(c->h_specs.p[b]));
+        EE_CUDA(staged(c, EE_STAGE_GEOMETRY, 1, [&] { return ee_launch_geom_init(dge, nb, s); }));
+        EE_CUDA(staged(c, EE_STAGE_TERMA, 1, [&] {
+            return ee_launch_terma(c->P, dsp, dge, A.d_fluence, c->terma.p, adj ? c->unit.p : nullptr,
+                                   adj ? c->bl_idx.p : nullptr, nb, D.max_tvol, s);
+        }));
+        EE_CUDA(staged(c, EE_STAGE_GEOMETRY, 1, [&] { return ee_launch_geometry(c->P, dsp, dge, nb, s); }));
+        EeBeamGeom* hg = c->h_geoms.p + b0;
+        EE_CUDA(cudaMemcpyAsync(hg, dge, sizeof(EeBeamGeom) * nb, cudaMemcpyDeviceToHost, s));
+        EE_CUDA(cudaStreamSynchronize(s));
+        for (int b = 0; b < nb; b++) {
+            EeBeamGeom& G = hg[b];
+            if (G.status != 0) return fail(G.status, "beam %d: %s", b0 + b, status_text(G.status));
+            G.arena_off = D.rev_total;
+            G.arena_cap = G.rev_total;
+            D.rev_total += G.rev_total;
+            D.max_line = std::max(D.max_line, G.max_line);
+            D.max_lines = std::max(D.max_lines, G.max_lines);
+            D.max_rows = std::max(D.max_rows, G.rows);
+        }
+        EE_CUDA(cudaMemcpyAsync(dge, hg, sizeof(EeBeamGeom) * nb, cudaMemcpyHostToDevice, s));
+        c->last_geoms.insert(c->last_geoms.end(), hg, hg + nb);
+        if (!fwd) continue;
+        EE_CUDA(grow(c, c->rev, D.rev_total));
+        EE_CUDA(staged(c, EE_STAGE_CONE, 1, [&] {
+            return ee_launch_cone(c->P, dsp, dge, c->terma.p, c->rev.p, nb, D.max_lines, D.max_line, s);
+        }));
+        float* out = A.dose_mode == EE_DOSE_PER_BEAM ? A.d_dose + (long long)b0 * nfull : A.d_dose;
+        const int m = A.dose_mode == EE_DOSE_PER_BEAM ? 2 : 1;
+        EE_CUDA(staged(c, EE_STAGE_GATHER, 1, [&] {
+            return ee_launch_gather(c->P, dsp, dge, c->rev.p, out, nb, m, D.max_rows, s);
+        }));
     }
-    EE_CUDA(staged(c, EE_STAGE_GEOMETRY, 1, [&] { return ee_launch_geom_init(c->d_geoms.p, nb, s); }));
-    EE_CUDA(staged(c, EE_STAGE_TERMA, 1, [&] {
-        return ee_launch_terma(c->P, c->d_specs.p, c->d_geoms.p, d_fluence, c->terma.p, adjoint ? c->unit.p : nullptr,
-                               adjoint ? c->bl_idx.p : nullptr, nb, D.max_tvol, s);
-    }));
-    EE_CUDA(staged(c, EE_STAGE_GEOMETRY, 1, [&] { return ee_launch_geometry(c->P, c->d_specs.p, c->d_geoms.p, nb, s); }));
-    EE_CUDA(cudaMemcpyAsync(c->h_geoms.p, c->d_geoms.p, sizeof(EeBeamGeom) * nb, cudaMemcpyDeviceToHost, s));
-    EE_CUDA(cudaStreamSynchronize(s));
-    for (int b = 0; b < nb; b++) {
-        EeBeamGeom& G = c->h_geoms.p[b];
-        if (G.status != 0) return fail(G.status, "beam %d: %s", b, status_text(G.status));
-        G.arena_off = D.rev_total;
-        G.arena_cap = G.rev_total;
-        D.rev_total += G.rev_total;
-        D.max_line = std::max(D.max_line, G.max_line);
-        D.max_lines = std::max(D.max_lines, G.max_lines);
-        D.max_rows = std::max(D.max_rows, G.rows);
+    if (!adj) return EE_OK;
+
+    // ---- dose gradient of the loss
+    const float* dgrad = A.d_dose_grad;
+    if (A.loss) {
+        EE_CUDA(grow(c, c->io_grad, nfull));
+        EE_CUDA(ee_launch_loss_grad(A.d_dose, A.loss->ptv_weight, A.loss->ptv_target, A.loss->oar_weight,
+                                    A.loss->oar_target, c->io_grad.p, A.loss_acc, nfull, s));
+        dgrad = c->io_grad.p;
     }
-    EE_CUDA(cudaMemcpyAsync(c->d_geoms.p, c->h_geoms.p, sizeof(EeBeamGeom) * nb, cudaMemcpyHostToDevice, s));
-    c->last_geoms.insert(c->last_geoms.end(), c->h_geoms.p, c->h_geoms.p + nb);
-    c->last_specs.insert(c->last_specs.end(), c->h_specs.p, c->h_specs.p + nb);
+
+    // ---- adjoint, chunk by chunk (same plan, geometry resident)
+    long long nfl_all = 0;
+    for (int b = 0; b < n; b++) nfl_all += (long long)A.beams[b].fmap_size[0] * A.beams[b].fmap_size[1];
+    EE_CUDA(cudaMemsetAsync(A.d_fgrad, 0, sizeof(float) * nfl_all, s));
+    EE_CUDA(cudaMemsetAsync(c->terma_grad.p, 0, sizeof(float) * tvol_total, s));
+    for (int k = 0; k < nchunks; k++) {
+        const int b0 = starts[k], nb = starts[k + 1] - b0;
+        const EeBeamSpec* dsp = c->d_specs.p + b0;
+        const EeBeamGeom* dge = c->d_geoms.p + b0;
+        const ChunkDims& D = dims[k];
+        EE_CUDA(grow(c, c->rev_grad, D.rev_total));
+        EE_CUDA(cudaMemsetAsync(c->rev_grad.p, 0, sizeof(float) * D.rev_total, s));
+        EE_CUDA(staged(c, EE_STAGE_GATHER_T, 1, [&] {
+            return ee_launch_gather_T(c->P, dsp, dge, dgrad, c->rev_grad.p, nb, D.max_rows, s);
+        }));
+        EE_CUDA(staged(c, EE_STAGE_CONE_T, 1, [&] {
+            return ee_launch_cone_T(c->P, dsp, dge, c->rev_grad.p, c->terma_grad.p, nb, D.max_lines, D.max_line, s);
+        }));
+        EE_CUDA(staged(c, EE_STAGE_TERMA_T, 1, [&] {
+            return ee_launch_terma_T(c->P, dsp, dge, c->unit.p, c->bl_idx.p, c->terma_grad.p, A.d_fgrad, nb,
+                                     D.max_tvol, s);
+        }));
+    }
     return EE_OK;
 }
 
 int dose_device(ee_context* c, const ee_beam* beams, int nbeams, const float* d_fluence, float* d_dose, int mode) {
-    int st = check_ready(c);
-    if (st) return st;
-    if ((st = check_beams(beams, nbeams))) return st;
-    if (!d_fluence || !d_dose) return fail(EE_ERR_INVALID_ARG, "null fluence/dose pointer");
-    if (mode < 0 || mode > 2) return fail(EE_ERR_INVALID_ARG, "bad dose mode %d", mode);
-    EE_CUDA(cudaSetDevice(c->device));
-    const long long nfull = nfull_of(c);
-    std::vector<EeBeamSpec> specs(nbeams);
-    build_specs(c->P, beams, nbeams, specs.data());
-    std::vector<int> starts = plan_chunks(c, specs.data(), nbeams, false);
-    c->last_geoms.clear();
-    c->last_specs.clear();
-    if (mode == EE_DOSE_SUM) EE_CUDA(cudaMemsetAsync(d_dose, 0, sizeof(float) * nfull, c->stream));
-    if (mode == EE_DOSE_PER_BEAM)
-        EE_CUDA(cudaMemsetAsync(d_dose, 0, sizeof(float) * nfull * nbeams, c->stream));
-    for (size_t k = 0; k + 1 < starts.size(); k++) {
-        const int b0 = starts[k], nb = starts[k + 1] - b0;
-        ChunkDims D;
-        st = run_front(c, specs.data() + b0, nb, d_fluence + specs[b0].fl_off, false, D);
-        if (st) return st;
-        EE_CUDA(c->rev.ensure((size_t)D.rev_total));
-        EE_CUDA(staged(c, EE_STAGE_CONE, 1, [&] {
-            return ee_launch_cone(c->P, c->d_specs.p, c->d_geoms.p, c->terma.p, c->rev.p, nb, D.max_lines, D.max_line,
-                                  c->stream);
-        }));
-        float* out = mode == EE_DOSE_PER_BEAM ? d_dose + (long long)b0 * nfull : d_dose;
-        const int m = mode == EE_DOSE_PER_BEAM ? 2 : 1;
-        EE_CUDA(staged(c, EE_STAGE_GATHER, 1, [&] {
-            return ee_launch_gather(c->P, c->d_specs.p, c->d_geoms.p, c->rev.p, out, nb, m, D.max_rows, c->stream);
-        }));
-        if (k + 2 < starts.size()) EE_CUDA(cudaStreamSynchronize(c->stream));  // scratch reuse
-    }
-    return EE_OK;
+    if (!d_dose) return fail(EE_ERR_INVALID_ARG, "null dose pointer");
+    PipeArgs A;
+    A.beams = beams; A.nbeams = nbeams; A.d_fluence = d_fluence; A.d_dose = d_dose; A.dose_mode = mode;
+    return pipeline(c, A);
 }
 
 int adjoint_device(ee_context* c, const ee_beam* beams, int nbeams, const float* d_fluence, const float* d_grad,
                    float* d_fgrad) {
-    int st = check_ready(c);
-    if (st) return st;
-    if ((st = check_beams(beams, nbeams))) return st;
-    if (!d_fluence || !d_grad || !d_fgrad) return fail(EE_ERR_INVALID_ARG, "null pointer");
-    EE_CUDA(cudaSetDevice(c->device));
-    std::vector<EeBeamSpec> specs(nbeams);
-    build_specs(c->P, beams, nbeams, specs.data());
-    std::vector<int> starts = plan_chunks(c, specs.data(), nbeams, true);
-    c->last_geoms.clear();
-    c->last_specs.clear();
-    long long nfl_all = 0;
-    for (int b = 0; b < nbeams; b++) nfl_all += (long long)beams[b].fmap_size[0] * beams[b].fmap_size[1];
-    EE_CUDA(cudaMemsetAsync(d_fgrad, 0, sizeof(float) * nfl_all, c->stream));
-    for (size_t k = 0; k + 1 < starts.size(); k++) {
-        const int b0 = starts[k], nb = starts[k + 1] - b0;
-        const long long fl0 = specs[b0].fl_off;
-        ChunkDims D;
-        st = run_front(c, specs.data() + b0, nb, d_fluence + fl0, true, D);
-        if (st) return st;
-        EE_CUDA(c->rev_grad.ensure((size_t)D.rev_total));
-        EE_CUDA(c->terma_grad.ensure((size_t)D.tvol_total));
-        EE_CUDA(cudaMemsetAsync(c->rev_grad.p, 0, sizeof(float) * D.rev_total, c->stream));
-        EE_CUDA(cudaMemsetAsync(c->terma_grad.p, 0, sizeof(float) * D.tvol_total, c->stream));
-        EE_CUDA(staged(c, EE_STAGE_GATHER_T, 1, [&] {
-            return ee_launch_gather_T(c->P, c->d_specs.p, c->d_geoms.p, d_grad, c->rev_grad.p, nb, D.max_rows, c->stream);
-        }));
-        EE_CUDA(staged(c, EE_STAGE_CONE_T, 1, [&] {
-            return ee_launch_cone_T(c->P, c->d_specs.p, c->d_geoms.p, c->rev_grad.p, c->terma_grad.p, nb, D.max_lines,
-                                    D.max_line, c->stream);
-        }));
-        EE_CUDA(staged(c, EE_STAGE_TERMA_T, 1, [&] {
-            return ee_launch_terma_T(c->P, c->d_specs.p, c->d_geoms.p, c->unit.p, c->bl_idx.p, c->terma_grad.p,
-                                     d_fgrad + fl0, nb, D.max_tvol, c->stream);
-        }));
-        if (k + 2 < starts.size()) EE_CUDA(cudaStreamSynchronize(c->stream));
-    }
-    return EE_OK;
+    if (!d_grad || !d_fgrad) return fail(EE_ERR_INVALID_ARG, "null pointer");
+    PipeArgs A;
+    A.beams = beams; A.nbeams = nbeams; A.d_fluence = d_fluence; A.d_dose_grad = d_grad; A.d_fgrad = d_fgrad;
+    return pipeline(c, A);
 }
 
 // max_rev_size as initCudaConstandTex derives it when the caller gives none
@@ -526,6 +555,7 @@ int ee_destroy(ee_context* c) {
     c->d_specs.release(); c->d_geoms.release(); c->terma.release(); c->unit.release(); c->rev.release();
     c->rev_grad.release(); c->terma_grad.release(); c->bl_idx.release();
     c->io_fluence.release(); c->io_dose.release(); c->io_grad.release();
+    c->xf.release(); c->xg.release(); c->spread_w.release(); c->acc.release();
     c->h_specs.release(); c->h_geoms.release();
     drain_profile(c);
     for (auto e : c->event_pool) cudaEventDestroy(e);
@@ -698,6 +728,107 @@ int ee_beam_dose_adjoint(ee_context* c, const ee_beam* beams, int nbeams, const 
     if (st) return st;
     EE_CUDA(cudaMemcpyAsync(fgrad, c->io_grad.p + nfull, sizeof(float) * nfl, cudaMemcpyDeviceToHost, c->stream));
     EE_CUDA(cudaStreamSynchronize(c->stream));
+    return EE_OK;
+}
+
+int ee_dose_and_adjoint_device(ee_context* c, const ee_beam* beams, int nbeams, const float* d_fluence, float* d_dose,
+                               int dose_mode, const float* d_grad, float* d_fgrad) {
+    if (!c) return fail(EE_ERR_INVALID_ARG, "null context");
+    std::lock_guard<std::mutex> lk(c->mu);
+    if ((d_fgrad == nullptr) != (d_grad == nullptr)) return fail(EE_ERR_INVALID_ARG, "adjoint needs both gradient pointers");
+    PipeArgs A;
+    A.beams = beams; A.nbeams = nbeams; A.d_fluence = d_fluence; A.d_dose = d_dose; A.dose_mode = dose_mode;
+    A.d_dose_grad = d_grad; A.d_fgrad = d_fgrad;
+    return pipeline(c, A);
+}
+
+int ee_dose_and_adjoint(ee_context* c, const ee_beam* beams, int nbeams, const float* fluence, float* dose, int dose_mode,
+                        const float* grad, float* fgrad) {
+    if (!c) return fail(EE_ERR_INVALID_ARG, "null context");
+    int st = check_ready(c);
+    if (st) return st;
+    if ((st = check_beams(beams, nbeams))) return st;
+    if (!fluence || (!dose && !fgrad) || ((fgrad == nullptr) != (grad == nullptr)))
+        return fail(EE_ERR_INVALID_ARG, "null pointer");
+    if (dose_mode < 0 || dose_mode > 2) return fail(EE_ERR_INVALID_ARG, "bad dose mode %d", dose_mode);
+    std::lock_guard<std::mutex> lk(c->mu);
+    EE_CUDA(cudaSetDevice(c->device));
+    cudaStream_t s = c->stream;
+    const long long nfl = total_fluence(beams, nbeams), nfull = nfull_of(c);
+    const long long nout = dose ? nfull * (dose_mode == EE_DOSE_PER_BEAM ? nbeams : 1) : 0;
+    EE_CUDA(grow(c, c->io_fluence, 2 * nfl));
+    EE_CUDA(grow(c, c->io_dose, std::max(1ll, nout) + (grad ? nfull : 0)));
+    EE_CUDA(cudaMemcpyAsync(c->io_fluence.p, fluence, sizeof(float) * nfl, cudaMemcpyHostToDevice, s));
+    float* d_dose = dose ? c->io_dose.p : nullptr;
+    float* d_grad = grad ? c->io_dose.p + std::max(1ll, nout) : nullptr;
+    if (dose && dose_mode == EE_DOSE_ACCUMULATE)
+        EE_CUDA(cudaMemcpyAsync(d_dose, dose, sizeof(float) * nout, cudaMemcpyHostToDevice, s));
+    if (grad) EE_CUDA(cudaMemcpyAsync(d_grad, grad, sizeof(float) * nfull, cudaMemcpyHostToDevice, s));
+    PipeArgs A;
+    A.beams = beams; A.nbeams = nbeams; A.d_fluence = c->io_fluence.p; A.d_dose = d_dose; A.dose_mode = dose_mode;
+    A.d_dose_grad = d_grad; A.d_fgrad = fgrad ? c->io_fluence.p + nfl : nullptr;
+    st = pipeline(c, A);
+    if (st) return st;
+    if (dose) EE_CUDA(cudaMemcpyAsync(dose, d_dose, sizeof(float) * nout, cudaMemcpyDeviceToHost, s));
+    if (fgrad) EE_CUDA(cudaMemcpyAsync(fgrad, c->io_fluence.p + nfl, sizeof(float) * nfl, cudaMemcpyDeviceToHost, s));
+    EE_CUDA(cudaStreamSynchronize(s));
+    return EE_OK;
+}
+
+int ee_loss_and_grad(ee_context* c, const ee_beam* beams, int nbeams, const float* d_x, const ee_loss* loss,
+                     float* d_dose, float* d_xgrad, double loss_out[3]) {
+    if (!c || !loss || !d_x || !d_dose || !d_xgrad) return fail(EE_ERR_INVALID_ARG, "null argument");
+    if (!(loss->eta >= 0) || !(loss->spread_sigma >= 0)) return fail(EE_ERR_INVALID_ARG, "bad eta / spread sigma");
+    if ((loss->ptv_weight == nullptr) != (loss->ptv_target == nullptr) ||
+        (loss->oar_weight == nullptr) != (loss->oar_target == nullptr))
+        return fail(EE_ERR_INVALID_ARG, "weight and target arrays come in pairs");
+    int st = check_ready(c);
+    if (st) return st;
+    if ((st = check_beams(beams, nbeams))) return st;
+    std::lock_guard<std::mutex> lk(c->mu);
+    EE_CUDA(cudaSetDevice(c->device));
+    cudaStream_t s = c->stream;
+    long long nfl = total_fluence(beams, nbeams);
+    int max_pix = 1;
+    for (int b = 0; b < nbeams; b++) max_pix = std::max(max_pix, beams[b].fmap_size[0] * beams[b].fmap_size[1]);
+    EE_CUDA(grow(c, c->acc, 3));
+    EE_CUDA(cudaMemsetAsync(c->acc.p, 0, 3 * sizeof(double), s));
+    // fluence seen by the dose engine: G * x
+    const float* f = d_x;
+    int R = 0;
+    if (loss->spread_sigma > 0) {
+        R = (int)std::ceil(3.0 * loss->spread_sigma);
+        std::vector<float> w(2 * R + 1);
+        double sum = 0;
+        for (int k = -R; k <= R; k++) sum += (w[k + R] = (float)std::exp(-0.5 * k * k / (loss->spread_sigma * loss->spread_sigma)));
+        for (auto& v : w) v = (float)(v / sum);
+        EE_CUDA(grow(c, c->spread_w, w.size()));
+        EE_CUDA(cudaMemcpyAsync(c->spread_w.p, w.data(), sizeof(float) * w.size(), cudaMemcpyHostToDevice, s));
+        EE_CUDA(c->h_specs.ensure(nbeams));
+        build_specs(c->P, beams, nbeams, c->h_specs.p);
+        EE_CUDA(grow(c, c->d_specs, nbeams));
+        EE_CUDA(cudaMemcpyAsync(c->d_specs.p, c->h_specs.p, sizeof(EeBeamSpec) * nbeams, cudaMemcpyHostToDevice, s));
+        EE_CUDA(grow(c, c->xf, nfl));
+        EE_CUDA(ee_launch_spread(c->d_specs.p, d_x, c->xf.p, c->spread_w.p, R, nbeams, max_pix, s));
+        f = c->xf.p;
+    }
+    PipeArgs A;
+    A.beams = beams; A.nbeams = nbeams; A.d_fluence = f; A.d_dose = d_dose; A.dose_mode = EE_DOSE_SUM;
+    A.loss = loss; A.loss_acc = c->acc.p;
+    float* fg = d_xgrad;
+    if (R > 0) {
+        EE_CUDA(grow(c, c->xg, nfl));
+        fg = c->xg.p;
+    }
+    A.d_fgrad = fg;
+    st = pipeline(c, A);
+    if (st) return st;
+    if (R > 0) EE_CUDA(ee_launch_spread(c->d_specs.p, c->xg.p, d_xgrad, c->spread_w.p, R, nbeams, max_pix, s));
+    if (loss->eta > 0) EE_CUDA(ee_launch_smooth(c->d_specs.p, d_x, d_xgrad, loss->eta, c->acc.p, nbeams, max_pix, s));
+    double h[3];
+    EE_CUDA(cudaMemcpyAsync(h, c->acc.p, sizeof(h), cudaMemcpyDeviceToHost, s));
+    EE_CUDA(cudaStreamSynchronize(s));
+    if (loss_out) for (int k = 0; k < 3; k++) loss_out[k] = h[k];
     return EE_OK;
 }
 

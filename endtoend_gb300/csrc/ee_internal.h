@@ -116,3 +116,10 @@ cudaError_t ee_launch_cone_T(const EeParams& P, const EeBeamSpec* specs, const E
 cudaError_t ee_launch_terma_T(const EeParams& P, const EeBeamSpec* specs, const EeBeamGeom* geoms,
                               const float* unit_terma, const int* beamlet_idx, const float* terma_grad,
                               float* fluence_grad, int nbeams, long long max_tvol, cudaStream_t s);
+// EndtoEnd loss pieces
+cudaError_t ee_launch_loss_grad(const float* dose, const float* ptv_w, const float* ptv_t, const float* oar_w,
+                                const float* oar_t, float* grad, double* acc, long long n, cudaStream_t s);
+cudaError_t ee_launch_spread(const EeBeamSpec* specs, const float* in, float* out, const float* w1d, int R, int nbeams,
+                             int max_pix, cudaStream_t s);
+cudaError_t ee_launch_smooth(const EeBeamSpec* specs, const float* x, float* grad, float eta, double* acc, int nbeams,
+                             int max_pix, cudaStream_t s);

@@ -18,6 +18,7 @@
 // Adjoint: k_gather_T (scatter), k_cone_T (reverse scans + TERMA scatter),
 // k_terma_T (per-beamlet reduction).
 #include "ee_internal.h"
+#include <algorithm>
 #include <cfloat>
 
 namespace {
@@ -388,23 +389,56 @@ __global__ void k_geometry(EeParams P, const EeBeamSpec* __restrict__ specs, EeB
 
 
 // ------------------------------------------------------- cone: gather ----
-// REV resample of one line into shared memory (device.cu:47-79): density
-// sentinel -3 outside the BEV crop box, -2 outside the calc bbox; TERMA is
-// zero at sentinel samples (never written by the reference).
+// Samples of REV line (tY, tZ) that can be valid: the line's intersection
+// with the BEV crop box and the calc bbox (both convex, so one segment),
+// widened by one sample for rounding.  Outside it every sample is a sentinel
+// (-3 outside the BEV box, -2 outside the bbox, device.cu:51-70) and its dose
+// is zero, so neither the gather nor the scans visit it.
+__device__ __forceinline__ void line_segment(const EeParams& P, const EeBeamGeom& G, const EeRayGeom& R, int tY,
+                                             int tZ, int L, int& i0, int& n) {
+    const f3 bl = ld3(R.B0) + ld3(R.By) * (float)tY + ld3(R.Bz) * (float)tZ;
+    const f3 gl = ld3(R.G0) + ld3(R.Gy) * (float)tY + ld3(R.Gz) * (float)tZ;
+    const float c[6] = {bl.x, bl.y, bl.z, gl.x, gl.y, gl.z};
+    const float m[6] = {R.Bx[0], R.Bx[1], R.Bx[2], R.Gx[0], R.Gx[1], R.Gx[2]};
+    const float lo[6] = {0.f, 0.f, 0.f, (float)P.bb0[0], (float)P.bb0[1], (float)P.bb0[2]};
+    const float hi[6] = {(float)G.bev[0], (float)G.bev[1], (float)G.bev[2], (float)(P.bb0[0] + P.bbs[0]),
+                         (float)(P.bb0[1] + P.bbs[1]), (float)(P.bb0[2] + P.bbs[2])};
+    float a = 0.f, b = (float)(L - 1);
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        if (fabsf(m[k]) < 1e-6f) {
+            if (c[k] < lo[k] - 1e-3f || c[k] > hi[k] + 1e-3f) { n = 0; i0 = 0; return; }
+        } else {
+            float t0 = (lo[k] - c[k]) / m[k], t1 = (hi[k] - c[k]) / m[k];
+            a = fmaxf(a, fminf(t0, t1));
+            b = fminf(b, fmaxf(t0, t1));
+        }
+    }
+    if (!(a <= b + 2.f)) { n = 0; i0 = 0; return; }
+    i0 = max(0, (int)floorf(a) - 1);
+    int i1 = min(L - 1, (int)ceilf(b) + 1);
+    n = max(0, i1 - i0 + 1);
+}
+
+// REV resample of samples i0..i0+n-1 of one line into shared memory
+// (device.cu:47-79): density sentinel -3 outside the BEV crop box, -2 outside
+// the calc bbox; TERMA is zero at sentinel samples (never written by the
+// reference).
 __device__ __forceinline__ void gather_line(const EeParams& P, const EeBeamSpec& S, const EeBeamGeom& G,
                                             const EeRayGeom& R, const float* __restrict__ terma_b, int tY, int tZ,
-                                            int L, int lane, float* rho, float* T) {
+                                            int i0, int n, int lane, float* rho, float* T) {
     const f3 bl = ld3(R.B0) + ld3(R.By) * (float)tY + ld3(R.Bz) * (float)tZ;
     const f3 gl = ld3(R.G0) + ld3(R.Gy) * (float)tY + ld3(R.Gz) * (float)tZ;
     const f3 bx = ld3(R.Bx), gx = ld3(R.Gx);
     const float bsx = (float)G.bev[0], bsy = (float)G.bev[1], bsz = (float)G.bev[2];
     const float b0x = (float)P.bb0[0], b0y = (float)P.bb0[1], b0z = (float)P.bb0[2];
     const float b1x = (float)(P.bb0[0] + P.bbs[0]), b1y = (float)(P.bb0[1] + P.bbs[1]), b1z = (float)(P.bb0[2] + P.bbs[2]);
-    for (int i = lane; i < L; i += 32) {
-        f3 bev = bl + bx * (float)i;
+    for (int k = lane; k < n; k += 32) {
+        const float fi = (float)(i0 + k);
+        f3 bev = bl + bx * fi;
         float r = -3.f, t = 0.f;
         if (!(bev.x < 0.f || bev.y < 0.f || bev.z < 0.f || bev.x >= bsx || bev.y >= bsy || bev.z >= bsz)) {
-            f3 g = gl + gx * (float)i;
+            f3 g = gl + gx * fi;
             if (g.x < b0x || g.x >= b1x || g.y < b0y || g.y >= b1y || g.z < b0z || g.z >= b1z) {
                 r = -2.f;
             } else {
@@ -414,8 +448,8 @@ __device__ __forceinline__ void gather_line(const EeParams& P, const EeBeamSpec&
                                    g.z - (float)S.t0[2]);
             }
         }
-        rho[i] = r;
-        if (T) T[i] = t;
+        rho[k] = r;
+        if (T) T[k] = t;
     }
 }
 
@@ -591,25 +625,34 @@ __global__ void __launch_bounds__(CONE_WARPS * 32) k_cone(EeParams P, const EeBe
     float* rho = sm + (size_t)warp * 3 * maxL;
     float* T = rho + maxL;
     float* D = T + maxL;
-    gather_line(P, specs[b], G, R, terma + specs[b].t_off, tY, tZ, L, lane, rho, T);
-    __syncwarp();
     float* out = rev + G.arena_off + R.offset + (long long)line * L;
-    const float inv_nphi = 1.f / (float)P.nphi;
-    const EeRayConst& RC = P.rays[ray];
-    if (P.mode == 1) {
-        line_scan<true>(rho, T, L, lane, P.lng, P.expp + 4 * RC.row_fwd, D, out, inv_nphi);
+    int i0, n;
+    line_segment(P, G, R, tY, tZ, L, i0, n);
+    if (n > 0) {
+        gather_line(P, specs[b], G, R, terma + specs[b].t_off, tY, tZ, i0, n, lane, rho, T);
         __syncwarp();
-        line_scan<false>(rho, T, L, lane, P.lng, P.expp + 4 * RC.row_rev, D, out, inv_nphi);
-    } else {
-        for (int i = lane; i < L; i += 32) {
-            float v = 0.f;
-            if (rho[i] >= 0.f) {
-                v = table_walk(rho, T, L, i, -1, tabK, tabR, P.nradii, P.lng, nullptr, 0.f);
-                v += table_walk(rho, T, L, i, +1, tabK + EE_MAX_RADII, tabR, P.nradii, P.lng, nullptr, 0.f);
-                v = __fdiv_rn(v, (float)P.nphi);
+        const float inv_nphi = 1.f / (float)P.nphi;
+        const EeRayConst& RC = P.rays[ray];
+        if (P.mode == 1) {
+            line_scan<true>(rho, T, n, lane, P.lng, P.expp + 4 * RC.row_fwd, D, D, inv_nphi);
+            __syncwarp();
+            line_scan<false>(rho, T, n, lane, P.lng, P.expp + 4 * RC.row_rev, D, D, inv_nphi);
+        } else {
+            for (int k = lane; k < n; k += 32) {
+                float v = 0.f;
+                if (rho[k] >= 0.f) {
+                    v = table_walk(rho, T, n, k, -1, tabK, tabR, P.nradii, P.lng, nullptr, 0.f);
+                    v += table_walk(rho, T, n, k, +1, tabK + EE_MAX_RADII, tabR, P.nradii, P.lng, nullptr, 0.f);
+                    v = __fdiv_rn(v, (float)P.nphi);
+                }
+                D[k] = v;
             }
-            out[i] = v;
         }
+        __syncwarp();
+    }
+    for (int i = lane; i < L; i += 32) {
+        int k = i - i0;
+        out[i] = (k >= 0 && k < n) ? D[k] : 0.f;
     }
 }
 
@@ -644,24 +687,28 @@ __global__ void __launch_bounds__(CONE_WARPS * 32) k_cone_T(EeParams P, const Ee
     float* g = rho + maxL;
     float* Tb = g + maxL;
     const EeBeamSpec& S = specs[b];
-    gather_line(P, S, G, R, nullptr, tY, tZ, L, lane, rho, nullptr);
-    const float* gin = rev_grad + G.arena_off + R.offset + (long long)line * L;
+    int i0, n;
+    line_segment(P, G, R, tY, tZ, L, i0, n);
+    if (n == 0) return;
+    gather_line(P, S, G, R, nullptr, tY, tZ, i0, n, lane, rho, nullptr);
+    const float* gin = rev_grad + G.arena_off + R.offset + (long long)line * L + i0;
     const float inv_nphi = 1.f / (float)P.nphi;
-    for (int i = lane; i < L; i += 32) {
-        g[i] = rho[i] >= 0.f ? gin[i] * inv_nphi : 0.f;
-        Tb[i] = 0.f;
+    __syncwarp();
+    for (int k = lane; k < n; k += 32) {
+        g[k] = rho[k] >= 0.f ? gin[k] * inv_nphi : 0.f;
+        Tb[k] = 0.f;
     }
     __syncwarp();
     const EeRayConst& RC = P.rays[ray];
     if (P.mode == 1) {
-        line_scan_T<true>(rho, g, L, lane, P.lng, P.expp + 4 * RC.row_fwd, Tb);
+        line_scan_T<true>(rho, g, n, lane, P.lng, P.expp + 4 * RC.row_fwd, Tb);
         __syncwarp();
-        line_scan_T<false>(rho, g, L, lane, P.lng, P.expp + 4 * RC.row_rev, Tb);
+        line_scan_T<false>(rho, g, n, lane, P.lng, P.expp + 4 * RC.row_rev, Tb);
     } else {
-        for (int i = lane; i < L; i += 32) {
-            if (rho[i] >= 0.f && g[i] != 0.f) {
-                table_walk(rho, nullptr, L, i, -1, tabK, tabR, P.nradii, P.lng, Tb, g[i]);
-                table_walk(rho, nullptr, L, i, +1, tabK + EE_MAX_RADII, tabR, P.nradii, P.lng, Tb, g[i]);
+        for (int k = lane; k < n; k += 32) {
+            if (rho[k] >= 0.f && g[k] != 0.f) {
+                table_walk(rho, nullptr, n, k, -1, tabK, tabR, P.nradii, P.lng, Tb, g[k]);
+                table_walk(rho, nullptr, n, k, +1, tabK + EE_MAX_RADII, tabR, P.nradii, P.lng, Tb, g[k]);
             }
         }
     }
@@ -670,10 +717,10 @@ __global__ void __launch_bounds__(CONE_WARPS * 32) k_cone_T(EeParams P, const Ee
     const f3 gl = ld3(R.G0) + ld3(R.Gy) * (float)tY + ld3(R.Gz) * (float)tZ;
     const f3 gx = ld3(R.Gx);
     float* tg = terma_grad + S.t_off;
-    for (int i = lane; i < L; i += 32) {
-        float v = Tb[i];
-        if (rho[i] < 0.f || v == 0.f) continue;
-        f3 gp = gl + gx * (float)i;
+    for (int k = lane; k < n; k += 32) {
+        float v = Tb[k];
+        if (rho[k] < 0.f || v == 0.f) continue;
+        f3 gp = gl + gx * (float)(i0 + k);
         tri_border_scatter(tg, S.tn[0], S.tn[1], S.tn[2], gp.x - (float)S.t0[0], gp.y - (float)S.t0[1],
                            gp.z - (float)S.t0[2], v);
     }
@@ -891,5 +938,116 @@ cudaError_t ee_launch_terma_T(const EeParams& P, const EeBeamSpec* specs, const 
     (void)geoms;
     dim3 grid(grid1(max_tvol, 256), 1, nbeams);
     k_terma_T<<<grid, 256, 0, s>>>(P, specs, unit_terma, beamlet_idx, terma_grad, fluence_grad);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------- EndtoEnd loss terms ----
+// Dose terms of the EndtoEnd loss (README.md:20):
+//   L_d = sum_i w0_i (d_i - t0_i)^2 + sum_i w_i max(d_i - t_i, 0)^2
+// and its gradient dL/dd.  acc[0] += PTV term, acc[1] += OAR term.
+__global__ void __launch_bounds__(256) k_loss_grad(const float* __restrict__ dose, const float* __restrict__ ptv_w,
+                                                   const float* __restrict__ ptv_t, const float* __restrict__ oar_w,
+                                                   const float* __restrict__ oar_t, float* __restrict__ grad,
+                                                   double* __restrict__ acc, long long n) {
+    double lp = 0.0, lo = 0.0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        float d = dose[i];
+        float g = 0.f;
+        if (ptv_w) {
+            float w = ptv_w[i], e = d - ptv_t[i];
+            lp += (double)w * e * e;
+            g += 2.f * w * e;
+        }
+        if (oar_w) {
+            float w = oar_w[i], e = fmaxf(d - oar_t[i], 0.f);
+            lo += (double)w * e * e;
+            g += 2.f * w * e;
+        }
+        grad[i] = g;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        lp += __shfl_xor_sync(FULL, lp, o);
+        lo += __shfl_xor_sync(FULL, lo, o);
+    }
+    __shared__ double sp[8], so[8];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) { sp[w] = lp; so[w] = lo; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0, b = 0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); k++) { a += sp[k]; b += so[k]; }
+        atomicAdd(acc, a);
+        atomicAdd(acc + 1, b);
+    }
+}
+
+// Fluence-map convolution with a normalised 2-D Gaussian (the EndtoEnd
+// fluence-spread step, README.md:15-18), zero padding.  The kernel is
+// symmetric, so the same launch is its own transpose.  One thread per output
+// pixel of beam blockIdx.z.
+__global__ void __launch_bounds__(256) k_spread(const EeBeamSpec* __restrict__ specs, const float* __restrict__ in,
+                                                float* __restrict__ out, const float* __restrict__ w1d, int R) {
+    const EeBeamSpec& S = specs[blockIdx.z];
+    const int fx = S.fmap[0], fy = S.fmap[1];
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= fx * fy) return;
+    int x = p % fx, y = p / fx;
+    const float* src = in + S.fl_off;
+    float acc = 0.f;
+    for (int dy = -R; dy <= R; dy++) {
+        int yy = y + dy;
+        if (yy < 0 || yy >= fy) continue;
+        float wy = w1d[dy + R];
+        for (int dx = -R; dx <= R; dx++) {
+            int xx = x + dx;
+            if (xx < 0 || xx >= fx) continue;
+            acc += wy * w1d[dx + R] * src[xx + fx * yy];
+        }
+    }
+    out[S.fl_off + p] = acc;
+}
+
+// eta * ||D x||_1 with D the forward differences along both fluence-map axes
+// (BOO/BOO_QL/CreateDxDyFMO.m:1-36); adds eta * D^T sign(D x)
+// into grad and the term into acc[2].
+__global__ void __launch_bounds__(256) k_smooth(const EeBeamSpec* __restrict__ specs, const float* __restrict__ x,
+                                                float* __restrict__ grad, float eta, double* __restrict__ acc) {
+    const EeBeamSpec& S = specs[blockIdx.z];
+    const int fx = S.fmap[0], fy = S.fmap[1];
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    double l = 0.0;
+    if (p < fx * fy) {
+        int i = p % fx, j = p / fx;
+        const float* m = x + S.fl_off;
+        float v = m[p], g = 0.f;
+        if (i + 1 < fx) { float d = m[p + 1] - v; l += fabsf(d); g -= (d > 0.f) - (d < 0.f); }
+        if (i > 0) { float d = v - m[p - 1]; g += (d > 0.f) - (d < 0.f); }
+        if (j + 1 < fy) { float d = m[p + fx] - v; l += fabsf(d); g -= (d > 0.f) - (d < 0.f); }
+        if (j > 0) { float d = v - m[p - fx]; g += (d > 0.f) - (d < 0.f); }
+        grad[S.fl_off + p] += eta * g;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) l += __shfl_xor_sync(FULL, l, o);
+    if ((threadIdx.x & 31) == 0 && l != 0.0) atomicAdd(acc + 2, (double)eta * l);
+}
+
+cudaError_t ee_launch_loss_grad(const float* dose, const float* ptv_w, const float* ptv_t, const float* oar_w,
+                                const float* oar_t, float* grad, double* acc, long long n, cudaStream_t s) {
+    k_loss_grad<<<std::min<long long>(grid1(n, 256), 152 * 8), 256, 0, s>>>(dose, ptv_w, ptv_t, oar_w, oar_t, grad, acc, n);
+    return cudaGetLastError();
+}
+
+cudaError_t ee_launch_spread(const EeBeamSpec* specs, const float* in, float* out, const float* w1d, int R, int nbeams,
+                             int max_pix, cudaStream_t s) {
+    dim3 grid(grid1(max_pix, 256), 1, nbeams);
+    k_spread<<<grid, 256, 0, s>>>(specs, in, out, w1d, R);
+    return cudaGetLastError();
+}
+
+cudaError_t ee_launch_smooth(const EeBeamSpec* specs, const float* x, float* grad, float eta, double* acc, int nbeams,
+                             int max_pix, cudaStream_t s) {
+    dim3 grid(grid1(max_pix, 256), 1, nbeams);
+    k_smooth<<<grid, 256, 0, s>>>(specs, x, grad, eta, acc);
     return cudaGetLastError();
 }

@@ -74,6 +74,11 @@ class EEBeam(C.Structure):
                 ("fmap_size", C.c_int * 2), ("beamlet_size", C.c_float * 2)]
 
 
+class Loss(C.Structure):
+    _fields_ = [("ptv_weight", C.c_void_p), ("ptv_target", C.c_void_p), ("oar_weight", C.c_void_p),
+                ("oar_target", C.c_void_p), ("eta", C.c_float), ("spread_sigma", C.c_float)]
+
+
 class BeamInfo(C.Structure):
     _fields_ = [("source", C.c_float * 3), ("direction", C.c_float * 3), ("b_min", C.c_float * 3),
                 ("bev_size", C.c_int * 3), ("lim_min", C.c_float * 3), ("v_beam", C.c_longlong),
@@ -100,6 +105,12 @@ _SIGS = {
     "ee_synchronize": (C.c_int, [C.c_void_p]),
     "ee_get_stream": (C.c_void_p, [C.c_void_p]),
     "ee_beam_source": (C.c_int, [C.POINTER(EEBeam), C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "ee_loss_and_grad": (C.c_int, [C.c_void_p, C.POINTER(EEBeam), C.c_int, C.c_void_p, C.POINTER(Loss), C.c_void_p,
+                                   C.c_void_p, C.POINTER(C.c_double)]),
+    "ee_dose_and_adjoint_device": (C.c_int, [C.c_void_p, C.POINTER(EEBeam), C.c_int, C.c_void_p, C.c_void_p, C.c_int,
+                                             C.c_void_p, C.c_void_p]),
+    "ee_dose_and_adjoint": (C.c_int, [C.c_void_p, C.POINTER(EEBeam), C.c_int, C.c_void_p, C.c_void_p, C.c_int,
+                                      C.c_void_p, C.c_void_p]),
     "ee_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
     "ee_set_scratch_limit": (C.c_int, [C.c_void_p, C.c_longlong]),
     "ee_read_profile": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_longlong), C.c_int]),
@@ -250,6 +261,28 @@ class Engine:
         eb = to_ee_beams(beams)
         self._check(self.lib.ee_beam_dose_adjoint_device(self.h, eb, len(beams), C.c_void_p(d_fluence),
                                                          C.c_void_p(d_dose_grad), C.c_void_p(d_fluence_grad)))
+
+    def dose_and_adjoint_device(self, beams, d_fluence: int, d_dose: int, d_dose_grad: int, d_fluence_grad: int,
+                                mode: int = DOSE_SUM):
+        """Forward dose and adjoint in one call (shared TERMA / geometry)."""
+        eb = to_ee_beams(beams)
+        self._check(self.lib.ee_dose_and_adjoint_device(self.h, eb, len(beams), C.c_void_p(d_fluence),
+                                                        C.c_void_p(d_dose or 0), mode, C.c_void_p(d_dose_grad or 0),
+                                                        C.c_void_p(d_fluence_grad or 0)))
+
+    def loss_and_grad_device(self, beams, d_x: int, d_dose: int, d_xgrad: int, ptv=(0, 0), oar=(0, 0),
+                             eta: float = 0.0, spread_sigma: float = 0.0):
+        """EndtoEnd loss (README.md:20) and its gradient w.r.t. the fluence maps.
+        ptv/oar: (weight_ptr, target_ptr) device pointers or (0, 0)."""
+        eb = to_ee_beams(beams)
+        L = Loss()
+        L.ptv_weight, L.ptv_target = ptv
+        L.oar_weight, L.oar_target = oar
+        L.eta, L.spread_sigma = float(eta), float(spread_sigma)
+        out = (C.c_double * 3)()
+        self._check(self.lib.ee_loss_and_grad(self.h, eb, len(beams), C.c_void_p(d_x), C.byref(L), C.c_void_p(d_dose),
+                                              C.c_void_p(d_xgrad), out))
+        return list(out)
 
     # -- diagnostics
     def beam_info(self, i: int) -> dict:

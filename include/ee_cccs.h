@@ -20,9 +20,10 @@
  *                          CCCS/dosecalc-beam/nvbbRayConvolve_host.cu:297,775
  *   ee_destroy          <- freeCudaTexture
  *                          CCCS/dosecalc-beam/nvbbRayConvolve_host.cu:746
- *   ee_beam_dose_adjoint, ee_loss_and_grad
- *                       <- the EndtoEnd fluence-gradient call (README.md:15-22,
- *                          source not in the reference snapshot)
+ *   ee_beam_dose_adjoint, ee_loss_and_grad, ee_dose_and_adjoint_device
+ *                       <- the EndtoEnd forward-dose and fluence-gradient
+ *                          calls (README.md:15-22; that source is not in the
+ *                          reference snapshot, so only the README defines them)
  */
 #ifndef EE_CCCS_H
 #define EE_CCCS_H
@@ -157,6 +158,36 @@ int ee_beam_dose_adjoint_device(ee_context *ctx, const ee_beam *beams, int nbeam
 /* Device scratch budget for one chunk of beams (TERMA and REV arenas);
  * larger batches are processed in chunks that fit.  Default 8 GiB. */
 int ee_set_scratch_limit(ee_context *ctx, long long bytes);
+
+/* ---- EndtoEnd loss and fluence gradient ----
+ * L = sum_i w0_i (d_i - t0_i)^2 + sum_i w_i max(d_i - t_i, 0)^2 + eta sum_k ||D x_k||_1
+ * (README.md:20), d = sum_k A_k (G * x_k): A_k the CCCS chain of beam k, G a
+ * normalised Gaussian fluence-spread kernel of `spread_sigma` pixels (0 = none,
+ * README.md:15-18), D the forward differences along both fluence-map axes
+ * (BOO/BOO_QL/CreateDxDyFMO.m).  Weight/target pointers are device arrays of
+ * the volume's size; either pair may be NULL. */
+typedef struct {
+    const float *ptv_weight;
+    const float *ptv_target;
+    const float *oar_weight;
+    const float *oar_target;
+    float eta;
+    float spread_sigma;
+} ee_loss;
+
+/* d_x: the beams' fluence maps (optimisation variable, concatenated);
+ * outputs the summed dose, dL/dx and loss_out = {PTV term, OAR term,
+ * smoothness term}.  TERMA, crop boxes and REV frames are computed once and
+ * shared by the forward and adjoint passes. */
+int ee_loss_and_grad(ee_context *ctx, const ee_beam *beams, int nbeams, const float *d_x, const ee_loss *loss,
+                     float *d_dose, float *d_xgrad, double loss_out[3]);
+/* Forward dose and the adjoint of a caller-given dose gradient in one call
+ * (shared TERMA/geometry).  Either output may be NULL. */
+int ee_dose_and_adjoint_device(ee_context *ctx, const ee_beam *beams, int nbeams, const float *d_fluence,
+                               float *d_dose, int dose_mode, const float *d_dose_grad, float *d_fluence_grad);
+/* Host-pointer form of ee_dose_and_adjoint_device (copies in and out, synchronous). */
+int ee_dose_and_adjoint(ee_context *ctx, const ee_beam *beams, int nbeams, const float *fluence_host,
+                        float *dose_host, int dose_mode, const float *dose_grad_host, float *fluence_grad_host);
 
 /* ---- diagnostics ---- */
 /* Stage ids for ee_read_profile. */
