@@ -4,9 +4,10 @@ The gradient of
     L = sum w0 (d - t0)^2 + sum w (d - t)_+^2 + eta sum_k ||D x_k||_1,
     d = sum_k A_k (G * x_k)
 is checked (a) against central finite differences (step 1e-3) of the FP64
-oracle's loss on 64 seeded pixels -- the oracle dose is linear in each beam's
-fluence, so L(x +- h e_p) is formed from the oracle's dose column A_k G e_p --
-and (b) against the oracle's own adjoint.  Tolerance: 2e-3 of max |dL/dx|.
+oracle's loss on 64 seeded pixels -- only the perturbed beam's dose is
+recomputed, with its whole fluence map so that its crop box stays the one of
+the unperturbed call -- and (b) against the oracle's own adjoint.
+Tolerance: 2e-3 of max |dL/dx|.
 """
 import numpy as np
 import pytest
@@ -131,13 +132,18 @@ def test_gradient_central_differences_64_pixels(problem):
     for p in picks:
         k = int(np.searchsorted(offs, p, side="right") - 1)
         q = int(p - offs[k])
-        e = np.zeros(sizes[k])
-        e[q] = 1.0
-        e = e.reshape(beams[k].fluence.shape)
-        bcol = inputs.Beam(**{**beams[k].__dict__, "fluence": _spread(e, K).astype(np.float32)})
-        col = o.beam_dose(bcol)[0]  # dose per unit of pixel p (linear)
-        lp = _loss(dose + h * col, arrays, _perturbed(beams, k, q, +h))
-        lm = _loss(dose - h * col, arrays, _perturbed(beams, k, q, -h))
+        # beam k's dose at x_k +- h e_p, full fluence map (the crop box is
+        # set by the whole map, so it is the same as in the unperturbed call)
+        dk = {}
+        for sgn in (+1, -1):
+            f = beams[k].fluence.astype(np.float64).copy()
+            f.ravel()[q] += sgn * h
+            bk = inputs.Beam(**{**beams[k].__dict__, "fluence": _spread(f, K).astype(np.float64)})
+            dk[sgn] = o.beam_dose(bk)[0]
+        b0 = inputs.Beam(**{**beams[k].__dict__, "fluence": _spread(beams[k].fluence, K)})
+        d0 = o.beam_dose(b0)[0]
+        lp = _loss(dose - d0 + dk[+1], arrays, _perturbed(beams, k, q, +h))
+        lm = _loss(dose - d0 + dk[-1], arrays, _perturbed(beams, k, q, -h))
         fd.append((lp - lm) / (2 * h))
         eg.append(xg[p])
     fd, eg = np.array(fd), np.array(eg)
