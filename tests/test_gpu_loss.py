@@ -127,7 +127,22 @@ def test_gradient_central_differences_64_pixels(problem):
     sizes = [b.fluence.size for b in beams]
     offs = np.cumsum([0] + sizes)
     h = 1e-3
-    picks = rng.choice(offs[-1], size=64, replace=False)
+    # the L1 smoothness term has kinks where neighbouring pixels are equal:
+    # pixels with a neighbour within 2h are excluded (a central difference
+    # across a kink is not the derivative at either side)
+    smooth_ok = []
+    for b in beams:
+        f = b.fluence.astype(np.float64)
+        ok = np.ones(f.shape, bool)
+        dx = np.abs(np.diff(f, axis=1)) < 2 * h
+        dy = np.abs(np.diff(f, axis=0)) < 2 * h
+        ok[:, :-1] &= ~dx
+        ok[:, 1:] &= ~dx
+        ok[:-1, :] &= ~dy
+        ok[1:, :] &= ~dy
+        smooth_ok.append(ok.ravel())
+    cand = np.nonzero(np.concatenate(smooth_ok))[0]
+    picks = rng.choice(cand, size=64, replace=False)
     fd, eg = [], []
     for p in picks:
         k = int(np.searchsorted(offs, p, side="right") - 1)
