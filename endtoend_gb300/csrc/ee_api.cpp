@@ -902,3 +902,22 @@ int ee_beam_source(const ee_beam* b, float source[3], float direction[3]) {
 }
 
 }  // extern "C"
+
+// ------------------------------------------------ internal accessors ----
+// Used by ee_noalloc.cu: a copy of the context's kernel parameters (device
+// pointers to its resident density and kernel tables) and the host-side
+// beam set-up, so that file's entry point needs no context scratch.
+int ee_internal_snapshot(ee_context* c, EeParams* P, int* device) {
+    int st = check_ready(c);
+    if (st) return st;
+    std::lock_guard<std::mutex> lk(c->mu);
+    *P = c->P;
+    *device = c->device;
+    return EE_OK;
+}
+
+void ee_internal_build_spec(const EeParams& P, const ee_beam& beam, EeBeamSpec* out) { build_specs(P, &beam, 1, out); }
+
+const char* ee_internal_status_text(int st) { return status_text(st); }
+
+int ee_internal_fail(int code, const char* msg) { return fail(code, "%s", msg); }

@@ -111,6 +111,7 @@ _SIGS = {
                                              C.c_void_p, C.c_void_p]),
     "ee_dose_and_adjoint": (C.c_int, [C.c_void_p, C.POINTER(EEBeam), C.c_int, C.c_void_p, C.c_void_p, C.c_int,
                                       C.c_void_p, C.c_void_p]),
+    "ee_beam_dose_noalloc": (C.c_int, [C.c_void_p, C.POINTER(EEBeam), C.c_void_p, C.c_void_p, C.c_void_p]),
     "ee_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
     "ee_set_scratch_limit": (C.c_int, [C.c_void_p, C.c_longlong]),
     "ee_read_profile": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_longlong), C.c_int]),
@@ -283,6 +284,13 @@ class Engine:
         self._check(self.lib.ee_loss_and_grad(self.h, eb, len(beams), C.c_void_p(d_x), C.byref(L), C.c_void_p(d_dose),
                                               C.c_void_p(d_xgrad), out))
         return list(out)
+
+    def beam_dose_noalloc(self, beam, d_fluence: int, d_dose: int, stream: int = 0):
+        """One beam's dose without any device allocation (static 64 MiB
+        scratch); for callers that cannot allocate per call."""
+        eb = to_ee_beams([beam])
+        self._check(self.lib.ee_beam_dose_noalloc(self.h, eb, C.c_void_p(d_fluence), C.c_void_p(d_dose),
+                                                  C.c_void_p(stream or None)))
 
     # -- diagnostics
     def beam_info(self, i: int) -> dict:

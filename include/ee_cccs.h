@@ -189,6 +189,20 @@ int ee_dose_and_adjoint_device(ee_context *ctx, const ee_beam *beams, int nbeams
 int ee_dose_and_adjoint(ee_context *ctx, const ee_beam *beams, int nbeams, const float *fluence_host,
                         float *dose_host, int dose_mode, const float *dose_grad_host, float *fluence_grad_host);
 
+/* ---- allocation-free single-beam dose ----
+ * No counterpart in the reference: an extra entry point for callers that
+ * must not allocate device memory per call (a pre-carved memory pool owned
+ * by another allocator, a per-process memory budget, a real-time loop).
+ * Same result as ee_beam_dose_device for one beam (dose = that beam's dose on
+ * the full grid, overwritten), with all intermediates in a 64 MiB static
+ * device array held by every GPU that loads the library; beams whose TERMA
+ * box + REV arena exceed it fail with EE_ERR_CAPACITY.  Calls no cudaMalloc /
+ * cudaFree.  The context must be set up (ee_set_*, which allocate) first.
+ * Calls share the array, so calls that overlap on the GPU race; the first
+ * call on a device looks the array's address up and should come before any
+ * stream capture.  `stream` is a cudaStream_t (NULL = legacy default). */
+int ee_beam_dose_noalloc(ee_context *ctx, const ee_beam *beam, const float *d_fluence, float *d_dose, void *stream);
+
 /* ---- diagnostics ---- */
 /* Stage ids for ee_read_profile. */
 #define EE_STAGE_TERMA 0     /* k_terma (+crop-box reduction)           */
