@@ -150,6 +150,8 @@ struct ee_context {
     ee_conv_params conv{};
     std::vector<EeRayConst> rays;
     DevBuf<float> density, cumkern, expp;
+    cudaArray_t dens_array = nullptr;
+    cudaTextureObject_t dens_tex = 0;
     DevBuf<EeRayConst> d_rays;
     // per-call scratch
     DevBuf<EeBeamSpec> d_specs;
@@ -399,7 +401,7 @@ int pipeline(ee_context* c, const PipeArgs& A) {
     if (adj) {
         EE_CUDA(grow(c, c->unit, tvol_total));
         EE_CUDA(grow(c, c->bl_idx, tvol_total));
-        EE_CUDA(grow(c, c->terma_grad, tvol_total));
+        EE_CUDA(grow(c, c->terma_grad, tvol_total + 4));  // +4: vector-reduction padding
     }
     EE_CUDA(cudaMemcpyAsync(c->d_specs.p, c->h_specs.p, sizeof(EeBeamSpec) * n, cudaMemcpyHostToDevice, s));
     std::vector<int> starts = plan_chunks(c, c->h_specs.p, n, adj);
@@ -470,7 +472,7 @@ int pipeline(ee_context* c, const PipeArgs& A) {
         const EeBeamSpec* dsp = c->d_specs.p + b0;
         const EeBeamGeom* dge = c->d_geoms.p + b0;
         const ChunkDims& D = dims[k];
-        EE_CUDA(grow(c, c->rev_grad, D.rev_total));
+        EE_CUDA(grow(c, c->rev_grad, D.rev_total + 4));  // +4: vector-reduction padding
         EE_CUDA(cudaMemsetAsync(c->rev_grad.p, 0, sizeof(float) * D.rev_total, s));
         EE_CUDA(staged(c, EE_STAGE_GATHER_T, 1, [&] {
             return ee_launch_gather_T(c->P, dsp, dge, dgrad, c->rev_grad.p, nb, D.max_rows, s);
@@ -551,6 +553,8 @@ int ee_destroy(ee_context* c) {
     if (!c) return EE_OK;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->dens_tex) cudaDestroyTextureObject(c->dens_tex);
+    if (c->dens_array) cudaFreeArray(c->dens_array);
     c->density.release(); c->cumkern.release(); c->expp.release(); c->d_rays.release();
     c->d_specs.release(); c->d_geoms.release(); c->terma.release(); c->unit.release(); c->rev.release();
     c->rev_grad.release(); c->terma_grad.release(); c->bl_idx.release();
@@ -579,12 +583,40 @@ int ee_set_volume(ee_context* c, const ee_frame* f, const float* density) {
     EE_CUDA(c->density.ensure(n));
     EE_CUDA(cudaMemcpyAsync(c->density.p, density, n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
     EE_CUDA(cudaStreamSynchronize(c->stream));
+    // the density also as a 3-D texture: the SM texture units do the
+    // trilinear interpolation of every Siddon and REV-resample fetch
+    // (linear filter, border 0, unnormalised coordinates; the reference's
+    // texDens, nvbbRayConvolve_host.cu:229-242)
+    if (c->dens_tex) { cudaDestroyTextureObject(c->dens_tex); c->dens_tex = 0; }
+    if (c->dens_array) { cudaFreeArray(c->dens_array); c->dens_array = nullptr; }
+    {
+        cudaChannelFormatDesc fd = cudaCreateChannelDesc<float>();
+        cudaExtent ext = make_cudaExtent(fr.size[0], fr.size[1], fr.size[2]);
+        EE_CUDA(cudaMalloc3DArray(&c->dens_array, &fd, ext));
+        cudaMemcpy3DParms cp = {};
+        cp.srcPtr = make_cudaPitchedPtr((void*)c->density.p, fr.size[0] * sizeof(float), fr.size[0], fr.size[1]);
+        cp.dstArray = c->dens_array;
+        cp.extent = ext;
+        cp.kind = cudaMemcpyDeviceToDevice;
+        EE_CUDA(cudaMemcpy3DAsync(&cp, c->stream));
+        cudaResourceDesc rd = {};
+        rd.resType = cudaResourceTypeArray;
+        rd.res.array.array = c->dens_array;
+        cudaTextureDesc td = {};
+        for (int a = 0; a < 3; a++) td.addressMode[a] = cudaAddressModeBorder;
+        td.filterMode = cudaFilterModeLinear;
+        td.readMode = cudaReadModeElementType;
+        td.normalizedCoords = 0;
+        EE_CUDA(cudaCreateTextureObject(&c->dens_tex, &rd, &td, nullptr));
+        EE_CUDA(cudaStreamSynchronize(c->stream));
+    }
     c->frame = fr;
     for (int a = 0; a < 3; a++) {
         c->P.size[a] = fr.size[a]; c->P.voxel[a] = fr.voxel[a]; c->P.start[a] = fr.start[a];
         c->P.bb0[a] = fr.bbox_start[a]; c->P.bbs[a] = fr.bbox_size[a];
     }
     c->P.density = c->density.p;
+    c->P.dens_tex = c->dens_tex;
     c->have_volume = true;
     derive_max_rev(c);
     return EE_OK;

@@ -18,6 +18,9 @@ struct EeParams {
     int bb0[3];
     int bbs[3];
     const float* density;  // full grid
+    cudaTextureObject_t dens_tex;  // same volume as a 3-D texture: linear filter, border 0,
+                                   // unnormalised coordinates (the reference's texDens,
+                                   // nvbbRayConvolve_host.cu:229-242)
     int nE;
     float sp_fluence[EE_MAX_E];
     float sp_energy[EE_MAX_E];

@@ -97,13 +97,32 @@ __device__ __forceinline__ float tri_border(const float* __restrict__ v, int nx,
     return acc;
 }
 
-// Transpose of tri_border: atomically scatter g with the trilinear weights.
+// Add (a, b) to p[0], p[1] with vector reductions: both land in one 16-byte
+// aligned quad unless p sits in its last slot.  The other slots of the quad
+// receive +0, so the buffer must hold 3 floats of padding past its last
+// element and its base must be 16-byte aligned (cudaMalloc'd).
+__device__ __forceinline__ void red_pair(float* p, float a, float b) {
+    const uintptr_t u = (uintptr_t)p;
+    float4* q = (float4*)(u & ~(uintptr_t)15);
+    const int o = (int)((u >> 2) & 3);
+    if (o == 0) atomicAdd(q, make_float4(a, b, 0.f, 0.f));
+    else if (o == 1) atomicAdd(q, make_float4(0.f, a, b, 0.f));
+    else if (o == 2) atomicAdd(q, make_float4(0.f, 0.f, a, b));
+    else {
+        atomicAdd(p, a);
+        atomicAdd(p + 1, b);
+    }
+}
+
+// Transpose of tri_border: atomically scatter g with the trilinear weights,
+// x-adjacent corner pairs as one vector reduction (see red_pair).
 __device__ __forceinline__ void tri_border_scatter(float* v, int nx, int ny, int nz, float x, float y, float z, float g) {
     if (!(x > -1.f && x < (float)nx && y > -1.f && y < (float)ny && z > -1.f && z < (float)nz)) return;
     float fx = floorf(x), fy = floorf(y), fz = floorf(z);
     int i = (int)fx, j = (int)fy, k = (int)fz;
     float ax = x - fx, ay = y - fy, az = z - fz;
     long long sxy = (long long)nx * ny;
+    const bool in0 = i >= 0, in1 = i + 1 < nx;
 #pragma unroll
     for (int dk = 0; dk < 2; dk++) {
         int kk = k + dk;
@@ -113,14 +132,11 @@ __device__ __forceinline__ void tri_border_scatter(float* v, int nx, int ny, int
         for (int dj = 0; dj < 2; dj++) {
             int jj = j + dj;
             if (jj < 0 || jj >= ny) continue;
-            float wy = dj ? ay : 1.f - ay;
-#pragma unroll
-            for (int di = 0; di < 2; di++) {
-                int ii = i + di;
-                if (ii < 0 || ii >= nx) continue;
-                float wx = di ? ax : 1.f - ax;
-                atomicAdd(v + ii + (long long)nx * jj + sxy * kk, wx * wy * wz * g);
-            }
+            float w = (dj ? ay : 1.f - ay) * wz * g;
+            float* row = v + (long long)nx * jj + sxy * kk;
+            if (in0 && in1) red_pair(row + i, (1.f - ax) * w, ax * w);
+            else if (in0) atomicAdd(row + i, (1.f - ax) * w);
+            else if (in1) atomicAdd(row + i + 1, ax * w);
         }
     }
 }
@@ -160,7 +176,7 @@ __device__ float siddon_rpl(const EeParams& P, f3 vox, f3 src, bool& iter_cap) {
                 float fx = (src.x + mid * diff.x - start.x) * ivx;
                 float fy = (src.y + mid * diff.y - start.y) * ivy;
                 float fz = (src.z + mid * diff.z - start.z) * ivz;
-                rpl += isect * tri_border(P.density, P.size[0], P.size[1], P.size[2], fx - 0.5f, fy - 0.5f, fz - 0.5f);
+                rpl += isect * tex3D<float>(P.dens_tex, fx, fy, fz);
             }
             alpha = next;
         }
@@ -442,7 +458,7 @@ __device__ __forceinline__ void gather_line(const EeParams& P, const EeBeamSpec&
             if (g.x < b0x || g.x >= b1x || g.y < b0y || g.y >= b1y || g.z < b0z || g.z >= b1z) {
                 r = -2.f;
             } else {
-                r = tri_border(P.density, P.size[0], P.size[1], P.size[2], g.x, g.y, g.z);
+                r = tex3D<float>(P.dens_tex, g.x + 0.5f, g.y + 0.5f, g.z + 0.5f);
                 if (terma_b)
                     t = tri_border(terma_b, S.tn[0], S.tn[1], S.tn[2], g.x - (float)S.t0[0], g.y - (float)S.t0[1],
                                    g.z - (float)S.t0[2]);
@@ -459,106 +475,129 @@ __device__ __forceinline__ void gather_line(const EeParams& P, const EeBeamSpec&
 // measured from the receiving voxel's boundary to the source voxel's centre):
 //   D_i = sum_c A_c/a_c [ Y_i + T_{i-1} (1 - h_{i-1}) ],
 //   Y_{i+1} = h_i^2 Y_i + T_{i-1} h_i (1 - h_{i-1} h_i),  h_j = e^{-a p_j/2},
-// evaluated as a warp-shuffle inclusive scan of the affine maps
-// Y -> F Y + U over 32-sample tiles with a carried Y.  p = delr*rho, p = T = 0
-// at sentinel samples.  FWD walks ascending i (contributions from k < i).
-template <bool FWD>
-__device__ __forceinline__ void line_scan(const float* rho, const float* T, int L, int lane, float delr,
-                                          const float* prm, float* D, float* out, float inv_nphi) {
-    const float A1 = prm[0], a1 = prm[1], A2 = prm[2], a2 = prm[3];
-    const float c1 = A1 / a1, c2 = A2 / a2;
-    float Y1 = 0.f, Y2 = 0.f;
-    const int ntiles = (L + 31) >> 5;
-    for (int tile = 0; tile < ntiles; tile++) {
-        const int n = (tile << 5) + lane;
-        const int i = FWD ? n : (L - 1 - n);
-        const int im = FWD ? i - 1 : i + 1;  // previous sample in walk order
-        float p = 0.f, t = 0.f, pm = 0.f, tm = 0.f;
-        bool valid = false;
-        if (n < L) {
-            float r = rho[i];
-            valid = r >= 0.f;
-            if (valid) { p = delr * r; t = T[i]; }
-            if (n > 0) {
-                float rm = rho[im];
-                if (rm >= 0.f) { pm = delr * rm; tm = T[im]; }
-            }
-        }
-        float h1 = __expf(-0.5f * a1 * p), hm1 = __expf(-0.5f * a1 * pm);
-        float h2 = __expf(-0.5f * a2 * p), hm2 = __expf(-0.5f * a2 * pm);
-        float F1 = h1 * h1, U1 = tm * h1 * (1.f - hm1 * h1);
-        float F2 = h2 * h2, U2 = tm * h2 * (1.f - hm2 * h2);
+// p = delr*rho, with p = T = 0 at sentinel samples.  Work-efficient warp
+// scan: each lane owns a contiguous chunk of the line, composes its chunk's
+// affine maps Y -> F Y + U sequentially, one 5-step shuffle scan over the 32
+// chunk maps gives every lane its starting Y, and a second sequential pass
+// replays the chunk.  Odd chunk lengths keep the lanes' shared-memory
+// strides bank-conflict free.  FWD walks ascending i (contributions from
+// k < i); the reverse pass adds its part to D and applies 1/nphi.
+
+// inclusive warp scan of affine maps (F, U): lane j gets maps 0..j composed
+__device__ __forceinline__ void warp_affine_scan(int lane, float& F1, float& U1, float& F2, float& U2) {
 #pragma unroll
-        for (int off = 1; off < 32; off <<= 1) {
-            float fF1 = __shfl_up_sync(FULL, F1, off), fU1 = __shfl_up_sync(FULL, U1, off);
-            float fF2 = __shfl_up_sync(FULL, F2, off), fU2 = __shfl_up_sync(FULL, U2, off);
-            if (lane >= off) {
-                U1 = fmaf(F1, fU1, U1); F1 *= fF1;
-                U2 = fmaf(F2, fU2, U2); F2 *= fF2;
-            }
+    for (int off = 1; off < 32; off <<= 1) {
+        float fF1 = __shfl_up_sync(FULL, F1, off), fU1 = __shfl_up_sync(FULL, U1, off);
+        float fF2 = __shfl_up_sync(FULL, F2, off), fU2 = __shfl_up_sync(FULL, U2, off);
+        if (lane >= off) {
+            U1 = fmaf(F1, fU1, U1); F1 *= fF1;
+            U2 = fmaf(F2, fU2, U2); F2 *= fF2;
         }
-        float Ya1 = fmaf(F1, Y1, U1), Ya2 = fmaf(F2, Y2, U2);
-        float Yb1 = __shfl_up_sync(FULL, Ya1, 1), Yb2 = __shfl_up_sync(FULL, Ya2, 1);
-        if (lane == 0) { Yb1 = Y1; Yb2 = Y2; }
-        float d = c1 * (Yb1 + tm * (1.f - hm1)) + c2 * (Yb2 + tm * (1.f - hm2));
-        if (n < L) {
-            if (FWD) D[i] = d;
-            else out[i] = valid ? (D[i] + d) * inv_nphi : 0.f;
-        }
-        Y1 = __shfl_sync(FULL, Ya1, 31);
-        Y2 = __shfl_sync(FULL, Ya2, 31);
     }
 }
 
-// Transpose of line_scan<FWD> for the terma adjoint: with g_i the incoming
-// REV-dose gradient (already / nphi, zero at sentinels),
-//   Z_i = c g_i + h_i^2 Z_{i+1}   (walking opposite to FWD),
-//   Tbar_{i-1} += c g_i (1 - h_{i-1}) + Z_{i+1} h_i (1 - h_{i-1} h_i).
 template <bool FWD>
-__device__ __forceinline__ void line_scan_T(const float* rho, const float* g, int L, int lane, float delr,
+__device__ __forceinline__ void line_scan(const float* rho, const float* T, int n, int lane, float delr,
+                                          const float* prm, float* D, float inv_nphi) {
+    const float c1 = prm[0] / prm[1], c2 = prm[2] / prm[3];
+    const float e1 = -0.5f * prm[1] * delr, e2 = -0.5f * prm[3] * delr;  // h = exp(e * rho)
+    const int cs = ((n + 31) >> 5) | 1;
+    const int w0 = min(n, lane * cs), w1 = min(n, w0 + cs);
+    // previous sample (walk order) of the chunk's first step
+    float tm0 = 0.f, hm10 = 1.f, hm20 = 1.f;
+    if (w0 > 0 && w0 < w1) {
+        const int im = FWD ? w0 - 1 : n - w0;
+        const float rm = rho[im];
+        if (rm >= 0.f) { tm0 = T[im]; hm10 = __expf(e1 * rm); hm20 = __expf(e2 * rm); }
+    }
+    // pass 1: compose this chunk's steps
+    float F1 = 1.f, U1 = 0.f, F2 = 1.f, U2 = 0.f;
+    float tm = tm0, hm1 = hm10, hm2 = hm20;
+    for (int w = w0; w < w1; w++) {
+        const int i = FWD ? w : n - 1 - w;
+        const float r = rho[i];
+        float t = 0.f, h1 = 1.f, h2 = 1.f;
+        if (r >= 0.f) { t = T[i]; h1 = __expf(e1 * r); h2 = __expf(e2 * r); }
+        const float f1 = h1 * h1, f2 = h2 * h2;
+        U1 = fmaf(f1, U1, tm * h1 * (1.f - hm1 * h1)); F1 *= f1;
+        U2 = fmaf(f2, U2, tm * h2 * (1.f - hm2 * h2)); F2 *= f2;
+        tm = t; hm1 = h1; hm2 = h2;
+    }
+    warp_affine_scan(lane, F1, U1, F2, U2);
+    // Y at the start of the chunk: the line starts from Y = 0
+    float Y1 = __shfl_up_sync(FULL, U1, 1), Y2 = __shfl_up_sync(FULL, U2, 1);
+    if (lane == 0) { Y1 = 0.f; Y2 = 0.f; }
+    // pass 2: replay
+    tm = tm0; hm1 = hm10; hm2 = hm20;
+    for (int w = w0; w < w1; w++) {
+        const int i = FWD ? w : n - 1 - w;
+        const float r = rho[i];
+        float t = 0.f, h1 = 1.f, h2 = 1.f;
+        if (r >= 0.f) { t = T[i]; h1 = __expf(e1 * r); h2 = __expf(e2 * r); }
+        const float d = c1 * (Y1 + tm * (1.f - hm1)) + c2 * (Y2 + tm * (1.f - hm2));
+        if (FWD) D[i] = d;
+        else D[i] = r >= 0.f ? (D[i] + d) * inv_nphi : 0.f;
+        Y1 = fmaf(h1 * h1, Y1, tm * h1 * (1.f - hm1 * h1));
+        Y2 = fmaf(h2 * h2, Y2, tm * h2 * (1.f - hm2 * h2));
+        tm = t; hm1 = h1; hm2 = h2;
+    }
+}
+
+// Transpose of line_scan<FWD> for the TERMA adjoint.  With g_i the incoming
+// REV-dose gradient (already / nphi, zero at sentinels) and im the forward
+// walk's previous sample of i,
+//   Z_i = c g_i + h_i^2 Z_{i+1}         (walking opposite to FWD),
+//   Tbar_im += c g_i (1 - h_im) + Z_{i+1} h_i (1 - h_im h_i),
+// with the same chunked scan.  im is the next sample of this walk, so its
+// h is computed once and carried.
+template <bool FWD>
+__device__ __forceinline__ void line_scan_T(const float* rho, const float* g, int n, int lane, float delr,
                                             const float* prm, float* Tb) {
-    const float A1 = prm[0], a1 = prm[1], A2 = prm[2], a2 = prm[3];
-    const float c1 = A1 / a1, c2 = A2 / a2;
-    float Z1 = 0.f, Z2 = 0.f;
-    const int ntiles = (L + 31) >> 5;
-    for (int tile = 0; tile < ntiles; tile++) {
-        const int n = (tile << 5) + lane;
-        // adjoint walk runs opposite to the forward walk
-        const int i = FWD ? (L - 1 - n) : n;
-        const int im = FWD ? i - 1 : i + 1;  // the forward walk's previous sample
-        float p = 0.f, gi = 0.f, pm = 0.f;
-        bool has_m = false;
-        if (n < L) {
-            float r = rho[i];
-            if (r >= 0.f) { p = delr * r; gi = g[i]; }
-            if (im >= 0 && im < L) {
-                float rm = rho[im];
-                if (rm >= 0.f) { pm = delr * rm; has_m = true; }
-            }
+    const float c1 = prm[0] / prm[1], c2 = prm[2] / prm[3];
+    const float e1 = -0.5f * prm[1] * delr, e2 = -0.5f * prm[3] * delr;
+    const int cs = ((n + 31) >> 5) | 1;
+    const int v0 = min(n, lane * cs), v1 = min(n, v0 + cs);
+    // pass 1: compose Z -> h^2 Z + c g over the chunk
+    float F1 = 1.f, U1 = 0.f, F2 = 1.f, U2 = 0.f;
+    for (int v = v0; v < v1; v++) {
+        const int i = FWD ? n - 1 - v : v;
+        const float r = rho[i];
+        float gi = 0.f, h1 = 1.f, h2 = 1.f;
+        if (r >= 0.f) { gi = g[i]; h1 = __expf(e1 * r); h2 = __expf(e2 * r); }
+        const float f1 = h1 * h1, f2 = h2 * h2;
+        U1 = fmaf(f1, U1, c1 * gi); F1 *= f1;
+        U2 = fmaf(f2, U2, c2 * gi); F2 *= f2;
+    }
+    warp_affine_scan(lane, F1, U1, F2, U2);
+    float Z1 = __shfl_up_sync(FULL, U1, 1), Z2 = __shfl_up_sync(FULL, U2, 1);
+    if (lane == 0) { Z1 = 0.f; Z2 = 0.f; }
+    // pass 2: replay, emitting the TERMA-gradient contributions
+    float h1 = 1.f, h2 = 1.f, gi = 0.f;
+    bool vi = false;
+    if (v0 < v1) {
+        const int i = FWD ? n - 1 - v0 : v0;
+        const float r = rho[i];
+        if (r >= 0.f) { vi = true; gi = g[i]; h1 = __expf(e1 * r); h2 = __expf(e2 * r); }
+    }
+    for (int v = v0; v < v1; v++) {
+        const int i = FWD ? n - 1 - v : v;
+        const int im = FWD ? i - 1 : i + 1;
+        float hm1 = 1.f, hm2 = 1.f, gm = 0.f;
+        bool vm = false;
+        if (im >= 0 && im < n) {
+            const float rm = rho[im];
+            if (rm >= 0.f) { vm = true; gm = g[im]; hm1 = __expf(e1 * rm); hm2 = __expf(e2 * rm); }
         }
-        float h1 = __expf(-0.5f * a1 * p), hm1 = __expf(-0.5f * a1 * pm);
-        float h2 = __expf(-0.5f * a2 * p), hm2 = __expf(-0.5f * a2 * pm);
-        float F1 = h1 * h1, U1 = c1 * gi;
-        float F2 = h2 * h2, U2 = c2 * gi;
-#pragma unroll
-        for (int off = 1; off < 32; off <<= 1) {
-            float fF1 = __shfl_up_sync(FULL, F1, off), fU1 = __shfl_up_sync(FULL, U1, off);
-            float fF2 = __shfl_up_sync(FULL, F2, off), fU2 = __shfl_up_sync(FULL, U2, off);
-            if (lane >= off) {
-                U1 = fmaf(F1, fU1, U1); F1 *= fF1;
-                U2 = fmaf(F2, fU2, U2); F2 *= fF2;
-            }
+        if (vm) {
+            const float c = c1 * gi * (1.f - hm1) + Z1 * h1 * (1.f - hm1 * h1) + c2 * gi * (1.f - hm2) +
+                            Z2 * h2 * (1.f - hm2 * h2);
+            Tb[im] += c;  // each im has exactly one i per pass
         }
-        float Za1 = fmaf(F1, Z1, U1), Za2 = fmaf(F2, Z2, U2);  // Z_i
-        float Zb1 = __shfl_up_sync(FULL, Za1, 1), Zb2 = __shfl_up_sync(FULL, Za2, 1);  // Z_{i+1}
-        if (lane == 0) { Zb1 = Z1; Zb2 = Z2; }
-        if (n < L && has_m) {
-            float v = c1 * gi * (1.f - hm1) + Zb1 * h1 * (1.f - hm1 * h1) + c2 * gi * (1.f - hm2) +
-                      Zb2 * h2 * (1.f - hm2 * h2);
-            Tb[im] += v;  // unique im per lane within a pass
-        }
-        Z1 = __shfl_sync(FULL, Za1, 31);
-        Z2 = __shfl_sync(FULL, Za2, 31);
+        (void)vi;
+        Z1 = fmaf(h1 * h1, Z1, c1 * gi);
+        Z2 = fmaf(h2 * h2, Z2, c2 * gi);
+        // the next step's sample is im
+        h1 = hm1; h2 = hm2; gi = gm; vi = vm;
     }
 }
 
@@ -634,9 +673,9 @@ __global__ void __launch_bounds__(CONE_WARPS * 32) k_cone(EeParams P, const EeBe
         const float inv_nphi = 1.f / (float)P.nphi;
         const EeRayConst& RC = P.rays[ray];
         if (P.mode == 1) {
-            line_scan<true>(rho, T, n, lane, P.lng, P.expp + 4 * RC.row_fwd, D, D, inv_nphi);
+            line_scan<true>(rho, T, n, lane, P.lng, P.expp + 4 * RC.row_fwd, D, inv_nphi);
             __syncwarp();
-            line_scan<false>(rho, T, n, lane, P.lng, P.expp + 4 * RC.row_rev, D, D, inv_nphi);
+            line_scan<false>(rho, T, n, lane, P.lng, P.expp + 4 * RC.row_rev, D, inv_nphi);
         } else {
             for (int k = lane; k < n; k += 32) {
                 float v = 0.f;
