@@ -1,0 +1,97 @@
+"""ctypes front end of the reference harness (test infrastructure only): the
+reference's own dosecalc-beam kernel source executed on the CPU.  Needs the
+reference checkout (see build.py); tests skip it when that is absent."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+
+class RefSetup(C.Structure):
+    _fields_ = [("size", C.c_int * 3), ("voxel", C.c_float * 3), ("start", C.c_float * 3),
+                ("bbox_start", C.c_int * 3), ("bbox_size", C.c_int * 3), ("density", C.POINTER(C.c_float)),
+                ("nE", C.c_int), ("energy", C.POINTER(C.c_float)), ("fluence", C.POINTER(C.c_float)),
+                ("mu", C.POINTER(C.c_float)), ("mu_en", C.POINTER(C.c_float)),
+                ("ntheta", C.c_int), ("nphi", C.c_int), ("nradii", C.c_int),
+                ("radii", C.POINTER(C.c_float)), ("cumkern", C.POINTER(C.c_float)),
+                ("theta_deg", C.POINTER(C.c_float)), ("phi_deg", C.POINTER(C.c_float)),
+                ("rev_latspacing", C.c_float), ("rev_longspacing", C.c_float), ("penumbra", C.c_float),
+                ("tex_emulate", C.c_int), ("nthreads", C.c_int)]
+
+
+class RefBeam(C.Structure):
+    _fields_ = [("azimuth", C.c_float), ("zenith", C.c_float), ("coll", C.c_float), ("iso", C.c_float * 3),
+                ("sad", C.c_float), ("fmap", C.c_int * 2), ("beamlet", C.c_float * 2)]
+
+
+available = _build.available
+_LIB = None
+
+
+def _lib():
+    global _LIB
+    if _LIB is None:
+        lib = C.CDLL(_build.build())
+        lib.ccref_beam_dose.argtypes = [C.POINTER(RefSetup), C.POINTER(RefBeam), C.POINTER(C.c_float),
+                                        C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_int)]
+        lib.ccref_beam_dose.restype = C.c_int
+        _LIB = lib
+    return _LIB
+
+
+def _fp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+class ReferenceHarness:
+    """The reference's cudaSiddon / cudaRaytrace / RowConvolve / REV2XYZdose
+    kernels (cumulative-kernel table) run on the CPU for one beam."""
+
+    def __init__(self, vol, phys, tex_emulate=True, nthreads=None):
+        self.lib = _lib()
+        self.vol, self.phys = vol, phys
+        keep = self._keep = []
+
+        def farr(x):
+            a = np.ascontiguousarray(np.asarray(x, dtype=np.float32).ravel())
+            keep.append(a)
+            return _fp(a)
+
+        s = RefSetup()
+        s.size[:] = [int(v) for v in vol.size]
+        s.voxel[:] = [float(v) for v in vol.voxel]
+        s.start[:] = [float(v) for v in vol.start]
+        s.bbox_start[:] = [int(v) for v in vol.bbox_start]
+        s.bbox_size[:] = [int(v) for v in vol.bbox_size]
+        s.density = farr(vol.density)
+        fl = np.asarray(phys.fluence, np.float64)
+        s.nE = len(phys.energy)
+        s.energy, s.fluence, s.mu, s.mu_en = farr(phys.energy), farr(fl / fl.sum()), farr(phys.mu), farr(phys.mu_en)
+        s.ntheta, s.nphi, s.nradii = phys.ntheta, phys.nphi, phys.nradii
+        s.radii, s.cumkern = farr(phys.radii), farr(phys.cumkern)
+        s.theta_deg, s.phi_deg = farr(phys.theta_deg), farr(phys.phi_deg)
+        s.rev_latspacing, s.rev_longspacing, s.penumbra = phys.rev_latspacing, phys.rev_longspacing, phys.penumbra
+        s.tex_emulate = int(bool(tex_emulate))
+        s.nthreads = int(nthreads or os.cpu_count() or 1)
+        self.setup = s
+
+    def beam_dose(self, beam):
+        b = RefBeam()
+        b.azimuth, b.zenith, b.coll = beam.azimuth, beam.zenith, beam.coll
+        b.iso[:] = [float(v) for v in beam.isocenter]
+        b.sad = beam.sad
+        b.fmap[:] = [int(v) for v in beam.fmap_size]
+        b.beamlet[:] = [float(v) for v in beam.beamlet_size]
+        fl = np.ascontiguousarray(beam.fluence, np.float32).ravel()
+        dose = np.zeros(self.vol.density.shape, np.float32)
+        bs = self.vol.bbox_size
+        terma = np.zeros((bs[2], bs[1], bs[0]), np.float32)
+        info = (C.c_int * 4)()
+        st = self.lib.ccref_beam_dose(C.byref(self.setup), C.byref(b), _fp(fl), _fp(dose), _fp(terma), info)
+        if st != 0:
+            raise RuntimeError(f"reference harness status {st}")
+        return dose, terma, list(info)[:3]

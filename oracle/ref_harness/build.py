@@ -1,0 +1,47 @@
+"""Build recipe for the reference harness (test infrastructure only).
+
+Compiles oracle/ref_harness/ref_harness.cpp, which includes the reference's
+own kernel sources from the reference checkout, into oracle/_ref/libccref.so
+with the host C++ compiler (kernels executed on the CPU through
+cuda_cpu_shim.h).  Needs the reference checkout; the library is git-ignored
+and is only used to pin the oracle and to regenerate tests/golden.
+"""
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE = os.path.dirname(HERE)
+OUT = os.path.join(ORACLE, "_ref")
+LIB = os.path.join(OUT, "libccref.so")
+REF = os.environ.get("CCCS_REFERENCE", "/root/reference")
+
+
+def available():
+    return os.path.isdir(os.path.join(REF, "CCCS", "dosecalc-beam"))
+
+
+def build(verbose=False):
+    if not available():
+        raise RuntimeError(f"reference checkout not found at {REF}")
+    os.makedirs(OUT, exist_ok=True)
+    src = os.path.join(HERE, "ref_harness.cpp")
+    if os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(src),
+                                                            os.path.getmtime(os.path.join(HERE, "cuda_cpu_shim.h"))):
+        return LIB
+    cuda_inc = "/usr/local/cuda/include"
+    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-w",
+           "-I", HERE,
+           "-I", os.path.join(REF, "CCCS"),
+           "-I", os.path.join(REF, "CCCS", "include"),
+           "-I", os.path.join(REF, "CCCS", "include", "cuda-common"),
+           "-I", cuda_inc, src, "-o", LIB + ".tmp"]
+    if verbose:
+        print(" ".join(cmd))
+    subprocess.check_call(cmd)
+    os.replace(LIB + ".tmp", LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(verbose=True))

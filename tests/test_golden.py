@@ -1,0 +1,39 @@
+"""The oracle against golden outputs of the reference's own dosecalc-beam
+kernel source (cudaSiddon, cudaRaytrace, RowConvolve, REV2XYZdose compiled
+unmodified and run on the CPU; see tests/golden/make_golden.py).
+
+Tolerances: crop boxes identical; TERMA within 1e-4 of its maximum in
+99.9 % of voxels and within 2e-3 everywhere (FP32 vs FP64 can resolve a
+near-tie between Siddon plane crossings differently at density interfaces);
+dose within 6e-4 of Dmax (the reference is FP32, the oracle FP64; both
+filter with 8-bit texture weights, so last-bit differences in a texel
+coordinate can move a weight by 1/256)."""
+import numpy as np
+import pytest
+
+import golden_cases
+from oracle.oracle import Oracle
+
+
+@pytest.mark.parametrize("name", golden_cases.names())
+def test_oracle_matches_reference_kernels(name):
+    vol, phys, beams, doses, termas, bevs = golden_cases.load(name)
+    o = Oracle(vol, phys, kernel_mode=0, tex_emulate=True)
+    for b, dref, tref, bev in zip(beams, doses, termas, bevs):
+        d, info, t = o.beam_dose(b, return_terma=True)
+        assert list(info.bev_size) == bev
+        rel = np.abs(t - tref) / tref.max()
+        assert np.mean(rel > 1e-4) <= 1e-3 and rel.max() <= 2e-3
+        assert np.abs(d - dref).max() <= 6e-4 * dref.max(), np.abs(d - dref).max() / dref.max()
+
+
+def test_golden_fixtures_reproduce_from_reference_source():
+    """When the reference checkout is present, the harness regenerates the
+    committed fixtures."""
+    from oracle import ref_harness
+    if not ref_harness.available():
+        pytest.skip("reference checkout not present")
+    name = golden_cases.names()[0]
+    vol, phys, beams, doses, _, _ = golden_cases.load(name)
+    d, _, _ = ref_harness.ReferenceHarness(vol, phys, tex_emulate=True).beam_dose(beams[1])
+    assert np.abs(d - doses[1]).max() <= 1e-6 * doses[1].max()
