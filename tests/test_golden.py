@@ -33,7 +33,6 @@ def test_golden_fixtures_reproduce_from_reference_source():
     from oracle import ref_harness
     if not ref_harness.available():
         pytest.skip("reference checkout not present")
-    name = golden_cases.names()[0]
-    vol, phys, beams, doses, _, _ = golden_cases.load(name)
+    vol, phys, beams, doses, _, _ = golden_cases.load("slab32")
     d, _, _ = ref_harness.ReferenceHarness(vol, phys, tex_emulate=True).beam_dose(beams[1])
     assert np.abs(d - doses[1]).max() <= 1e-6 * doses[1].max()
