@@ -72,6 +72,15 @@ d3 inv_rot_kern(d3 v, double th, double ph) {
     return rot_axis(u, {std::cos(ph), 0, -std::sin(ph)}, th);
 }
 template <class F>
+void matrix_of_d(F f, double* M) {
+    d3 c[3] = {f({1, 0, 0}), f({0, 1, 0}), f({0, 0, 1})};
+    for (int j = 0; j < 3; j++) {
+        M[0 * 3 + j] = c[j].x;
+        M[1 * 3 + j] = c[j].y;
+        M[2 * 3 + j] = c[j].z;
+    }
+}
+template <class F>
 void matrix_of(F f, float* M) {
     d3 c[3] = {f({1, 0, 0}), f({0, 1, 0}), f({0, 0, 1})};
     for (int j = 0; j < 3; j++) {
@@ -264,6 +273,10 @@ void build_specs(const EeParams& P, const ee_beam* beams, int nbeams, EeBeamSpec
         double coll = B.coll;
         matrix_of([&](d3 v) { return rot_beam(v, az, zen, coll); }, S.MB);
         matrix_of([&](d3 v) { return inv_rot_beam(v, az, zen, coll); }, S.MBi);
+        matrix_of_d([&](d3 v) { return rot_beam(v, az, zen, coll); }, S.MBd);
+        S.srcd[0] = src.x; S.srcd[1] = src.y; S.srcd[2] = src.z;
+        S.dird[0] = dir.x; S.dird[1] = dir.y; S.dird[2] = dir.z;
+        S.isodistd = std::sqrt(id.x * id.x + id.y * id.y + id.z * id.z);
         S.fmap[0] = B.fmap_size[0]; S.fmap[1] = B.fmap_size[1];
         S.beamlet[0] = B.beamlet_size[0]; S.beamlet[1] = B.beamlet_size[1];
         S.fl_off = off;

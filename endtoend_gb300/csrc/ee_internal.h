@@ -60,6 +60,12 @@ struct EeBeamSpec {
     int t0[3];             // origin (full-grid voxel index)
     int tn[3];             // size
     long long t_off;       // element offset in the TERMA arena
+    // FP64 copies for re-deciding the beamlet of voxels whose FP32 fluence-map
+    // coordinate lands within 1e-4 of a beamlet boundary
+    double srcd[3];
+    double dird[3];
+    double MBd[9];
+    double isodistd;
 };
 
 // Per-cone geometry of one beam, computed on the device.

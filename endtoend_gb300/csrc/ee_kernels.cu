@@ -185,6 +185,35 @@ __device__ float siddon_rpl(const EeParams& P, f3 vox, f3 src, bool& iter_cap) {
     return rpl;
 }
 
+// The beamlet decision of beamlet_of in FP64 (same formula), for voxels
+// whose FP32 fluence-map coordinate is within 1e-4 of a beamlet boundary
+// (50x the FP32 error of that coordinate):
+// there the FP32 rounding of the projection decides which beamlet (of two
+// with different fluence) the voxel takes, and the result would not be
+// reproducible.  About two voxels per beam take this path.
+__device__ __noinline__ int beamlet_of_fp64(const EeParams& P, const EeBeamSpec& S, int x, int y, int z) {
+    const double vx = (double)P.start[0] + (double)x * (double)P.voxel[0];
+    const double vy = (double)P.start[1] + (double)y * (double)P.voxel[1];
+    const double vz = (double)P.start[2] + (double)z * (double)P.voxel[2];
+    const double dx = vx - S.srcd[0], dy = vy - S.srcd[1], dz = vz - S.srcd[2];
+    const double pl = dx * S.dird[0] + dy * S.dird[1] + dz * S.dird[2];
+    const double rx = dx - pl * S.dird[0], ry = dy - pl * S.dird[1], rz = dz - pl * S.dird[2];
+    const double rl = sqrt(rx * rx + ry * ry + rz * rz);
+    if (!(rl > 0.0)) return -1;
+    const double prl = fabs(pl);
+    const double trad = rl * fabs(S.isodistd / prl);
+    const double sc = trad / rl;
+    const double px = rx * sc, py = ry * sc, pz = rz * sc;
+    const double bx = S.MBd[0] * px + S.MBd[1] * py + S.MBd[2] * pz;
+    const double bz = S.MBd[6] * px + S.MBd[7] * py + S.MBd[8] * pz;
+    const double fx = bx / (double)S.beamlet[0] + S.fmap[0] * 0.5;
+    const double fz = bz / (double)S.beamlet[1] + S.fmap[1] * 0.5;
+    if (!(fx >= 0.0 && fx < (double)S.fmap[0] && fz >= 0.0 && fz < (double)S.fmap[1])) return -1;
+    const int idx = (int)floor(fx) + S.fmap[0] * (int)floor(fz);
+    if (idx < 0 || idx >= S.fmap[0] * S.fmap[1]) return -1;
+    return idx;
+}
+
 // Beamlet under this voxel (cudaSiddon.cu:143-165), -1 if none.
 __device__ __forceinline__ int beamlet_of(const EeBeamSpec& S, f3 vox) {
     f3 src = ld3(S.src), nd = ld3(S.dir);
@@ -199,6 +228,8 @@ __device__ __forceinline__ int beamlet_of(const EeBeamSpec& S, f3 vox) {
     f3 pb = mv(S.MB, pf);
     float fx = pb.x / S.beamlet[0] + S.fmap[0] * 0.5f;
     float fz = pb.z / S.beamlet[1] + S.fmap[1] * 0.5f;
+    // near a beamlet boundary (integer coordinate): signal the FP64 path
+    if (fabsf(fx - rintf(fx)) < 1e-4f || fabsf(fz - rintf(fz)) < 1e-4f) return -2;
     if (!(fx >= 0.f && fx < (float)S.fmap[0] && fz >= 0.f && fz < (float)S.fmap[1])) return -1;
     int idx = (int)floorf(fx) + S.fmap[0] * (int)floorf(fz);
     if (idx < 0 || idx >= S.fmap[0] * S.fmap[1]) return -1;
@@ -232,6 +263,7 @@ __global__ void __launch_bounds__(256) k_terma(EeParams P, const EeBeamSpec* __r
         f3 vox = mk(P.start[0] + x * P.voxel[0], P.start[1] + y * P.voxel[1], P.start[2] + z * P.voxel[2]);
         f3 src = ld3(S.src);
         int bl = beamlet_of(S, vox);
+        if (bl == -2) bl = beamlet_of_fp64(P, S, x, y, z);
         float t = 0.f, u = 0.f;
         if (bl >= 0) {
             float fl = __ldg(fluence + S.fl_off + bl);

@@ -113,14 +113,17 @@ class Oracle:
         keep.append(dens)
 
         def darr(x):
-            a = np.ascontiguousarray(np.asarray(x, dtype=np.float64).ravel())
+            # values rounded to float32 first: the engine receives float32
+            # through its C ABI, so the oracle evaluates the same numbers
+            a = np.ascontiguousarray(np.asarray(x, dtype=np.float32).astype(np.float64).ravel())
             keep.append(a)
             return _dp(a)
 
         s = OrcSetup()
         s.size[:] = [int(v) for v in vol.size]
-        s.voxel[:] = [float(v) for v in vol.voxel]
-        s.start[:] = [float(v) for v in vol.start]
+        f32 = lambda v: float(np.float32(v))
+        s.voxel[:] = [f32(v) for v in vol.voxel]
+        s.start[:] = [f32(v) for v in vol.start]
         s.bbox_start[:] = [int(v) for v in vol.bbox_start]
         s.bbox_size[:] = [int(v) for v in vol.bbox_size]
         s.density = dens.ctypes.data_as(C.POINTER(C.c_float))
@@ -132,19 +135,21 @@ class Oracle:
         s.exp_params = darr(phys.exp_params)
         s.theta_deg, s.phi_deg = darr(phys.theta_deg), darr(phys.phi_deg)
         s.kernel_mode = int(kernel_mode)
-        s.rev_latspacing, s.rev_longspacing, s.penumbra = phys.rev_latspacing, phys.rev_longspacing, phys.penumbra
+        s.rev_latspacing, s.rev_longspacing, s.penumbra = (f32(phys.rev_latspacing), f32(phys.rev_longspacing),
+                                                            f32(phys.penumbra))
         s.max_rev_size[:] = list(max_rev_size)
         s.tex_emulate = int(bool(tex_emulate))
         s.nthreads = int(nthreads or os.cpu_count() or 1)
         self.setup = s
 
     def _beam(self, b):
+        f32 = lambda v: float(np.float32(v))
         ob = OrcBeam()
-        ob.azimuth, ob.zenith, ob.coll = b.azimuth, b.zenith, b.coll
-        ob.iso[:] = [float(v) for v in b.isocenter]
-        ob.sad = b.sad
+        ob.azimuth, ob.zenith, ob.coll = f32(b.azimuth), f32(b.zenith), f32(b.coll)
+        ob.iso[:] = [f32(v) for v in b.isocenter]
+        ob.sad = f32(b.sad)
         ob.fmap[:] = [int(v) for v in b.fmap_size]
-        ob.beamlet[:] = [float(v) for v in b.beamlet_size]
+        ob.beamlet[:] = [f32(v) for v in b.beamlet_size]
         fl = np.ascontiguousarray(b.fluence, dtype=np.float32).ravel()
         return ob, fl
 
