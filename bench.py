@@ -268,9 +268,12 @@ def main():
     d2h = pin_dose.nbytes + pin_fgrad.nbytes
 
     # plain per-beam path: one beam per call
+    # plain path on beams spread evenly through the batch (same size mix)
     npl = min(args.plain_beams, len(beams))
-    pb = beams[:npl]
-    offs = np.cumsum([0] + [b.fluence.size for b in pb])
+    allofs = np.cumsum([0] + [b.fluence.size for b in beams])
+    pick = np.linspace(0, len(beams) - 1, npl).round().astype(int)
+    pb = [beams[i] for i in pick]
+    offs = allofs[pick]
     torch.cuda.synchronize()
     lat = []
     t0 = time.perf_counter()

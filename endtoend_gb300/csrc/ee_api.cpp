@@ -360,7 +360,7 @@ std::vector<int> plan_chunks(const ee_context* c, const EeBeamSpec* specs, int n
 
 struct ChunkDims {
     long long rev_total = 0, max_tvol = 1;
-    int max_line = 1, max_lines = 1, max_rows = 1;
+    int max_line = 1, max_lines = 1, max_rows = 1, max_tiles = 1;
 };
 
 // Device buffer growth: a freed buffer may still be read by queued kernels,
@@ -450,6 +450,7 @@ int pipeline(ee_context* c, const PipeArgs& A) {
             D.max_line = std::max(D.max_line, G.max_line);
             D.max_lines = std::max(D.max_lines, G.max_lines);
             D.max_rows = std::max(D.max_rows, G.rows);
+            D.max_tiles = std::max(D.max_tiles, G.tiles);
         }
         EE_CUDA(cudaMemcpyAsync(dge, hg, sizeof(EeBeamGeom) * nb, cudaMemcpyHostToDevice, s));
         c->last_geoms.insert(c->last_geoms.end(), hg, hg + nb);
@@ -488,7 +489,7 @@ int pipeline(ee_context* c, const PipeArgs& A) {
         EE_CUDA(grow(c, c->rev_grad, D.rev_total + 4));  // +4: vector-reduction padding
         EE_CUDA(cudaMemsetAsync(c->rev_grad.p, 0, sizeof(float) * D.rev_total, s));
         EE_CUDA(staged(c, EE_STAGE_GATHER_T, 1, [&] {
-            return ee_launch_gather_T(c->P, dsp, dge, dgrad, c->rev_grad.p, nb, D.max_rows, s);
+            return ee_launch_gather_T(c->P, dsp, dge, dgrad, c->rev_grad.p, nb, D.max_tiles, s);
         }));
         EE_CUDA(staged(c, EE_STAGE_CONE_T, 1, [&] {
             return ee_launch_cone_T(c->P, dsp, dge, c->rev_grad.p, c->terma_grad.p, nb, D.max_lines, D.max_line, s);

@@ -97,6 +97,8 @@ struct EeBeamGeom {
     // of the crop box dilated by 2 voxels, clipped to the calc bbox
     int gy0, gz0, gny, gnz;
     int rows;
+    int gx0, gnx;          // x range of the same AABB
+    int tiles;             // 8x8x4 patient tiles covering the AABB (adjoint gather)
     long long arena_off;   // element offset of this beam's REV arena
     long long arena_cap;   // elements available to this beam
     EeRayGeom ray[EE_MAX_RAYS];
@@ -119,7 +121,7 @@ cudaError_t ee_launch_gather(const EeParams& P, const EeBeamSpec* specs, const E
                              float* dose, int nbeams, int dose_mode, int max_rows, cudaStream_t s);
 // adjoint
 cudaError_t ee_launch_gather_T(const EeParams& P, const EeBeamSpec* specs, const EeBeamGeom* geoms,
-                               const float* dose_grad, float* rev_grad, int nbeams, int max_rows, cudaStream_t s);
+                               const float* dose_grad, float* rev_grad, int nbeams, int max_tiles, cudaStream_t s);
 cudaError_t ee_launch_cone_T(const EeParams& P, const EeBeamSpec* specs, const EeBeamGeom* geoms, const float* rev_grad,
                              float* terma_grad, int nbeams, int max_lines, int max_line, cudaStream_t s);
 cudaError_t ee_launch_terma_T(const EeParams& P, const EeBeamSpec* specs, const EeBeamGeom* geoms,

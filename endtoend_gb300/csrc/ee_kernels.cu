@@ -415,11 +415,13 @@ __global__ void k_geometry(EeParams P, const EeBeamSpec* __restrict__ specs, EeB
             lo[0] = fminf(lo[0], t.x); lo[1] = fminf(lo[1], t.y); lo[2] = fminf(lo[2], t.z);
             hi[0] = fmaxf(hi[0], t.x); hi[1] = fmaxf(hi[1], t.y); hi[2] = fmaxf(hi[2], t.z);
         }
+        int x0 = max(P.bb0[0], (int)floorf(lo[0]) - 1), x1 = min(P.bb0[0] + P.bbs[0] - 1, (int)ceilf(hi[0]) + 1);
         int y0 = max(P.bb0[1], (int)floorf(lo[1]) - 1), y1 = min(P.bb0[1] + P.bbs[1] - 1, (int)ceilf(hi[1]) + 1);
         int z0 = max(P.bb0[2], (int)floorf(lo[2]) - 1), z1 = min(P.bb0[2] + P.bbs[2] - 1, (int)ceilf(hi[2]) + 1);
-        G.gy0 = y0; G.gz0 = z0;
-        G.gny = max(0, y1 - y0 + 1); G.gnz = max(0, z1 - z0 + 1);
+        G.gx0 = x0; G.gy0 = y0; G.gz0 = z0;
+        G.gnx = max(0, x1 - x0 + 1); G.gny = max(0, y1 - y0 + 1); G.gnz = max(0, z1 - z0 + 1);
         G.rows = G.gny * G.gnz;
+        G.tiles = ((G.gnx + 7) / 8) * ((G.gny + 7) / 8) * ((G.gnz + 3) / 4);
         long long off = 0;
         int ml = 0, mls = 0;
         for (int r = 0; r < P.nrays; r++) {
@@ -875,38 +877,122 @@ __global__ void __launch_bounds__(ROW_WARPS * 32) k_gather(EeParams P, const EeB
     }
 }
 
-// Transpose of beam_voxel_dose over the same rows: rev_grad += S^T dose_grad.
-__global__ void __launch_bounds__(ROW_WARPS * 32) k_gather_T(EeParams P, const EeBeamSpec* __restrict__ specs,
-                                                             const EeBeamGeom* __restrict__ geoms,
-                                                             const float* __restrict__ dose_grad,
-                                                             float* __restrict__ rev_grad) {
+// Transpose of beam_voxel_dose: rev_grad += S^T dose_grad, one block per
+// 8x8x4 tile of patient voxels.  For each cone the tile's trilinear
+// footprint in the REV grid (an AABB computed from the tile's corners under
+// the affine patient -> REV map) is accumulated in shared memory first, then
+// flushed with one global reduction per non-zero REV sample: about 4x fewer
+// L2 atomics than scattering each voxel's 8 weights directly.
+constexpr int GT_TX = 8, GT_TY = 8, GT_TZ = 4;
+constexpr int GT_SMEM = 22 * 22 * 22;  // max footprint AABB (extent <= 8+8+4+2 per axis)
+
+__global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, const EeBeamSpec* __restrict__ specs,
+                                                                   const EeBeamGeom* __restrict__ geoms,
+                                                                   const float* __restrict__ dose_grad,
+                                                                   float* __restrict__ rev_grad) {
+    extern __shared__ float acc[];
+    __shared__ int s_box[6];
     const int b = blockIdx.z;
     const EeBeamGeom& G = geoms[b];
-    if (G.status != 0) return;
-    const int row = blockIdx.x * ROW_WARPS + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-    if (row >= G.rows) return;
-    const int y = G.gy0 + row % G.gny, z = G.gz0 + row / G.gny;
+    if (G.status != 0 || (int)blockIdx.x >= G.tiles) return;
     const EeBeamSpec& S = specs[b];
-    int x0, x1;
-    if (!row_span(P, S, G, y, z, x0, x1)) return;
-    const long long rbase = (long long)P.size[0] * (y + (long long)P.size[1] * z);
-    float* base = rev_grad + G.arena_off;
-    for (int x = x0 + lane; x <= x1; x += 32) {
-        float gd = __ldg(dose_grad + rbase + x);
-        if (gd == 0.f) continue;
-        f3 d = mk((float)x - G.lim_off[0], (float)y - G.lim_off[1], (float)z - G.lim_off[2]);
-        f3 bi = mv(S.MB, d);
+    const int ntx = (G.gnx + GT_TX - 1) / GT_TX, nty = (G.gny + GT_TY - 1) / GT_TY;
+    const int tile = blockIdx.x;
+    const int ox = G.gx0 + (tile % ntx) * GT_TX, oy = G.gy0 + ((tile / ntx) % nty) * GT_TY,
+              oz = G.gz0 + (tile / (ntx * nty)) * GT_TZ;
+    const int t = threadIdx.x;
+    const int x = ox + t % GT_TX, y = oy + (t / GT_TX) % GT_TY, z = oz + t / (GT_TX * GT_TY);
+    float gd = 0.f;
+    f3 bi = mk(0.f, 0.f, 0.f);
+    if (x < G.gx0 + G.gnx && y < G.gy0 + G.gny && z < G.gz0 + G.gnz) {
+        gd = __ldg(dose_grad + x + (long long)P.size[0] * (y + (long long)P.size[1] * z));
+        bi = mv(S.MB, mk((float)x - G.lim_off[0], (float)y - G.lim_off[1], (float)z - G.lim_off[2]));
         if (bi.x < -2.f || bi.y < -2.f || bi.z < -2.f || bi.x > G.bev[0] + 2.f || bi.y > G.bev[1] + 2.f ||
             bi.z > G.bev[2] + 2.f)
-            continue;
-        for (int r = 0; r < P.nrays; r++) {
-            const EeRayGeom& R = G.ray[r];
-            f3 q = mv(R.M, bi) - ld3(R.q0);
-            if (q.y >= (float)R.rev[0] || q.z >= (float)R.rev[1] || q.x >= (float)R.rev[2] || q.x < 0.f ||
-                q.y < 0.f || q.z < 0.f)
-                continue;
-            tri_border_scatter(base + R.offset, R.rev[0], R.rev[1], R.rev[2], q.y, q.z, q.x, gd);
+            gd = 0.f;
+    }
+    if (!__syncthreads_or(gd != 0.f)) return;
+    // BEV index of the tile origin and the BEV steps of a unit patient step
+    const f3 b0 = mv(S.MB, mk((float)ox - G.lim_off[0], (float)oy - G.lim_off[1], (float)oz - G.lim_off[2]));
+    float* base = rev_grad + G.arena_off;
+    for (int r = 0; r < P.nrays; r++) {
+        const EeRayGeom& R = G.ray[r];
+        // q(v) = M (MB (v - lim_off)) - q0; columns of A = M MB
+        if (t == 0) {
+            f3 q0 = mv(R.M, b0) - ld3(R.q0);
+            float qa[3] = {q0.x, q0.y, q0.z}, lo[3], hi[3];
+            f3 cx = mv(R.M, mk(S.MB[0], S.MB[3], S.MB[6])), cy = mv(R.M, mk(S.MB[1], S.MB[4], S.MB[7])),
+               cz = mv(R.M, mk(S.MB[2], S.MB[5], S.MB[8]));
+            float c[3][3] = {{cx.x, cy.x, cz.x}, {cx.y, cy.y, cz.y}, {cx.z, cy.z, cz.z}};
+            const float ext[3] = {(float)(GT_TX - 1), (float)(GT_TY - 1), (float)(GT_TZ - 1)};
+            for (int a = 0; a < 3; a++) {
+                lo[a] = hi[a] = qa[a];
+                for (int k = 0; k < 3; k++) {
+                    float d = c[a][k] * ext[k];
+                    lo[a] += fminf(d, 0.f);
+                    hi[a] += fmaxf(d, 0.f);
+                }
+            }
+            // REV axes: q.y -> rev[0] (along the line), q.z -> rev[1], q.x -> rev[2]
+            int l0 = max(0, (int)floorf(lo[1])), h0 = min(R.rev[0] - 1, (int)floorf(hi[1]) + 1);
+            int l1 = max(0, (int)floorf(lo[2])), h1 = min(R.rev[1] - 1, (int)floorf(hi[2]) + 1);
+            int l2 = max(0, (int)floorf(lo[0])), h2 = min(R.rev[2] - 1, (int)floorf(hi[0]) + 1);
+            s_box[0] = l0; s_box[1] = h0 - l0 + 1;
+            s_box[2] = l1; s_box[3] = h1 - l1 + 1;
+            s_box[4] = l2; s_box[5] = h2 - l2 + 1;
         }
+        __syncthreads();
+        const int l0 = s_box[0], n0 = s_box[1], l1 = s_box[2], n1 = s_box[3], l2 = s_box[4], n2 = s_box[5];
+        const bool empty = n0 <= 0 || n1 <= 0 || n2 <= 0;
+        const int nbox = empty ? 0 : n0 * n1 * n2;
+        if (nbox > 0 && nbox <= GT_SMEM) {
+            for (int k = t; k < nbox; k += blockDim.x) acc[k] = 0.f;
+            __syncthreads();
+            if (gd != 0.f) {
+                f3 q = mv(R.M, bi) - ld3(R.q0);
+                if (!(q.y >= (float)R.rev[0] || q.z >= (float)R.rev[1] || q.x >= (float)R.rev[2] || q.x < 0.f ||
+                      q.y < 0.f || q.z < 0.f)) {
+                    float f0 = floorf(q.y), f1 = floorf(q.z), f2 = floorf(q.x);
+                    int i0 = (int)f0, i1 = (int)f1, i2 = (int)f2;
+                    float a0 = q.y - f0, a1 = q.z - f1, a2 = q.x - f2;
+#pragma unroll
+                    for (int d2 = 0; d2 < 2; d2++) {
+                        int k2 = i2 + d2 - l2;
+                        if (i2 + d2 >= R.rev[2] || k2 < 0 || k2 >= n2) continue;
+                        float w2 = (d2 ? a2 : 1.f - a2) * gd;
+#pragma unroll
+                        for (int d1 = 0; d1 < 2; d1++) {
+                            int k1 = i1 + d1 - l1;
+                            if (i1 + d1 >= R.rev[1] || k1 < 0 || k1 >= n1) continue;
+                            float w1 = (d1 ? a1 : 1.f - a1) * w2;
+#pragma unroll
+                            for (int d0 = 0; d0 < 2; d0++) {
+                                int k0 = i0 + d0 - l0;
+                                if (i0 + d0 >= R.rev[0] || k0 < 0 || k0 >= n0) continue;
+                                atomicAdd(acc + k0 + n0 * (k1 + n1 * k2), (d0 ? a0 : 1.f - a0) * w1);
+                            }
+                        }
+                    }
+                }
+            }
+            __syncthreads();
+            float* rb = base + R.offset;
+            for (int k = t; k < nbox; k += blockDim.x) {
+                float v = acc[k];
+                if (v != 0.f) {
+                    int k0 = k % n0, k1 = (k / n0) % n1, k2 = k / (n0 * n1);
+                    atomicAdd(rb + (l0 + k0) + (long long)R.rev[0] * ((l1 + k1) + (long long)R.rev[1] * (l2 + k2)), v);
+                }
+            }
+        } else if (nbox > GT_SMEM && gd != 0.f) {
+            // footprint too large for shared memory (not expected for 8x8x4
+            // tiles): scatter directly
+            f3 q = mv(R.M, bi) - ld3(R.q0);
+            if (!(q.y >= (float)R.rev[0] || q.z >= (float)R.rev[1] || q.x >= (float)R.rev[2] || q.x < 0.f ||
+                  q.y < 0.f || q.z < 0.f))
+                tri_border_scatter(base + R.offset, R.rev[0], R.rev[1], R.rev[2], q.y, q.z, q.x, gd);
+        }
+        __syncthreads();
     }
 }
 
@@ -987,9 +1073,12 @@ cudaError_t ee_launch_gather(const EeParams& P, const EeBeamSpec* specs, const E
 }
 
 cudaError_t ee_launch_gather_T(const EeParams& P, const EeBeamSpec* specs, const EeBeamGeom* geoms,
-                               const float* dose_grad, float* rev_grad, int nbeams, int max_rows, cudaStream_t s) {
-    dim3 grid(grid1(max_rows, ROW_WARPS), 1, nbeams);
-    k_gather_T<<<grid, ROW_WARPS * 32, 0, s>>>(P, specs, geoms, dose_grad, rev_grad);
+                               const float* dose_grad, float* rev_grad, int nbeams, int max_tiles, cudaStream_t s) {
+    const size_t smem = sizeof(float) * GT_SMEM;
+    cudaError_t e = cudaFuncSetAttribute((const void*)k_gather_T, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    dim3 grid(max(1, max_tiles), 1, nbeams);
+    k_gather_T<<<grid, GT_TX * GT_TY * GT_TZ, smem, s>>>(P, specs, geoms, dose_grad, rev_grad);
     return cudaGetLastError();
 }
 
