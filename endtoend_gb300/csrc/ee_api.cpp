@@ -456,6 +456,7 @@ int pipeline(ee_context* c, const PipeArgs& A) {
         c->last_geoms.insert(c->last_geoms.end(), hg, hg + nb);
         if (!fwd) continue;
         EE_CUDA(grow(c, c->rev, D.rev_total));
+        EE_CUDA(cudaMemsetAsync(c->rev.p, 0, sizeof(float) * D.rev_total, s));
         EE_CUDA(staged(c, EE_STAGE_CONE, 1, [&] {
             return ee_launch_cone(c->P, dsp, dge, c->terma.p, c->rev.p, nb, D.max_lines, D.max_line, s);
         }));
@@ -487,12 +488,14 @@ int pipeline(ee_context* c, const PipeArgs& A) {
         const EeBeamGeom* dge = c->d_geoms.p + b0;
         const ChunkDims& D = dims[k];
         EE_CUDA(grow(c, c->rev_grad, D.rev_total + 4));  // +4: vector-reduction padding
+        EE_CUDA(grow(c, c->rev, D.rev_total));             // scratch of the exp-mode adjoint cone
         EE_CUDA(cudaMemsetAsync(c->rev_grad.p, 0, sizeof(float) * D.rev_total, s));
         EE_CUDA(staged(c, EE_STAGE_GATHER_T, 1, [&] {
             return ee_launch_gather_T(c->P, dsp, dge, dgrad, c->rev_grad.p, nb, D.max_tiles, s);
         }));
         EE_CUDA(staged(c, EE_STAGE_CONE_T, 1, [&] {
-            return ee_launch_cone_T(c->P, dsp, dge, c->rev_grad.p, c->terma_grad.p, nb, D.max_lines, D.max_line, s);
+            return ee_launch_cone_T(c->P, dsp, dge, c->rev_grad.p, c->rev.p, c->terma_grad.p, nb, D.max_lines,
+                                    D.max_line, s);
         }));
         EE_CUDA(staged(c, EE_STAGE_TERMA_T, 1, [&] {
             return ee_launch_terma_T(c->P, dsp, dge, c->unit.p, c->bl_idx.p, c->terma_grad.p, A.d_fgrad, nb,

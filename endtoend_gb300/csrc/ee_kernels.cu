@@ -729,6 +729,191 @@ __global__ void __launch_bounds__(CONE_WARPS * 32) k_cone(EeParams P, const EeBe
     }
 }
 
+// ------------------------------------------- cone: one lane per line ----
+// EE_KERNEL_EXP fast path.  Each thread owns one REV line (adjacent threads
+// own adjacent lines, so their segments and gathers stay close): it computes
+// its segment analytically and runs the recurrence sequentially, without
+// shuffles or shared memory.  Forward pass (ascending i) stores D_fwd in the
+// pre-zeroed REV arena; reverse pass (descending i) gathers the samples again,
+// adds its part and applies 1/nphi.  Same operator as line_scan.
+struct LineFrame {
+    f3 bl, gl, bx, gx;
+};
+
+__device__ __forceinline__ LineFrame line_frame(const EeRayGeom& R, int tY, int tZ) {
+    LineFrame F;
+    F.bl = ld3(R.B0) + ld3(R.By) * (float)tY + ld3(R.Bz) * (float)tZ;
+    F.gl = ld3(R.G0) + ld3(R.Gy) * (float)tY + ld3(R.Gz) * (float)tZ;
+    F.bx = ld3(R.Bx);
+    F.gx = ld3(R.Gx);
+    return F;
+}
+
+// One REV sample (device.cu:47-79): returns rho (sentinel < 0 outside) and,
+// when terma_b != nullptr, the TERMA sample.
+__device__ __forceinline__ float sample_rho(const EeParams& P, const EeBeamSpec& S, const EeBeamGeom& G,
+                                            const LineFrame& F, int i, const float* __restrict__ terma_b, float& t) {
+    const float fi = (float)i;
+    f3 bev = F.bl + F.bx * fi;
+    t = 0.f;
+    if (bev.x < 0.f || bev.y < 0.f || bev.z < 0.f || bev.x >= (float)G.bev[0] || bev.y >= (float)G.bev[1] ||
+        bev.z >= (float)G.bev[2])
+        return -3.f;
+    f3 g = F.gl + F.gx * fi;
+    if (g.x < (float)P.bb0[0] || g.x >= (float)(P.bb0[0] + P.bbs[0]) || g.y < (float)P.bb0[1] ||
+        g.y >= (float)(P.bb0[1] + P.bbs[1]) || g.z < (float)P.bb0[2] || g.z >= (float)(P.bb0[2] + P.bbs[2]))
+        return -2.f;
+    if (terma_b)
+        t = tri_border(terma_b, S.tn[0], S.tn[1], S.tn[2], g.x - (float)S.t0[0], g.y - (float)S.t0[1],
+                       g.z - (float)S.t0[2]);
+    return tex3D<float>(P.dens_tex, g.x + 0.5f, g.y + 0.5f, g.z + 0.5f);
+}
+
+constexpr int LANE_BLOCK = 128;
+
+__global__ void __launch_bounds__(LANE_BLOCK) k_cone_lane(EeParams P, const EeBeamSpec* __restrict__ specs,
+                                                          const EeBeamGeom* __restrict__ geoms,
+                                                          const float* __restrict__ terma, float* __restrict__ rev) {
+    const int ray = blockIdx.y, b = blockIdx.z;
+    const EeBeamGeom& G = geoms[b];
+    if (G.status != 0) return;
+    const EeRayGeom& R = G.ray[ray];
+    const int line = blockIdx.x * LANE_BLOCK + threadIdx.x;
+    if (line >= R.nlines) return;
+    const int L = R.rev[0];
+    const int tY = line % R.rev[1], tZ = line / R.rev[1];
+    int i0, n;
+    line_segment(P, G, R, tY, tZ, L, i0, n);
+    if (n <= 0) return;
+    const EeBeamSpec& S = specs[b];
+    const float* tb = terma + S.t_off;
+    const LineFrame F = line_frame(R, tY, tZ);
+    float* out = rev + G.arena_off + R.offset + (long long)line * L;
+    const EeRayConst& RC = P.rays[ray];
+    const float delr = P.lng;
+    {   // forward direction: contributions from k < i, kernel row P
+        const float* prm = P.expp + 4 * RC.row_fwd;
+        const float c1 = prm[0] / prm[1], c2 = prm[2] / prm[3];
+        const float e1 = -0.5f * prm[1] * delr, e2 = -0.5f * prm[3] * delr;
+        float Y1 = 0.f, Y2 = 0.f, tm = 0.f, hm1 = 1.f, hm2 = 1.f;
+        for (int i = i0; i < i0 + n; i++) {
+            float t;
+            const float r = sample_rho(P, S, G, F, i, tb, t);
+            const bool v = r >= 0.f;
+            const float h1 = v ? __expf(e1 * r) : 1.f, h2 = v ? __expf(e2 * r) : 1.f;
+            if (!v) t = 0.f;
+            out[i] = v ? c1 * (Y1 + tm * (1.f - hm1)) + c2 * (Y2 + tm * (1.f - hm2)) : 0.f;
+            Y1 = fmaf(h1 * h1, Y1, tm * h1 * (1.f - hm1 * h1));
+            Y2 = fmaf(h2 * h2, Y2, tm * h2 * (1.f - hm2 * h2));
+            tm = t; hm1 = h1; hm2 = h2;
+        }
+    }
+    {   // reverse direction: contributions from k > i, kernel row ntheta-1-P
+        const float* prm = P.expp + 4 * RC.row_rev;
+        const float c1 = prm[0] / prm[1], c2 = prm[2] / prm[3];
+        const float e1 = -0.5f * prm[1] * delr, e2 = -0.5f * prm[3] * delr;
+        const float inv_nphi = 1.f / (float)P.nphi;
+        float Y1 = 0.f, Y2 = 0.f, tm = 0.f, hm1 = 1.f, hm2 = 1.f;
+        for (int i = i0 + n - 1; i >= i0; i--) {
+            float t;
+            const float r = sample_rho(P, S, G, F, i, tb, t);
+            const bool v = r >= 0.f;
+            const float h1 = v ? __expf(e1 * r) : 1.f, h2 = v ? __expf(e2 * r) : 1.f;
+            if (!v) t = 0.f;
+            const float d = c1 * (Y1 + tm * (1.f - hm1)) + c2 * (Y2 + tm * (1.f - hm2));
+            out[i] = v ? (out[i] + d) * inv_nphi : 0.f;
+            Y1 = fmaf(h1 * h1, Y1, tm * h1 * (1.f - hm1 * h1));
+            Y2 = fmaf(h2 * h2, Y2, tm * h2 * (1.f - hm2 * h2));
+            tm = t; hm1 = h1; hm2 = h2;
+        }
+    }
+}
+
+// Adjoint of k_cone_lane followed by the transpose of the REV TERMA resample.
+// Pass A (descending i) runs the transpose of the forward recurrence and
+// stores its contribution to Tbar[i-1] in `scratch` (the REV-arena layout);
+// pass B (ascending i) runs the transpose of the reverse recurrence, adds its
+// contribution to Tbar[i] and scatters Tbar[i] into the TERMA-box gradient.
+__global__ void __launch_bounds__(LANE_BLOCK) k_cone_T_lane(EeParams P, const EeBeamSpec* __restrict__ specs,
+                                                            const EeBeamGeom* __restrict__ geoms,
+                                                            const float* __restrict__ rev_grad,
+                                                            float* __restrict__ scratch, float* __restrict__ terma_grad) {
+    const int ray = blockIdx.y, b = blockIdx.z;
+    const EeBeamGeom& G = geoms[b];
+    if (G.status != 0) return;
+    const EeRayGeom& R = G.ray[ray];
+    const int line = blockIdx.x * LANE_BLOCK + threadIdx.x;
+    if (line >= R.nlines) return;
+    const int L = R.rev[0];
+    const int tY = line % R.rev[1], tZ = line / R.rev[1];
+    int i0, n;
+    line_segment(P, G, R, tY, tZ, L, i0, n);
+    if (n <= 0) return;
+    const EeBeamSpec& S = specs[b];
+    const LineFrame F = line_frame(R, tY, tZ);
+    const long long row = G.arena_off + R.offset + (long long)line * L;
+    const float* gin = rev_grad + row;
+    float* sA = scratch + row;
+    const EeRayConst& RC = P.rays[ray];
+    const float delr = P.lng, inv_nphi = 1.f / (float)P.nphi;
+    const int i1 = i0 + n - 1;
+    float dummy;
+    {   // pass A: transpose of the forward recurrence, walking down
+        const float* prm = P.expp + 4 * RC.row_fwd;
+        const float c1 = prm[0] / prm[1], c2 = prm[2] / prm[3];
+        const float e1 = -0.5f * prm[1] * delr, e2 = -0.5f * prm[3] * delr;
+        float r = sample_rho(P, S, G, F, i1, nullptr, dummy);
+        bool v = r >= 0.f;
+        float h1 = v ? __expf(e1 * r) : 1.f, h2 = v ? __expf(e2 * r) : 1.f;
+        float Z1 = 0.f, Z2 = 0.f;
+        sA[i1] = 0.f;
+        for (int i = i1; i >= i0; i--) {
+            const float gi = v ? gin[i] * inv_nphi : 0.f;
+            if (i > i0) {
+                const float rm = sample_rho(P, S, G, F, i - 1, nullptr, dummy);
+                const bool vm = rm >= 0.f;
+                const float hm1 = vm ? __expf(e1 * rm) : 1.f, hm2 = vm ? __expf(e2 * rm) : 1.f;
+                sA[i - 1] = vm ? c1 * gi * (1.f - hm1) + Z1 * h1 * (1.f - hm1 * h1) + c2 * gi * (1.f - hm2) +
+                                     Z2 * h2 * (1.f - hm2 * h2)
+                               : 0.f;
+                Z1 = fmaf(h1 * h1, Z1, c1 * gi);
+                Z2 = fmaf(h2 * h2, Z2, c2 * gi);
+                v = vm; h1 = hm1; h2 = hm2;
+            }
+        }
+    }
+    {   // pass B: transpose of the reverse recurrence, walking up; scatter
+        const float* prm = P.expp + 4 * RC.row_rev;
+        const float c1 = prm[0] / prm[1], c2 = prm[2] / prm[3];
+        const float e1 = -0.5f * prm[1] * delr, e2 = -0.5f * prm[3] * delr;
+        float* tg = terma_grad + S.t_off;
+        float r = sample_rho(P, S, G, F, i0, nullptr, dummy);
+        bool v = r >= 0.f;
+        float h1 = v ? __expf(e1 * r) : 1.f, h2 = v ? __expf(e2 * r) : 1.f;
+        float Z1 = 0.f, Z2 = 0.f, cprev = 0.f;
+        for (int i = i0; i <= i1; i++) {
+            const float gi = v ? gin[i] * inv_nphi : 0.f;
+            const float tot = sA[i] + cprev;
+            if (v && tot != 0.f) {
+                f3 gp = F.gl + F.gx * (float)i;
+                tri_border_scatter(tg, S.tn[0], S.tn[1], S.tn[2], gp.x - (float)S.t0[0], gp.y - (float)S.t0[1],
+                                   gp.z - (float)S.t0[2], tot);
+            }
+            if (i < i1) {
+                const float rm = sample_rho(P, S, G, F, i + 1, nullptr, dummy);
+                const bool vm = rm >= 0.f;
+                const float hm1 = vm ? __expf(e1 * rm) : 1.f, hm2 = vm ? __expf(e2 * rm) : 1.f;
+                cprev = vm ? c1 * gi * (1.f - hm1) + Z1 * h1 * (1.f - hm1 * h1) + c2 * gi * (1.f - hm2) +
+                                 Z2 * h2 * (1.f - hm2 * h2)
+                           : 0.f;
+                Z1 = fmaf(h1 * h1, Z1, c1 * gi);
+                Z2 = fmaf(h2 * h2, Z2, c2 * gi);
+                v = vm; h1 = hm1; h2 = hm2;
+            }
+        }
+    }
+}
+
 // Adjoint of k_cone followed by the transpose of the REV TERMA resample:
 // terma_grad (bbox grid) += R_T^T C^T rev_grad.
 __global__ void __launch_bounds__(CONE_WARPS * 32) k_cone_T(EeParams P, const EeBeamSpec* __restrict__ specs,
@@ -1056,6 +1241,11 @@ static cudaError_t cone_attr(const void* fn, size_t smem) {
 
 cudaError_t ee_launch_cone(const EeParams& P, const EeBeamSpec* specs, const EeBeamGeom* geoms, const float* terma,
                            float* rev, int nbeams, int max_lines, int max_line, cudaStream_t s) {
+    if (P.mode == 1) {  // exp kernel: one lane per line; the caller zeroed `rev`
+        dim3 grid(grid1(max_lines, LANE_BLOCK), P.nrays, nbeams);
+        k_cone_lane<<<grid, LANE_BLOCK, 0, s>>>(P, specs, geoms, terma, rev);
+        return cudaGetLastError();
+    }
     size_t smem = cone_smem(max_line);
     cudaError_t e = cone_attr((const void*)k_cone, smem);
     if (e != cudaSuccess) return e;
@@ -1083,7 +1273,13 @@ cudaError_t ee_launch_gather_T(const EeParams& P, const EeBeamSpec* specs, const
 }
 
 cudaError_t ee_launch_cone_T(const EeParams& P, const EeBeamSpec* specs, const EeBeamGeom* geoms, const float* rev_grad,
-                             float* terma_grad, int nbeams, int max_lines, int max_line, cudaStream_t s) {
+                             float* scratch, float* terma_grad, int nbeams, int max_lines, int max_line,
+                             cudaStream_t s) {
+    if (P.mode == 1 && scratch) {
+        dim3 grid(grid1(max_lines, LANE_BLOCK), P.nrays, nbeams);
+        k_cone_T_lane<<<grid, LANE_BLOCK, 0, s>>>(P, specs, geoms, rev_grad, scratch, terma_grad);
+        return cudaGetLastError();
+    }
     size_t smem = cone_smem(max_line);
     cudaError_t e = cone_attr((const void*)k_cone_T, smem);
     if (e != cudaSuccess) return e;
