@@ -698,7 +698,9 @@ __global__ void __launch_bounds__(CONE_WARPS * 32) k_cone(EeParams P, const EeBe
     float* rho = sm + (size_t)warp * 3 * maxL;
     float* T = rho + maxL;
     float* D = T + maxL;
-    float* out = rev + G.arena_off + R.offset + (long long)line * L;
+    // REV arena layout: [i][tZ][tY] (line index fastest)
+    const long long nl = R.nlines;
+    float* out = rev + G.arena_off + R.offset + line;
     int i0, n;
     line_segment(P, G, R, tY, tZ, L, i0, n);
     if (n > 0) {
@@ -723,10 +725,7 @@ __global__ void __launch_bounds__(CONE_WARPS * 32) k_cone(EeParams P, const EeBe
         }
         __syncwarp();
     }
-    for (int i = lane; i < L; i += 32) {
-        int k = i - i0;
-        out[i] = (k >= 0 && k < n) ? D[k] : 0.f;
-    }
+    for (int k = lane; k < n; k += 32) out[(long long)(i0 + k) * nl] = D[k];
 }
 
 // ------------------------------------------- cone: one lane per line ----
@@ -788,7 +787,10 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_lane(EeParams P, const EeBe
     const EeBeamSpec& S = specs[b];
     const float* tb = terma + S.t_off;
     const LineFrame F = line_frame(R, tY, tZ);
-    float* out = rev + G.arena_off + R.offset + (long long)line * L;
+    // REV arena layout [i][tZ][tY]: lanes (consecutive lines) access
+    // consecutive addresses at every i
+    const long long nl = R.nlines;
+    float* out = rev + G.arena_off + R.offset + line;
     const EeRayConst& RC = P.rays[ray];
     const float delr = P.lng;
     {   // forward direction: contributions from k < i, kernel row P
@@ -802,7 +804,7 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_lane(EeParams P, const EeBe
             const bool v = r >= 0.f;
             const float h1 = v ? __expf(e1 * r) : 1.f, h2 = v ? __expf(e2 * r) : 1.f;
             if (!v) t = 0.f;
-            out[i] = v ? c1 * (Y1 + tm * (1.f - hm1)) + c2 * (Y2 + tm * (1.f - hm2)) : 0.f;
+            out[i * nl] = v ? c1 * (Y1 + tm * (1.f - hm1)) + c2 * (Y2 + tm * (1.f - hm2)) : 0.f;
             Y1 = fmaf(h1 * h1, Y1, tm * h1 * (1.f - hm1 * h1));
             Y2 = fmaf(h2 * h2, Y2, tm * h2 * (1.f - hm2 * h2));
             tm = t; hm1 = h1; hm2 = h2;
@@ -821,7 +823,7 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_lane(EeParams P, const EeBe
             const float h1 = v ? __expf(e1 * r) : 1.f, h2 = v ? __expf(e2 * r) : 1.f;
             if (!v) t = 0.f;
             const float d = c1 * (Y1 + tm * (1.f - hm1)) + c2 * (Y2 + tm * (1.f - hm2));
-            out[i] = v ? (out[i] + d) * inv_nphi : 0.f;
+            out[i * nl] = v ? (out[i * nl] + d) * inv_nphi : 0.f;
             Y1 = fmaf(h1 * h1, Y1, tm * h1 * (1.f - hm1 * h1));
             Y2 = fmaf(h2 * h2, Y2, tm * h2 * (1.f - hm2 * h2));
             tm = t; hm1 = h1; hm2 = h2;
@@ -851,7 +853,8 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_T_lane(EeParams P, const Ee
     if (n <= 0) return;
     const EeBeamSpec& S = specs[b];
     const LineFrame F = line_frame(R, tY, tZ);
-    const long long row = G.arena_off + R.offset + (long long)line * L;
+    const long long nl = R.nlines;  // REV arena layout [i][tZ][tY]
+    const long long row = G.arena_off + R.offset + line;
     const float* gin = rev_grad + row;
     float* sA = scratch + row;
     const EeRayConst& RC = P.rays[ray];
@@ -866,16 +869,16 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_T_lane(EeParams P, const Ee
         bool v = r >= 0.f;
         float h1 = v ? __expf(e1 * r) : 1.f, h2 = v ? __expf(e2 * r) : 1.f;
         float Z1 = 0.f, Z2 = 0.f;
-        sA[i1] = 0.f;
+        sA[i1 * nl] = 0.f;
         for (int i = i1; i >= i0; i--) {
-            const float gi = v ? gin[i] * inv_nphi : 0.f;
+            const float gi = v ? gin[i * nl] * inv_nphi : 0.f;
             if (i > i0) {
                 const float rm = sample_rho(P, S, G, F, i - 1, nullptr, dummy);
                 const bool vm = rm >= 0.f;
                 const float hm1 = vm ? __expf(e1 * rm) : 1.f, hm2 = vm ? __expf(e2 * rm) : 1.f;
-                sA[i - 1] = vm ? c1 * gi * (1.f - hm1) + Z1 * h1 * (1.f - hm1 * h1) + c2 * gi * (1.f - hm2) +
-                                     Z2 * h2 * (1.f - hm2 * h2)
-                               : 0.f;
+                sA[(i - 1) * nl] = vm ? c1 * gi * (1.f - hm1) + Z1 * h1 * (1.f - hm1 * h1) + c2 * gi * (1.f - hm2) +
+                                            Z2 * h2 * (1.f - hm2 * h2)
+                                      : 0.f;
                 Z1 = fmaf(h1 * h1, Z1, c1 * gi);
                 Z2 = fmaf(h2 * h2, Z2, c2 * gi);
                 v = vm; h1 = hm1; h2 = hm2;
@@ -892,8 +895,8 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_T_lane(EeParams P, const Ee
         float h1 = v ? __expf(e1 * r) : 1.f, h2 = v ? __expf(e2 * r) : 1.f;
         float Z1 = 0.f, Z2 = 0.f, cprev = 0.f;
         for (int i = i0; i <= i1; i++) {
-            const float gi = v ? gin[i] * inv_nphi : 0.f;
-            const float tot = sA[i] + cprev;
+            const float gi = v ? gin[i * nl] * inv_nphi : 0.f;
+            const float tot = sA[i * nl] + cprev;
             if (v && tot != 0.f) {
                 f3 gp = F.gl + F.gx * (float)i;
                 tri_border_scatter(tg, S.tn[0], S.tn[1], S.tn[2], gp.x - (float)S.t0[0], gp.y - (float)S.t0[1],
@@ -949,11 +952,11 @@ __global__ void __launch_bounds__(CONE_WARPS * 32) k_cone_T(EeParams P, const Ee
     line_segment(P, G, R, tY, tZ, L, i0, n);
     if (n == 0) return;
     gather_line(P, S, G, R, nullptr, tY, tZ, i0, n, lane, rho, nullptr);
-    const float* gin = rev_grad + G.arena_off + R.offset + (long long)line * L + i0;
+    const float* gin = rev_grad + G.arena_off + R.offset + line + (long long)i0 * R.nlines;
     const float inv_nphi = 1.f / (float)P.nphi;
     __syncwarp();
     for (int k = lane; k < n; k += 32) {
-        g[k] = rho[k] >= 0.f ? gin[k] * inv_nphi : 0.f;
+        g[k] = rho[k] >= 0.f ? gin[(long long)k * R.nlines] * inv_nphi : 0.f;
         Tb[k] = 0.f;
     }
     __syncwarp();
@@ -1005,7 +1008,8 @@ __device__ __forceinline__ float beam_voxel_dose(const EeParams& P, const EeBeam
         if (q.y >= (float)R.rev[0] || q.z >= (float)R.rev[1] || q.x >= (float)R.rev[2] || q.x < 0.f || q.y < 0.f ||
             q.z < 0.f)
             continue;
-        acc += tri_border(base + R.offset, R.rev[0], R.rev[1], R.rev[2], q.y, q.z, q.x);
+        // REV arena layout [i][tZ][tY]: x = tY (q.z), y = tZ (q.x), z = i (q.y)
+        acc += tri_border(base + R.offset, R.rev[1], R.rev[2], R.rev[0], q.z, q.x, q.y);
     }
     return acc;
 }
@@ -1166,7 +1170,7 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
                 float v = acc[k];
                 if (v != 0.f) {
                     int k0 = k % n0, k1 = (k / n0) % n1, k2 = k / (n0 * n1);
-                    atomicAdd(rb + (l0 + k0) + (long long)R.rev[0] * ((l1 + k1) + (long long)R.rev[1] * (l2 + k2)), v);
+                    atomicAdd(rb + (l1 + k1) + (long long)R.rev[1] * ((l2 + k2) + (long long)R.rev[2] * (l0 + k0)), v);
                 }
             }
         } else if (nbox > GT_SMEM && gd != 0.f) {
@@ -1175,7 +1179,7 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
             f3 q = mv(R.M, bi) - ld3(R.q0);
             if (!(q.y >= (float)R.rev[0] || q.z >= (float)R.rev[1] || q.x >= (float)R.rev[2] || q.x < 0.f ||
                   q.y < 0.f || q.z < 0.f))
-                tri_border_scatter(base + R.offset, R.rev[0], R.rev[1], R.rev[2], q.y, q.z, q.x, gd);
+                tri_border_scatter(base + R.offset, R.rev[1], R.rev[2], R.rev[0], q.z, q.x, q.y, gd);
         }
         __syncthreads();
     }
