@@ -166,6 +166,7 @@ struct ee_context {
     DevBuf<EeBeamSpec> d_specs;
     DevBuf<EeBeamGeom> d_geoms;
     DevBuf<float> terma, unit, rev, rev_grad, terma_grad;
+    DevBuf<float2> samples;  // per-REV-sample (rho, T) / (contribution, rho) of the exp-mode cone kernels
     DevBuf<int> bl_idx;
     DevBuf<float> io_fluence, io_dose, io_grad;
     DevBuf<float> xf, xg, spread_w;
@@ -345,7 +346,8 @@ long long nfull_of(const ee_context* c) { return (long long)c->P.size[0] * c->P.
 std::vector<int> plan_chunks(const ee_context* c, const EeBeamSpec* specs, int nbeams, bool adjoint) {
     std::vector<int> starts;
     long long acc = 0;
-    const long long per_vox = 4ll * (long long)c->P.nrays * 4 * (adjoint ? 2 : 1);
+    // REV arena + (rho, T) sample scratch (+ REV gradient for the adjoint)
+    const long long per_vox = 4ll * (long long)c->P.nrays * 4 * (adjoint ? 4 : 3);
     for (int b = 0; b < nbeams; b++) {
         long long need = std::max(1ll, tvol_of(specs[b])) * per_vox;
         if (starts.empty() || (acc + need > c->max_batch_bytes && acc > 0)) {
@@ -457,8 +459,10 @@ int pipeline(ee_context* c, const PipeArgs& A) {
         if (!fwd) continue;
         EE_CUDA(grow(c, c->rev, D.rev_total));
         EE_CUDA(cudaMemsetAsync(c->rev.p, 0, sizeof(float) * D.rev_total, s));
+        if (c->P.mode == EE_KERNEL_EXP) EE_CUDA(grow(c, c->samples, D.rev_total));
         EE_CUDA(staged(c, EE_STAGE_CONE, 1, [&] {
-            return ee_launch_cone(c->P, dsp, dge, c->terma.p, c->rev.p, nb, D.max_lines, D.max_line, s);
+            return ee_launch_cone(c->P, dsp, dge, c->terma.p, c->rev.p,
+                                  c->P.mode == EE_KERNEL_EXP ? c->samples.p : nullptr, nb, D.max_lines, D.max_line, s);
         }));
         float* out = A.dose_mode == EE_DOSE_PER_BEAM ? A.d_dose + (long long)b0 * nfull : A.d_dose;
         const int m = A.dose_mode == EE_DOSE_PER_BEAM ? 2 : 1;
@@ -488,14 +492,14 @@ int pipeline(ee_context* c, const PipeArgs& A) {
         const EeBeamGeom* dge = c->d_geoms.p + b0;
         const ChunkDims& D = dims[k];
         EE_CUDA(grow(c, c->rev_grad, D.rev_total + 4));  // +4: vector-reduction padding
-        EE_CUDA(grow(c, c->rev, D.rev_total));             // scratch of the exp-mode adjoint cone
+        if (c->P.mode == EE_KERNEL_EXP) EE_CUDA(grow(c, c->samples, D.rev_total));  // adjoint cone scratch
         EE_CUDA(cudaMemsetAsync(c->rev_grad.p, 0, sizeof(float) * D.rev_total, s));
         EE_CUDA(staged(c, EE_STAGE_GATHER_T, 1, [&] {
             return ee_launch_gather_T(c->P, dsp, dge, dgrad, c->rev_grad.p, nb, D.max_tiles, s);
         }));
         EE_CUDA(staged(c, EE_STAGE_CONE_T, 1, [&] {
-            return ee_launch_cone_T(c->P, dsp, dge, c->rev_grad.p, c->rev.p, c->terma_grad.p, nb, D.max_lines,
-                                    D.max_line, s);
+            return ee_launch_cone_T(c->P, dsp, dge, c->rev_grad.p, c->P.mode == EE_KERNEL_EXP ? c->samples.p : nullptr,
+                                    c->terma_grad.p, nb, D.max_lines, D.max_line, s);
         }));
         EE_CUDA(staged(c, EE_STAGE_TERMA_T, 1, [&] {
             return ee_launch_terma_T(c->P, dsp, dge, c->unit.p, c->bl_idx.p, c->terma_grad.p, A.d_fgrad, nb,
@@ -574,7 +578,7 @@ int ee_destroy(ee_context* c) {
     if (c->dens_array) cudaFreeArray(c->dens_array);
     c->density.release(); c->cumkern.release(); c->expp.release(); c->d_rays.release();
     c->d_specs.release(); c->d_geoms.release(); c->terma.release(); c->unit.release(); c->rev.release();
-    c->rev_grad.release(); c->terma_grad.release(); c->bl_idx.release();
+    c->rev_grad.release(); c->terma_grad.release(); c->bl_idx.release(); c->samples.release();
     c->io_fluence.release(); c->io_dose.release(); c->io_grad.release();
     c->xf.release(); c->xg.release(); c->spread_w.release(); c->acc.release();
     c->h_specs.release(); c->h_geoms.release();

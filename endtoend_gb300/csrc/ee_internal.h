@@ -113,9 +113,11 @@ cudaError_t ee_launch_terma(const EeParams& P, const EeBeamSpec* specs, EeBeamGe
                             cudaStream_t s);
 cudaError_t ee_launch_geometry(const EeParams& P, const EeBeamSpec* specs, EeBeamGeom* geoms, int nbeams,
                                cudaStream_t s);
-// exp mode writes only each line's valid segment: `rev` must be zeroed
+// exp mode writes only each line's valid segment: `rev` must be zeroed;
+// `samples` (REV-arena sized float2, exp mode) keeps (rho, T) per sample
+// between the two passes; nullptr selects the warp kernel
 cudaError_t ee_launch_cone(const EeParams& P, const EeBeamSpec* specs, const EeBeamGeom* geoms, const float* terma,
-                           float* rev, int nbeams, int max_lines, int max_line, cudaStream_t s);
+                           float* rev, float2* samples, int nbeams, int max_lines, int max_line, cudaStream_t s);
 // dose_mode 0/1 accumulate atomically into dose (the caller zeroes it for
 // mode 0); mode 2 writes dose[b] rows (the caller zeroes the volumes).
 cudaError_t ee_launch_gather(const EeParams& P, const EeBeamSpec* specs, const EeBeamGeom* geoms, const float* rev,
@@ -123,10 +125,11 @@ cudaError_t ee_launch_gather(const EeParams& P, const EeBeamSpec* specs, const E
 // adjoint
 cudaError_t ee_launch_gather_T(const EeParams& P, const EeBeamSpec* specs, const EeBeamGeom* geoms,
                                const float* dose_grad, float* rev_grad, int nbeams, int max_tiles, cudaStream_t s);
-// scratch: a buffer of the REV arena's size (exp mode's lane kernel stores
-// one pass's contributions there); nullptr selects the warp kernel
+// scratch: REV-arena sized float2 (exp mode's lane kernel keeps one pass's
+// contributions and the samples' density there); nullptr selects the warp
+// kernel
 cudaError_t ee_launch_cone_T(const EeParams& P, const EeBeamSpec* specs, const EeBeamGeom* geoms, const float* rev_grad,
-                             float* scratch, float* terma_grad, int nbeams, int max_lines, int max_line,
+                             float2* scratch, float* terma_grad, int nbeams, int max_lines, int max_line,
                              cudaStream_t s);
 cudaError_t ee_launch_terma_T(const EeParams& P, const EeBeamSpec* specs, const EeBeamGeom* geoms,
                               const float* unit_terma, const int* beamlet_idx, const float* terma_grad,

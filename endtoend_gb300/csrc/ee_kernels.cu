@@ -772,7 +772,8 @@ constexpr int LANE_BLOCK = 128;
 
 __global__ void __launch_bounds__(LANE_BLOCK) k_cone_lane(EeParams P, const EeBeamSpec* __restrict__ specs,
                                                           const EeBeamGeom* __restrict__ geoms,
-                                                          const float* __restrict__ terma, float* __restrict__ rev) {
+                                                          const float* __restrict__ terma, float* __restrict__ rev,
+                                                          float2* __restrict__ samples) {
     const int ray = blockIdx.y, b = blockIdx.z;
     const EeBeamGeom& G = geoms[b];
     if (G.status != 0) return;
@@ -791,6 +792,8 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_lane(EeParams P, const EeBe
     // consecutive addresses at every i
     const long long nl = R.nlines;
     float* out = rev + G.arena_off + R.offset + line;
+    // (rho, T) of each sample, kept from the forward pass for the reverse one
+    float2* smp = samples + G.arena_off + R.offset + line;
     const EeRayConst& RC = P.rays[ray];
     const float delr = P.lng;
     {   // forward direction: contributions from k < i, kernel row P
@@ -804,6 +807,7 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_lane(EeParams P, const EeBe
             const bool v = r >= 0.f;
             const float h1 = v ? __expf(e1 * r) : 1.f, h2 = v ? __expf(e2 * r) : 1.f;
             if (!v) t = 0.f;
+            smp[i * nl] = make_float2(r, t);
             out[i * nl] = v ? c1 * (Y1 + tm * (1.f - hm1)) + c2 * (Y2 + tm * (1.f - hm2)) : 0.f;
             Y1 = fmaf(h1 * h1, Y1, tm * h1 * (1.f - hm1 * h1));
             Y2 = fmaf(h2 * h2, Y2, tm * h2 * (1.f - hm2 * h2));
@@ -817,8 +821,9 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_lane(EeParams P, const EeBe
         const float inv_nphi = 1.f / (float)P.nphi;
         float Y1 = 0.f, Y2 = 0.f, tm = 0.f, hm1 = 1.f, hm2 = 1.f;
         for (int i = i0 + n - 1; i >= i0; i--) {
-            float t;
-            const float r = sample_rho(P, S, G, F, i, tb, t);
+            const float2 rt = smp[i * nl];
+            const float r = rt.x;
+            float t = rt.y;
             const bool v = r >= 0.f;
             const float h1 = v ? __expf(e1 * r) : 1.f, h2 = v ? __expf(e2 * r) : 1.f;
             if (!v) t = 0.f;
@@ -839,7 +844,7 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_lane(EeParams P, const EeBe
 __global__ void __launch_bounds__(LANE_BLOCK) k_cone_T_lane(EeParams P, const EeBeamSpec* __restrict__ specs,
                                                             const EeBeamGeom* __restrict__ geoms,
                                                             const float* __restrict__ rev_grad,
-                                                            float* __restrict__ scratch, float* __restrict__ terma_grad) {
+                                                            float2* __restrict__ scratch, float* __restrict__ terma_grad) {
     const int ray = blockIdx.y, b = blockIdx.z;
     const EeBeamGeom& G = geoms[b];
     if (G.status != 0) return;
@@ -856,7 +861,7 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_T_lane(EeParams P, const Ee
     const long long nl = R.nlines;  // REV arena layout [i][tZ][tY]
     const long long row = G.arena_off + R.offset + line;
     const float* gin = rev_grad + row;
-    float* sA = scratch + row;
+    float2* sA = scratch + row;  // (pass-A contribution to Tbar[i], rho of sample i)
     const EeRayConst& RC = P.rays[ray];
     const float delr = P.lng, inv_nphi = 1.f / (float)P.nphi;
     const int i1 = i0 + n - 1;
@@ -869,16 +874,17 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_T_lane(EeParams P, const Ee
         bool v = r >= 0.f;
         float h1 = v ? __expf(e1 * r) : 1.f, h2 = v ? __expf(e2 * r) : 1.f;
         float Z1 = 0.f, Z2 = 0.f;
-        sA[i1 * nl] = 0.f;
+        sA[i1 * nl] = make_float2(0.f, r);
         for (int i = i1; i >= i0; i--) {
             const float gi = v ? gin[i * nl] * inv_nphi : 0.f;
             if (i > i0) {
                 const float rm = sample_rho(P, S, G, F, i - 1, nullptr, dummy);
                 const bool vm = rm >= 0.f;
                 const float hm1 = vm ? __expf(e1 * rm) : 1.f, hm2 = vm ? __expf(e2 * rm) : 1.f;
-                sA[(i - 1) * nl] = vm ? c1 * gi * (1.f - hm1) + Z1 * h1 * (1.f - hm1 * h1) + c2 * gi * (1.f - hm2) +
-                                            Z2 * h2 * (1.f - hm2 * h2)
-                                      : 0.f;
+                sA[(i - 1) * nl] = make_float2(vm ? c1 * gi * (1.f - hm1) + Z1 * h1 * (1.f - hm1 * h1) +
+                                                        c2 * gi * (1.f - hm2) + Z2 * h2 * (1.f - hm2 * h2)
+                                                  : 0.f,
+                                               rm);
                 Z1 = fmaf(h1 * h1, Z1, c1 * gi);
                 Z2 = fmaf(h2 * h2, Z2, c2 * gi);
                 v = vm; h1 = hm1; h2 = hm2;
@@ -890,20 +896,22 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_T_lane(EeParams P, const Ee
         const float c1 = prm[0] / prm[1], c2 = prm[2] / prm[3];
         const float e1 = -0.5f * prm[1] * delr, e2 = -0.5f * prm[3] * delr;
         float* tg = terma_grad + S.t_off;
-        float r = sample_rho(P, S, G, F, i0, nullptr, dummy);
+        float2 a = sA[i0 * nl];
+        float r = a.y;
         bool v = r >= 0.f;
         float h1 = v ? __expf(e1 * r) : 1.f, h2 = v ? __expf(e2 * r) : 1.f;
         float Z1 = 0.f, Z2 = 0.f, cprev = 0.f;
         for (int i = i0; i <= i1; i++) {
             const float gi = v ? gin[i * nl] * inv_nphi : 0.f;
-            const float tot = sA[i * nl] + cprev;
+            const float tot = a.x + cprev;
             if (v && tot != 0.f) {
                 f3 gp = F.gl + F.gx * (float)i;
                 tri_border_scatter(tg, S.tn[0], S.tn[1], S.tn[2], gp.x - (float)S.t0[0], gp.y - (float)S.t0[1],
                                    gp.z - (float)S.t0[2], tot);
             }
             if (i < i1) {
-                const float rm = sample_rho(P, S, G, F, i + 1, nullptr, dummy);
+                a = sA[(i + 1) * nl];
+                const float rm = a.y;
                 const bool vm = rm >= 0.f;
                 const float hm1 = vm ? __expf(e1 * rm) : 1.f, hm2 = vm ? __expf(e2 * rm) : 1.f;
                 cprev = vm ? c1 * gi * (1.f - hm1) + Z1 * h1 * (1.f - hm1 * h1) + c2 * gi * (1.f - hm2) +
@@ -1244,10 +1252,10 @@ static cudaError_t cone_attr(const void* fn, size_t smem) {
 }
 
 cudaError_t ee_launch_cone(const EeParams& P, const EeBeamSpec* specs, const EeBeamGeom* geoms, const float* terma,
-                           float* rev, int nbeams, int max_lines, int max_line, cudaStream_t s) {
-    if (P.mode == 1) {  // exp kernel: one lane per line; the caller zeroed `rev`
+                           float* rev, float2* samples, int nbeams, int max_lines, int max_line, cudaStream_t s) {
+    if (P.mode == 1 && samples) {  // exp kernel: one lane per line; the caller zeroed `rev`
         dim3 grid(grid1(max_lines, LANE_BLOCK), P.nrays, nbeams);
-        k_cone_lane<<<grid, LANE_BLOCK, 0, s>>>(P, specs, geoms, terma, rev);
+        k_cone_lane<<<grid, LANE_BLOCK, 0, s>>>(P, specs, geoms, terma, rev, samples);
         return cudaGetLastError();
     }
     size_t smem = cone_smem(max_line);
@@ -1277,7 +1285,7 @@ cudaError_t ee_launch_gather_T(const EeParams& P, const EeBeamSpec* specs, const
 }
 
 cudaError_t ee_launch_cone_T(const EeParams& P, const EeBeamSpec* specs, const EeBeamGeom* geoms, const float* rev_grad,
-                             float* scratch, float* terma_grad, int nbeams, int max_lines, int max_line,
+                             float2* scratch, float* terma_grad, int nbeams, int max_lines, int max_line,
                              cudaStream_t s) {
     if (P.mode == 1 && scratch) {
         dim3 grid(grid1(max_lines, LANE_BLOCK), P.nrays, nbeams);

@@ -137,7 +137,10 @@ extern "C" int ee_beam_dose_noalloc(ee_context* ctx, const ee_beam* beam, const 
     const long long nfull = (long long)P.size[0] * P.size[1] * P.size[2];
     if ((e = cudaMemsetAsync(d_dose, 0, sizeof(float) * nfull, s)) != cudaSuccess) return cuda_fail(e, "dose clear");
     if ((e = cudaMemsetAsync(d_rev, 0, sizeof(float) * G.rev_total, s)) != cudaSuccess) return cuda_fail(e, "REV clear");
-    if ((e = ee_launch_cone(P, d_spec, d_geom, d_terma, d_rev, 1, G.max_lines, G.max_line, s)) != cudaSuccess)
+    // no (rho, T) sample scratch here: the warp-per-line cone kernel keeps a
+    // line's samples in shared memory instead
+    float2* d_smp = nullptr;
+    if ((e = ee_launch_cone(P, d_spec, d_geom, d_terma, d_rev, d_smp, 1, G.max_lines, G.max_line, s)) != cudaSuccess)
         return cuda_fail(e, "k_cone");
     if ((e = ee_launch_gather(P, d_spec, d_geom, d_rev, d_dose, 1, 1, G.rows > 0 ? G.rows : 1, s)) != cudaSuccess)
         return cuda_fail(e, "k_gather");
