@@ -207,9 +207,18 @@ def main():
     def step_device():
         eng.dose_and_adjoint_device(beams, d_fl.data_ptr(), d_dose.data_ptr(), d_grad.data_ptr(), d_fgrad.data_ptr())
 
+    # planned batch: the whole forward + adjoint captured into one CUDA graph
+    plan = eng.plan(beams, d_fl.data_ptr(), d_dose.data_ptr(), d_grad.data_ptr(), d_fgrad.data_ptr())
+    plan_info = plan.info()
+
+    def step_plan():
+        plan.launch()
+
     for _ in range(args.warmup):
         step_device()
+        step_plan()
     eng.synchronize()
+    plan.status()
     # one profiled step (untimed): per-stage device time + launches
     eng.set_profiling(True)
     eng.read_profile()
@@ -219,26 +228,34 @@ def main():
     eng.set_profiling(False)
     infos = [eng.beam_info(i) for i in range(len(beams))]
 
+    def timed(fn):
+        ms = []
+        for _ in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(1.0)
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            b.synchronize()
+            ms.append(a.elapsed_time(b))
+        return ms
+
     clocks = ClockSampler(local)
     barrier(ws)
     torch.cuda.synchronize()
     clocks.start()
-    step_ms = []
-    for _ in range(args.steps):
-        with torch.cuda.stream(stream):
-            flush.fill_(1.0)
-        a = torch.cuda.Event(enable_timing=True)
-        b = torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        step_device()
-        b.record(stream)
-        b.synchronize()
-        step_ms.append(a.elapsed_time(b))
+    step_ms = timed(step_plan)
     torch.cuda.synchronize()
     barrier(ws)
     clk = clocks.stop()
+    plan.status()
     t_dev = max_over_ranks(sum(step_ms) / 1e3, ws)
     value = ws * len(beams) * args.steps / t_dev
+    # the same batch through the direct pipeline call (one geometry read-back per chunk)
+    pipe_ms = timed(step_device)
+    pipeline_value = len(beams) * args.steps / (sum(pipe_ms) / 1e3)
 
     # e2e through host pointers (pinned host memory)
     pin_fl = torch.from_numpy(fl_host).pin_memory().numpy()
@@ -306,7 +323,9 @@ def main():
             "peak_source": "measured" if peaks else "fallback",
             "stage_ms": {k: round(v[0], 3) for k, v in prof.items()},
             "chain_frac": (2 * alg_bytes / (sum(step_ms) / len(step_ms) / 1e3) / 1e9) / peak}
-    gpu_launches = int(sum(v[1] for v in prof.values())) * args.steps
+    # kernels per graph replay: per chunk geom_init, terma, geometry, cone, gather,
+    # gather_T, cone_T, terma_T
+    gpu_launches = int(plan_info["chunks"]) * 8 * args.steps
 
     # accuracy vs the reference discretisation on one beam (FP64 oracle,
     # 24-radius table, texture 8-bit weights)
@@ -345,12 +364,16 @@ def main():
             "config": {"workload": "batched candidate beams: 200x200x160 @2mm head-neck phantom, "
                                    f"{len(beams)} beams/GPU, 48 cones (8x6), fluence 8^2-40^2 @2.5mm; "
                                    "step = forward + adjoint of every beam",
-                       "kernel": "double exponential, O(L) warp-scan", "parallelism": f"beams sharded x{ws}",
+                       "kernel": "double exponential, O(L) recurrence, one lane per cone line",
+                       "path": "planned batch replayed from one captured CUDA graph",
+                       "parallelism": f"beams sharded x{ws}",
                        "l2": "flushed (256 MB write) between timed steps"},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
             "plain": {"value": plain, "unit": UNIT, "beams": npl, "p50_ms": float(np.percentile(lat_ms, 50)),
                       "p99_ms": float(np.percentile(lat_ms, 99))},
             "batched_over_plain": value / plain,
+            "pipeline": {"value": pipeline_value, "unit": UNIT, "note": "same batch, direct call (host geometry read-back per chunk)"},
+            "plan": plan_info,
             "gpu_launches": gpu_launches,
             "roofline": roof,
             "clocks": clk,
@@ -358,6 +381,7 @@ def main():
             "cpu_baseline": cpu,
         }
         print(json.dumps(line), flush=True)
+    plan.close()
     eng.close()
 
 

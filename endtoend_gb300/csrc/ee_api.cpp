@@ -14,6 +14,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -434,7 +435,7 @@ int pipeline(ee_context* c, const PipeArgs& A) {
         EeBeamGeom* dge = c->d_geoms.p + b0;
         ChunkDims& D = dims[k];
         for (int b = b0; b < b0 + nb; b++) D.max_tvol = std::max(D.max_tvol, tvol_of(c->h_specs.p[b]));
-        EE_CUDA(staged(c, EE_STAGE_GEOMETRY, 1, [&] { return ee_launch_geom_init(dge, nb, s); }));
+        EE_CUDA(staged(c, EE_STAGE_GEOMETRY, 1, [&] { return ee_launch_geom_init(dsp, dge, nb, s); }));
         EE_CUDA(staged(c, EE_STAGE_TERMA, 1, [&] {
             return ee_launch_terma(c->P, dsp, dge, A.d_fluence, c->terma.p, adj ? c->unit.p : nullptr,
                                    adj ? c->bl_idx.p : nullptr, nb, D.max_tvol, s);
@@ -543,7 +544,178 @@ long long total_fluence(const ee_beam* beams, int nbeams) {
     return n;
 }
 
+// ====================================================== planned batches ==
+// An ee_plan fixes one batch of beams and sizes every device buffer from
+// geometric upper bounds, so the whole chain (TERMA, crop boxes, REV frames,
+// cones, gather and optionally the adjoint) runs without a host read-back and
+// is captured once into a CUDA graph; replaying the graph re-evaluates the
+// batch for new fluence / dose-gradient values in the same device buffers.
+//
+// Bounds: a beam's TERMA-non-zero voxels lie in its field frustum, so their
+// BEV indices lie in the BEV AABB of the frustum's 8 vertices; the crop box
+// (that AABB, its maximum floored at 0 as the reference's FLT_MIN start does,
+// widened by the penumbra) bounds every REV array (findREV is monotone in the
+// box size) and the patient rows/tiles the gather kernels visit.
+struct PlanBound {
+    long long rev = 0;
+    int max_line = 1, max_lines = 1, rows = 1, tiles = 1;
+};
+
+PlanBound plan_bound(const ee_context* c, const EeBeamSpec& S) {
+    const EeParams& P = c->P;
+    PlanBound B;
+    // frustum vertices in patient index space (as terma_box)
+    const double dir[3] = {S.dird[0], S.dird[1], S.dird[2]};
+    double dmin = 1e300, dmax = -1e300;
+    for (int k = 0; k < 8; k++) {
+        double d = 0;
+        for (int a = 0; a < 3; a++) {
+            int idx = ((k >> a) & 1) ? P.bb0[a] + P.bbs[a] - 1 : P.bb0[a];
+            d += (P.start[a] + (double)idx * P.voxel[a] - S.srcd[a]) * dir[a];
+        }
+        dmin = std::min(dmin, d);
+        dmax = std::max(dmax, d);
+    }
+    dmin = std::max(dmin, 1e-6);
+    const double hu = 0.5 * S.fmap[0] * S.beamlet[0], hw = 0.5 * S.fmap[1] * S.beamlet[1];
+    double blo[3] = {1e300, 1e300, 1e300}, bhi[3] = {-1e300, -1e300, -1e300};
+    for (int k = 0; k < 8; k++) {
+        double u = (k & 1) ? hu : -hu, w = (k & 2) ? hw : -hw, d = (k & 4) ? dmax : dmin;
+        double rel[3];
+        for (int a = 0; a < 3; a++) {
+            double q = S.srcd[a] + dir[a] * S.isodistd + S.MBi[3 * a] * u + S.MBi[3 * a + 2] * w;
+            double pos = S.srcd[a] + (q - S.srcd[a]) * (d / S.isodistd);
+            rel[a] = (pos - P.start[a]) / P.voxel[a] - P.bb0[a];
+        }
+        for (int a = 0; a < 3; a++) {
+            double b = S.MBd[3 * a] * rel[0] + S.MBd[3 * a + 1] * rel[1] + S.MBd[3 * a + 2] * rel[2];
+            blo[a] = std::min(blo[a], b);
+            bhi[a] = std::max(bhi[a], b);
+        }
+    }
+    const double pen[3] = {P.penumbra / P.lat, P.penumbra / P.lng, P.penumbra / P.lat};
+    double bmn[3], bev[3];
+    for (int a = 0; a < 3; a++) {
+        bmn[a] = blo[a] - pen[a] - 1.0;
+        double bmx = std::max(bhi[a], 0.0) + pen[a] + 1.0;
+        bev[a] = std::ceil(bmx - bmn[a]) + 1.0;
+    }
+    const double bd[3] = {bev[0] * P.lat, bev[1] * P.lng, bev[2] * P.lat};
+    for (int r = 0; r < P.nrays; r++) {
+        const float* M = c->rays[r].MK;
+        double mn[3] = {1e300, 1e300, 1e300}, mx[3] = {-1e300, -1e300, -1e300};
+        for (int k = 0; k < 8; k++) {
+            double v[3] = {bd[0] * (k & 1), bd[1] * ((k >> 1) & 1), bd[2] * ((k >> 2) & 1)};
+            for (int a = 0; a < 3; a++) {
+                double o = M[3 * a] * v[0] + M[3 * a + 1] * v[1] + M[3 * a + 2] * v[2];
+                mn[a] = std::min(mn[a], o);
+                mx[a] = std::max(mx[a], o);
+            }
+        }
+        long long s0 = (long long)std::ceil((mx[1] - mn[1]) / P.lng) + 2;
+        long long s1 = (long long)std::ceil((mx[2] - mn[2]) / P.lat) + 2;
+        long long s2 = (long long)std::ceil((mx[0] - mn[0]) / P.lat) + 2;
+        B.rev += s0 * s1 * s2;
+        B.max_line = (int)std::max<long long>(B.max_line, std::min<long long>(s0, EE_MAX_LINE));
+        B.max_lines = (int)std::max<long long>(B.max_lines, s1 * s2);
+    }
+    // patient AABB of the dilated bound box: t = MBi (b + bmn) + bb0
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int k = 0; k < 8; k++) {
+        double b[3] = {((k & 1) ? bev[0] + 2.0 : -2.0) + bmn[0], (((k >> 1) & 1) ? bev[1] + 2.0 : -2.0) + bmn[1],
+                       (((k >> 2) & 1) ? bev[2] + 2.0 : -2.0) + bmn[2]};
+        for (int a = 0; a < 3; a++) {
+            double t = S.MBi[3 * a] * b[0] + S.MBi[3 * a + 1] * b[1] + S.MBi[3 * a + 2] * b[2] + P.bb0[a];
+            lo[a] = std::min(lo[a], t);
+            hi[a] = std::max(hi[a], t);
+        }
+    }
+    long long n[3];
+    for (int a = 0; a < 3; a++) {
+        long long l = std::max<long long>(P.bb0[a], (long long)std::floor(lo[a]) - 2);
+        long long h = std::min<long long>(P.bb0[a] + P.bbs[a] - 1, (long long)std::ceil(hi[a]) + 2);
+        n[a] = std::max<long long>(1, h - l + 1);
+    }
+    B.rows = (int)(n[1] * n[2]);
+    B.tiles = (int)(((n[0] + 7) / 8) * ((n[1] + 7) / 8) * ((n[2] + 3) / 4));
+    return B;
+}
+
 }  // namespace
+
+struct ee_plan {
+    ee_context* c = nullptr;
+    int nbeams = 0;
+    bool adjoint = false;
+    std::vector<ee_beam> beams;
+    std::vector<EeBeamSpec> specs;
+    std::vector<int> starts;
+    std::vector<ChunkDims> dims;
+    long long tvol_total = 0, rev_max = 0, nfl = 0;
+    DevBuf<EeBeamSpec> d_specs;
+    DevBuf<EeBeamGeom> d_geoms;
+    DevBuf<float> terma, unit, terma_grad, rev, rev_grad;
+    DevBuf<int> bl_idx;
+    DevBuf<float2> samples;
+    const float* d_fluence = nullptr;
+    float* d_dose = nullptr;
+    const float* d_grad = nullptr;
+    float* d_fgrad = nullptr;
+    int lane_block = 128;
+    std::vector<int> status;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+namespace {
+
+// Every memset and launch of one plan evaluation, on stream s.
+cudaError_t plan_enqueue(ee_plan* pl, cudaStream_t s) {
+    ee_context* c = pl->c;
+    const EeParams& P = c->P;
+    const long long nfull = nfull_of(c);
+    cudaError_t e;
+#define PL(x)                              \
+    do {                                   \
+        if ((e = (x)) != cudaSuccess) return e; \
+    } while (0)
+    PL(cudaMemsetAsync(pl->d_dose, 0, sizeof(float) * nfull, s));
+    const int nchunks = (int)pl->starts.size() - 1;
+    for (int k = 0; k < nchunks; k++) {
+        const int b0 = pl->starts[k], nb = pl->starts[k + 1] - b0;
+        const EeBeamSpec* dsp = pl->d_specs.p + b0;
+        EeBeamGeom* dge = pl->d_geoms.p + b0;
+        const ChunkDims& D = pl->dims[k];
+        PL(ee_launch_geom_init(dsp, dge, nb, s));
+        PL(ee_launch_terma(P, dsp, dge, pl->d_fluence, pl->terma.p, pl->adjoint ? pl->unit.p : nullptr,
+                           pl->adjoint ? pl->bl_idx.p : nullptr, nb, D.max_tvol, s));
+        PL(ee_launch_geometry(P, dsp, dge, nb, s));
+        PL(cudaMemsetAsync(pl->rev.p, 0, sizeof(float) * D.rev_total, s));
+        PL(ee_launch_cone(P, dsp, dge, pl->terma.p, pl->rev.p, P.mode == EE_KERNEL_EXP ? pl->samples.p : nullptr, nb,
+                          D.max_lines, D.max_line, s, pl->lane_block));
+        PL(ee_launch_gather(P, dsp, dge, pl->rev.p, pl->d_dose, nb, 1, D.max_rows, s));
+    }
+    if (!pl->adjoint) return cudaSuccess;
+    PL(cudaMemsetAsync(pl->d_fgrad, 0, sizeof(float) * pl->nfl, s));
+    PL(cudaMemsetAsync(pl->terma_grad.p, 0, sizeof(float) * pl->tvol_total, s));
+    for (int k = 0; k < nchunks; k++) {
+        const int b0 = pl->starts[k], nb = pl->starts[k + 1] - b0;
+        const EeBeamSpec* dsp = pl->d_specs.p + b0;
+        const EeBeamGeom* dge = pl->d_geoms.p + b0;
+        const ChunkDims& D = pl->dims[k];
+        PL(cudaMemsetAsync(pl->rev_grad.p, 0, sizeof(float) * D.rev_total, s));
+        PL(ee_launch_gather_T(P, dsp, dge, pl->d_grad, pl->rev_grad.p, nb, D.max_tiles, s));
+        PL(ee_launch_cone_T(P, dsp, dge, pl->rev_grad.p, P.mode == EE_KERNEL_EXP ? pl->samples.p : nullptr,
+                            pl->terma_grad.p, nb, D.max_lines, D.max_line, s, pl->lane_block));
+        PL(ee_launch_terma_T(P, dsp, dge, pl->unit.p, pl->bl_idx.p, pl->terma_grad.p, pl->d_fgrad, nb, D.max_tvol, s));
+    }
+#undef PL
+    return cudaSuccess;
+}
+
+}  // namespace
+
+
 
 // ======================================================================= ABI
 extern "C" {
@@ -882,6 +1054,149 @@ int ee_loss_and_grad(ee_context* c, const ee_beam* beams, int nbeams, const floa
     EE_CUDA(cudaMemcpyAsync(h, c->acc.p, sizeof(h), cudaMemcpyDeviceToHost, s));
     EE_CUDA(cudaStreamSynchronize(s));
     if (loss_out) for (int k = 0; k < 3; k++) loss_out[k] = h[k];
+    return EE_OK;
+}
+
+int ee_plan_create(ee_context* c, const ee_beam* beams, int nbeams, const float* d_fluence, float* d_dose,
+                   const float* d_dose_grad, float* d_fluence_grad, ee_plan** out) {
+    if (!c || !out) return fail(EE_ERR_INVALID_ARG, "null argument");
+    *out = nullptr;
+    int st = check_ready(c);
+    if (st) return st;
+    if ((st = check_beams(beams, nbeams))) return st;
+    if (!d_fluence || !d_dose) return fail(EE_ERR_INVALID_ARG, "null fluence/dose pointer");
+    if ((d_dose_grad == nullptr) != (d_fluence_grad == nullptr))
+        return fail(EE_ERR_INVALID_ARG, "adjoint needs both gradient pointers");
+    std::lock_guard<std::mutex> lk(c->mu);
+    EE_CUDA(cudaSetDevice(c->device));
+    cudaStream_t s = c->stream;
+    std::unique_ptr<ee_plan> pl(new ee_plan());
+    pl->c = c;
+    pl->nbeams = nbeams;
+    pl->adjoint = d_fluence_grad != nullptr;
+    pl->beams.assign(beams, beams + nbeams);
+    pl->specs.resize(nbeams);
+    pl->d_fluence = d_fluence; pl->d_dose = d_dose; pl->d_grad = d_dose_grad; pl->d_fgrad = d_fluence_grad;
+    build_specs(c->P, beams, nbeams, pl->specs.data());
+    const bool expm = c->P.mode == EE_KERNEL_EXP;
+    const long long per_float = 4ll * (1 + (expm ? 2 : 0) + (pl->adjoint ? 1 : 0));
+    long long acc = 0;
+    for (int b = 0; b < nbeams; b++) {
+        EeBeamSpec& S = pl->specs[b];
+        PlanBound B = plan_bound(c, S);
+        long long need = B.rev * per_float;
+        if (pl->starts.empty() || (acc + need > c->max_batch_bytes && acc > 0)) {
+            pl->starts.push_back(b);
+            pl->dims.push_back(ChunkDims());
+            acc = 0;
+        }
+        ChunkDims& D = pl->dims.back();
+        S.plan_off = D.rev_total;
+        S.plan_cap = B.rev;
+        S.t_off = pl->tvol_total;
+        D.rev_total += B.rev;
+        D.max_tvol = std::max(D.max_tvol, tvol_of(S));
+        D.max_line = std::max(D.max_line, B.max_line);
+        D.max_lines = std::max(D.max_lines, B.max_lines);
+        D.max_rows = std::max(D.max_rows, B.rows);
+        D.max_tiles = std::max(D.max_tiles, B.tiles);
+        pl->tvol_total += tvol_of(S);
+        pl->rev_max = std::max(pl->rev_max, D.rev_total);
+        acc += need;
+    }
+    pl->starts.push_back(nbeams);
+    pl->nfl = total_fluence(beams, nbeams);
+    EE_CUDA(pl->d_specs.ensure(nbeams));
+    EE_CUDA(pl->d_geoms.ensure(nbeams));
+    EE_CUDA(pl->terma.ensure(pl->tvol_total));
+    EE_CUDA(pl->rev.ensure(pl->rev_max));
+    if (expm) EE_CUDA(pl->samples.ensure(pl->rev_max));
+    if (pl->adjoint) {
+        EE_CUDA(pl->unit.ensure(pl->tvol_total));
+        EE_CUDA(pl->bl_idx.ensure(pl->tvol_total));
+        EE_CUDA(pl->terma_grad.ensure(pl->tvol_total + 4));
+        EE_CUDA(pl->rev_grad.ensure(pl->rev_max + 4));
+    }
+    EE_CUDA(cudaMemcpyAsync(pl->d_specs.p, pl->specs.data(), sizeof(EeBeamSpec) * nbeams, cudaMemcpyHostToDevice, s));
+    pl->status.resize(nbeams);
+    // eager run: validates the bounds and sets kernel attributes before capture
+    EE_CUDA(plan_enqueue(pl.get(), s));
+    EE_CUDA(ee_copy_status(pl->d_geoms.p, pl->status.data(), nbeams, s));
+    EE_CUDA(cudaStreamSynchronize(s));
+    for (int b = 0; b < nbeams; b++)
+        if (pl->status[b] != 0) return fail(pl->status[b], "beam %d: %s", b, status_text(pl->status[b]));
+    // autotune the lane kernels' block size on this batch
+    if (expm) {
+        cudaEvent_t e0 = take_event(c), e1 = take_event(c);
+        float best = 1e30f;
+        int best_lb = 128;
+        for (int lb : {64, 128, 256}) {
+            pl->lane_block = lb;
+            cudaEventRecord(e0, s);
+            EE_CUDA(plan_enqueue(pl.get(), s));
+            cudaEventRecord(e1, s);
+            EE_CUDA(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (ms < best) { best = ms; best_lb = lb; }
+        }
+        pl->lane_block = best_lb;
+        c->event_pool.push_back(e0);
+        c->event_pool.push_back(e1);
+    }
+    EE_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
+    cudaError_t ce = plan_enqueue(pl.get(), s);
+    cudaGraph_t g = nullptr;
+    cudaError_t ee = cudaStreamEndCapture(s, &g);
+    if (ce != cudaSuccess) { if (g) cudaGraphDestroy(g); return fail(EE_ERR_CUDA, "plan capture: %s", cudaGetErrorString(ce)); }
+    if (ee != cudaSuccess) return fail(EE_ERR_CUDA, "plan capture: %s", cudaGetErrorString(ee));
+    pl->graph = g;
+    EE_CUDA(cudaGraphInstantiate(&pl->exec, g, 0));
+    *out = pl.release();
+    return EE_OK;
+}
+
+int ee_plan_launch(ee_plan* pl) {
+    if (!pl) return fail(EE_ERR_INVALID_ARG, "null plan");
+    EE_CUDA(cudaSetDevice(pl->c->device));
+    EE_CUDA(cudaGraphLaunch(pl->exec, pl->c->stream));
+    return EE_OK;
+}
+
+int ee_plan_status(ee_plan* pl, int* nfailed) {
+    if (!pl) return fail(EE_ERR_INVALID_ARG, "null plan");
+    EE_CUDA(cudaSetDevice(pl->c->device));
+    EE_CUDA(ee_copy_status(pl->d_geoms.p, pl->status.data(), pl->nbeams, pl->c->stream));
+    EE_CUDA(cudaStreamSynchronize(pl->c->stream));
+    int n = 0, first = -1;
+    for (int b = 0; b < pl->nbeams; b++)
+        if (pl->status[b] != 0) { n++; if (first < 0) first = b; }
+    if (nfailed) *nfailed = n;
+    if (n) return fail(pl->status[first], "beam %d: %s", first, status_text(pl->status[first]));
+    return EE_OK;
+}
+
+int ee_plan_info(ee_plan* pl, int* lane_block, long long* device_bytes, int* nchunks) {
+    if (!pl) return fail(EE_ERR_INVALID_ARG, "null plan");
+    if (lane_block) *lane_block = pl->lane_block;
+    if (nchunks) *nchunks = (int)pl->starts.size() - 1;
+    if (device_bytes) {
+        long long b = 4ll * (pl->tvol_total + pl->rev_max) + 8ll * pl->samples.n;
+        if (pl->adjoint) b += 4ll * (3 * pl->tvol_total + pl->rev_max);
+        *device_bytes = b;
+    }
+    return EE_OK;
+}
+
+int ee_plan_destroy(ee_plan* pl) {
+    if (!pl) return EE_OK;
+    cudaSetDevice(pl->c->device);
+    cudaStreamSynchronize(pl->c->stream);
+    if (pl->exec) cudaGraphExecDestroy(pl->exec);
+    if (pl->graph) cudaGraphDestroy(pl->graph);
+    pl->d_specs.release(); pl->d_geoms.release(); pl->terma.release(); pl->unit.release();
+    pl->terma_grad.release(); pl->rev.release(); pl->rev_grad.release(); pl->bl_idx.release(); pl->samples.release();
+    delete pl;
     return EE_OK;
 }
 

@@ -66,6 +66,10 @@ struct EeBeamSpec {
     double dird[3];
     double MBd[9];
     double isodistd;
+    // REV arena slot planned from geometric upper bounds (ee_plan);
+    // plan_cap == 0: the arena is sized after the geometry read-back
+    long long plan_off;
+    long long plan_cap;
 };
 
 // Per-cone geometry of one beam, computed on the device.
@@ -105,7 +109,7 @@ struct EeBeamGeom {
 };
 
 // Launch wrappers implemented in ee_kernels.cu.  All enqueue on `s`.
-cudaError_t ee_launch_geom_init(EeBeamGeom* g, int nbeams, cudaStream_t s);
+cudaError_t ee_launch_geom_init(const EeBeamSpec* specs, EeBeamGeom* g, int nbeams, cudaStream_t s);
 // unit/beamlet_idx (both optional) receive TERMA per unit fluence of every
 // in-field voxel and its beamlet index (adjoint).
 cudaError_t ee_launch_terma(const EeParams& P, const EeBeamSpec* specs, EeBeamGeom* geoms, const float* fluence,
@@ -117,7 +121,8 @@ cudaError_t ee_launch_geometry(const EeParams& P, const EeBeamSpec* specs, EeBea
 // `samples` (REV-arena sized float2, exp mode) keeps (rho, T) per sample
 // between the two passes; nullptr selects the warp kernel
 cudaError_t ee_launch_cone(const EeParams& P, const EeBeamSpec* specs, const EeBeamGeom* geoms, const float* terma,
-                           float* rev, float2* samples, int nbeams, int max_lines, int max_line, cudaStream_t s);
+                           float* rev, float2* samples, int nbeams, int max_lines, int max_line, cudaStream_t s,
+                           int lane_block = 128);
 // dose_mode 0/1 accumulate atomically into dose (the caller zeroes it for
 // mode 0); mode 2 writes dose[b] rows (the caller zeroes the volumes).
 cudaError_t ee_launch_gather(const EeParams& P, const EeBeamSpec* specs, const EeBeamGeom* geoms, const float* rev,
@@ -130,7 +135,9 @@ cudaError_t ee_launch_gather_T(const EeParams& P, const EeBeamSpec* specs, const
 // kernel
 cudaError_t ee_launch_cone_T(const EeParams& P, const EeBeamSpec* specs, const EeBeamGeom* geoms, const float* rev_grad,
                              float2* scratch, float* terma_grad, int nbeams, int max_lines, int max_line,
-                             cudaStream_t s);
+                             cudaStream_t s, int lane_block = 128);
+// per-beam status words of a geometry array (strided copy), for plans
+cudaError_t ee_copy_status(const EeBeamGeom* geoms, int* status_host, int nbeams, cudaStream_t s);
 cudaError_t ee_launch_terma_T(const EeParams& P, const EeBeamSpec* specs, const EeBeamGeom* geoms,
                               const float* unit_terma, const int* beamlet_idx, const float* terma_grad,
                               float* fluence_grad, int nbeams, long long max_tvol, cudaStream_t s);

@@ -20,6 +20,7 @@
 #include "ee_internal.h"
 #include <algorithm>
 #include <cfloat>
+#include <cstddef>
 
 namespace {
 
@@ -321,14 +322,15 @@ __global__ void __launch_bounds__(256) k_terma(EeParams P, const EeBeamSpec* __r
     }
 }
 
-__global__ void k_geom_init(EeBeamGeom* g, int n) {
+__global__ void k_geom_init(const EeBeamSpec* __restrict__ specs, EeBeamGeom* g, int n) {
     int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= n) return;
     for (int a = 0; a < 3; a++) { g[b].key_min[a] = f2key(FLT_MAX); g[b].key_max[a] = f2key(FLT_MIN); }
     g[b].nnz = 0;
     g[b].status = 0;
-    g[b].arena_off = 0;
-    g[b].arena_cap = 0;  // unbounded: the host sizes the arena after read-back
+    // planned slot, or unbounded (the host sizes the arena after read-back)
+    g[b].arena_off = specs[b].plan_off;
+    g[b].arena_cap = specs[b].plan_cap;
 }
 
 // ------------------------------------------------------------- geometry --
@@ -768,8 +770,7 @@ __device__ __forceinline__ float sample_rho(const EeParams& P, const EeBeamSpec&
     return tex3D<float>(P.dens_tex, g.x + 0.5f, g.y + 0.5f, g.z + 0.5f);
 }
 
-constexpr int LANE_BLOCK = 128;
-
+template <int LANE_BLOCK>
 __global__ void __launch_bounds__(LANE_BLOCK) k_cone_lane(EeParams P, const EeBeamSpec* __restrict__ specs,
                                                           const EeBeamGeom* __restrict__ geoms,
                                                           const float* __restrict__ terma, float* __restrict__ rev,
@@ -841,6 +842,7 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_lane(EeParams P, const EeBe
 // stores its contribution to Tbar[i-1] in `scratch` (the REV-arena layout);
 // pass B (ascending i) runs the transpose of the reverse recurrence, adds its
 // contribution to Tbar[i] and scatters Tbar[i] into the TERMA-box gradient.
+template <int LANE_BLOCK>
 __global__ void __launch_bounds__(LANE_BLOCK) k_cone_T_lane(EeParams P, const EeBeamSpec* __restrict__ specs,
                                                             const EeBeamGeom* __restrict__ geoms,
                                                             const float* __restrict__ rev_grad,
@@ -1225,9 +1227,14 @@ __global__ void __launch_bounds__(256) k_terma_T(EeParams P, const EeBeamSpec* _
 // ----------------------------------------------------------- launchers ---
 static inline unsigned grid1(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
-cudaError_t ee_launch_geom_init(EeBeamGeom* g, int nbeams, cudaStream_t s) {
-    k_geom_init<<<grid1(nbeams, 128), 128, 0, s>>>(g, nbeams);
+cudaError_t ee_launch_geom_init(const EeBeamSpec* specs, EeBeamGeom* g, int nbeams, cudaStream_t s) {
+    k_geom_init<<<grid1(nbeams, 128), 128, 0, s>>>(specs, g, nbeams);
     return cudaGetLastError();
+}
+
+cudaError_t ee_copy_status(const EeBeamGeom* geoms, int* status_host, int nbeams, cudaStream_t s) {
+    return cudaMemcpy2DAsync(status_host, sizeof(int), (const char*)geoms + offsetof(EeBeamGeom, status),
+                             sizeof(EeBeamGeom), sizeof(int), nbeams, cudaMemcpyDeviceToHost, s);
 }
 
 cudaError_t ee_launch_terma(const EeParams& P, const EeBeamSpec* specs, EeBeamGeom* geoms, const float* fluence,
@@ -1246,16 +1253,31 @@ cudaError_t ee_launch_geometry(const EeParams& P, const EeBeamSpec* specs, EeBea
 
 static size_t cone_smem(int maxL) { return sizeof(float) * ((size_t)CONE_WARPS * 3 * maxL + 2 * EE_MAX_RADII + EE_MAX_RADII); }
 
+// Raise a kernel's dynamic shared-memory limit once per size class (set
+// before any graph capture by the first eager launch).
 static cudaError_t cone_attr(const void* fn, size_t smem) {
-    if (smem > 48 * 1024) return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    return cudaSuccess;
+    if (smem <= 48 * 1024) return cudaSuccess;
+    static const void* done_fn[4] = {nullptr, nullptr, nullptr, nullptr};
+    static size_t done_sz[4] = {0, 0, 0, 0};
+    for (int k = 0; k < 4; k++)
+        if (done_fn[k] == fn && done_sz[k] >= smem) return cudaSuccess;
+    const size_t cap = 200 * 1024;  // set once to the largest size any line needs
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max(smem, cap));
+    if (e != cudaSuccess) e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+        for (int k = 0; k < 4; k++)
+            if (done_fn[k] == nullptr || done_fn[k] == fn) { done_fn[k] = fn; done_sz[k] = std::max(smem, cap); break; }
+    return e;
 }
 
 cudaError_t ee_launch_cone(const EeParams& P, const EeBeamSpec* specs, const EeBeamGeom* geoms, const float* terma,
-                           float* rev, float2* samples, int nbeams, int max_lines, int max_line, cudaStream_t s) {
+                           float* rev, float2* samples, int nbeams, int max_lines, int max_line, cudaStream_t s,
+                           int lane_block) {
     if (P.mode == 1 && samples) {  // exp kernel: one lane per line; the caller zeroed `rev`
-        dim3 grid(grid1(max_lines, LANE_BLOCK), P.nrays, nbeams);
-        k_cone_lane<<<grid, LANE_BLOCK, 0, s>>>(P, specs, geoms, terma, rev, samples);
+        dim3 grid(grid1(max_lines, lane_block), P.nrays, nbeams);
+        if (lane_block == 64) k_cone_lane<64><<<grid, 64, 0, s>>>(P, specs, geoms, terma, rev, samples);
+        else if (lane_block == 256) k_cone_lane<256><<<grid, 256, 0, s>>>(P, specs, geoms, terma, rev, samples);
+        else k_cone_lane<128><<<dim3(grid1(max_lines, 128), P.nrays, nbeams), 128, 0, s>>>(P, specs, geoms, terma, rev, samples);
         return cudaGetLastError();
     }
     size_t smem = cone_smem(max_line);
@@ -1277,8 +1299,13 @@ cudaError_t ee_launch_gather(const EeParams& P, const EeBeamSpec* specs, const E
 cudaError_t ee_launch_gather_T(const EeParams& P, const EeBeamSpec* specs, const EeBeamGeom* geoms,
                                const float* dose_grad, float* rev_grad, int nbeams, int max_tiles, cudaStream_t s) {
     const size_t smem = sizeof(float) * GT_SMEM;
-    cudaError_t e = cudaFuncSetAttribute((const void*)k_gather_T, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaError_t e = cudaFuncSetAttribute((const void*)k_gather_T, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+        attr_set = true;
+    }
     dim3 grid(max(1, max_tiles), 1, nbeams);
     k_gather_T<<<grid, GT_TX * GT_TY * GT_TZ, smem, s>>>(P, specs, geoms, dose_grad, rev_grad);
     return cudaGetLastError();
@@ -1286,10 +1313,14 @@ cudaError_t ee_launch_gather_T(const EeParams& P, const EeBeamSpec* specs, const
 
 cudaError_t ee_launch_cone_T(const EeParams& P, const EeBeamSpec* specs, const EeBeamGeom* geoms, const float* rev_grad,
                              float2* scratch, float* terma_grad, int nbeams, int max_lines, int max_line,
-                             cudaStream_t s) {
+                             cudaStream_t s, int lane_block) {
     if (P.mode == 1 && scratch) {
-        dim3 grid(grid1(max_lines, LANE_BLOCK), P.nrays, nbeams);
-        k_cone_T_lane<<<grid, LANE_BLOCK, 0, s>>>(P, specs, geoms, rev_grad, scratch, terma_grad);
+        dim3 grid(grid1(max_lines, lane_block), P.nrays, nbeams);
+        if (lane_block == 64) k_cone_T_lane<64><<<grid, 64, 0, s>>>(P, specs, geoms, rev_grad, scratch, terma_grad);
+        else if (lane_block == 256) k_cone_T_lane<256><<<grid, 256, 0, s>>>(P, specs, geoms, rev_grad, scratch, terma_grad);
+        else
+            k_cone_T_lane<128><<<dim3(grid1(max_lines, 128), P.nrays, nbeams), 128, 0, s>>>(P, specs, geoms, rev_grad,
+                                                                                          scratch, terma_grad);
         return cudaGetLastError();
     }
     size_t smem = cone_smem(max_line);

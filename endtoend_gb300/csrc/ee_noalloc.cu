@@ -113,7 +113,7 @@ extern "C" int ee_beam_dose_noalloc(ee_context* ctx, const ee_beam* beam, const 
     float* d_terma = (float*)(base + off_terma);
     if ((e = cudaMemcpyAsync(d_spec, &S, sizeof(S), cudaMemcpyHostToDevice, s)) != cudaSuccess)
         return cuda_fail(e, "spec upload");
-    if ((e = ee_launch_geom_init(d_geom, 1, s)) != cudaSuccess) return cuda_fail(e, "k_geom_init");
+    if ((e = ee_launch_geom_init(d_spec, d_geom, 1, s)) != cudaSuccess) return cuda_fail(e, "k_geom_init");
     if ((e = ee_launch_terma(P, d_spec, d_geom, d_fluence, d_terma, nullptr, nullptr, 1, tvol > 0 ? tvol : 1, s)) !=
         cudaSuccess)
         return cuda_fail(e, "k_terma");

@@ -112,6 +112,12 @@ _SIGS = {
     "ee_dose_and_adjoint": (C.c_int, [C.c_void_p, C.POINTER(EEBeam), C.c_int, C.c_void_p, C.c_void_p, C.c_int,
                                       C.c_void_p, C.c_void_p]),
     "ee_beam_dose_noalloc": (C.c_int, [C.c_void_p, C.POINTER(EEBeam), C.c_void_p, C.c_void_p, C.c_void_p]),
+    "ee_plan_create": (C.c_int, [C.c_void_p, C.POINTER(EEBeam), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                 C.c_void_p, C.POINTER(C.c_void_p)]),
+    "ee_plan_launch": (C.c_int, [C.c_void_p]),
+    "ee_plan_status": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "ee_plan_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_longlong), C.POINTER(C.c_int)]),
+    "ee_plan_destroy": (C.c_int, [C.c_void_p]),
     "ee_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
     "ee_set_scratch_limit": (C.c_int, [C.c_void_p, C.c_longlong]),
     "ee_read_profile": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_longlong), C.c_int]),
@@ -292,6 +298,10 @@ class Engine:
         self._check(self.lib.ee_beam_dose_noalloc(self.h, eb, C.c_void_p(d_fluence), C.c_void_p(d_dose),
                                                   C.c_void_p(stream or None)))
 
+    def plan(self, beams, d_fluence: int, d_dose: int, d_dose_grad: int = 0, d_fluence_grad: int = 0) -> "Plan":
+        """Capture a batch into a replayable CUDA graph (see ee_plan_create)."""
+        return Plan(self, beams, d_fluence, d_dose, d_dose_grad, d_fluence_grad)
+
     # -- diagnostics
     def beam_info(self, i: int) -> dict:
         bi = BeamInfo()
@@ -338,6 +348,43 @@ class Engine:
 
     def __exit__(self, *a):
         self.close()
+
+
+class Plan:
+    """A batch of beams captured into a CUDA graph (ee_plan_*)."""
+
+    def __init__(self, eng: Engine, beams, d_fluence, d_dose, d_dose_grad=0, d_fluence_grad=0):
+        self.eng = eng
+        self._eb = to_ee_beams(beams)
+        h = C.c_void_p()
+        eng._check(eng.lib.ee_plan_create(eng.h, self._eb, len(beams), C.c_void_p(d_fluence), C.c_void_p(d_dose),
+                                          C.c_void_p(d_dose_grad or None), C.c_void_p(d_fluence_grad or None),
+                                          C.byref(h)))
+        self.h = h
+
+    def launch(self):
+        self.eng._check(self.eng.lib.ee_plan_launch(self.h))
+
+    def status(self):
+        n = C.c_int()
+        self.eng._check(self.eng.lib.ee_plan_status(self.h, C.byref(n)))
+        return n.value
+
+    def info(self):
+        lb, by, nc = C.c_int(), C.c_longlong(), C.c_int()
+        self.eng._check(self.eng.lib.ee_plan_info(self.h, C.byref(lb), C.byref(by), C.byref(nc)))
+        return {"lane_block": lb.value, "device_bytes": by.value, "chunks": nc.value}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.eng.lib.ee_plan_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def beam_source(beam):

@@ -203,6 +203,23 @@ int ee_dose_and_adjoint(ee_context *ctx, const ee_beam *beams, int nbeams, const
  * stream capture.  `stream` is a cudaStream_t (NULL = legacy default). */
 int ee_beam_dose_noalloc(ee_context *ctx, const ee_beam *beam, const float *d_fluence, float *d_dose, void *stream);
 
+/* ---- planned batches (CUDA graph) ----
+ * ee_plan_create fixes a batch of beams and the device buffers it reads and
+ * writes (fluence in, dose out, and optionally dose gradient in / fluence
+ * gradient out), sizes every intermediate from geometric upper bounds, runs
+ * the batch once to validate them, autotunes the cone kernels' block shape
+ * on it and captures the whole forward(+adjoint) chain into one CUDA graph.
+ * ee_plan_launch replays that graph on the context stream with no host
+ * synchronisation (new fluence / gradient values are read from the same
+ * buffers); ee_plan_status then reports per-beam failures. */
+typedef struct ee_plan ee_plan;
+int ee_plan_create(ee_context *ctx, const ee_beam *beams, int nbeams, const float *d_fluence, float *d_dose,
+                   const float *d_dose_grad, float *d_fluence_grad, ee_plan **plan);
+int ee_plan_launch(ee_plan *plan);
+int ee_plan_status(ee_plan *plan, int *nfailed);
+int ee_plan_info(ee_plan *plan, int *lane_block, long long *device_bytes, int *nchunks);
+int ee_plan_destroy(ee_plan *plan);
+
 /* ---- diagnostics ---- */
 /* Stage ids for ee_read_profile. */
 #define EE_STAGE_TERMA 0     /* k_terma (+crop-box reduction)           */
