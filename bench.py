@@ -44,6 +44,10 @@ def parse():
     ap.add_argument("--scratch-gb", type=int, default=64)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--serve-requests", type=int, default=100)
+    ap.add_argument("--serve-rate", type=float, default=50.0)
+    ap.add_argument("--serve-slots", type=int, default=2)
+    ap.add_argument("--no-serve", action="store_true")
     return ap.parse_args()
 
 
@@ -130,6 +134,104 @@ def make_workload(n_beams, seed_offset=0):
     phys = inputs.make_physics(seed=0, spacing_cm=0.2)
     beams = inputs.candidate_beams(n_beams, seed=3 + seed_offset)
     return vol, phys, beams
+
+
+def serving_leg(args, device, phys):
+    """Request loop (ee_server_*) under Poisson arrivals versus the plain path
+    (one request at a time through the host-pointer calls, FIFO-queued against
+    the same arrival times)."""
+    import ctypes as C
+    import threading
+    from endtoend_gb300 import engine, inputs
+
+    vols, reqs = inputs.serving_workload(args.serve_requests, args.serve_rate, seed=9)
+    rng = np.random.default_rng(13)
+    grads = [rng.standard_normal(v.density.shape).astype(np.float32) for v in vols]
+    nbeams = sum(len(r["beams"]) for r in reqs)
+
+    # plain: one engine context per phantom, one request per call
+    engs = []
+    for v in vols:
+        e = engine.Engine(device)
+        e.set_volume(v)
+        e.set_physics(phys, mode="exp")
+        engs.append(e)
+
+    def plain_call(r):
+        e = engs[r["volume"]]
+        if not r["grad"]:
+            e.beam_dose(r["beams"])
+            return
+        eb = engine.to_ee_beams(r["beams"])
+        fl = engine.concat_fluence(r["beams"])
+        dose = np.empty(vols[r["volume"]].density.shape, np.float32)
+        fg = np.empty_like(fl)
+        g = grads[r["volume"]]
+        e._check(e.lib.ee_dose_and_adjoint(e.h, eb, len(r["beams"]), C.c_void_p(fl.ctypes.data),
+                                           C.c_void_p(dose.ctypes.data), engine.DOSE_SUM, C.c_void_p(g.ctypes.data),
+                                           C.c_void_p(fg.ctypes.data)))
+
+    for k in range(len(vols)):  # warm contexts
+        plain_call({"volume": k, "beams": reqs[0]["beams"][:1], "grad": True})
+    service = []
+    for r in reqs:
+        t0 = time.perf_counter()
+        plain_call(r)
+        service.append(time.perf_counter() - t0)
+    for e in engs:
+        e.close()
+    end, lat = 0.0, []
+    for r, sv in zip(reqs, service):
+        end = max(end, r["t"]) + sv
+        lat.append(end - r["t"])
+    lat_plain = np.array(lat) * 1e3
+    plain = {"beams_per_s": nbeams / sum(service), "p50_ms": float(np.percentile(lat_plain, 50)),
+             "p99_ms": float(np.percentile(lat_plain, 99)), "makespan_s": end}
+
+    srv = engine.Server(device, slots=args.serve_slots, max_batch_beams=256)
+    srv.set_physics(phys, mode="exp")
+    for v in vols:
+        srv.add_volume(v)
+    for k in range(len(vols)):  # every slot builds its contexts
+        ts = [srv.submit(k, reqs[0]["beams"][:1], grads[k]) for _ in range(args.serve_slots)]
+        for t in ts:
+            srv.wait(t)
+    srv.reset_stats()
+    tickets = []
+    done = threading.Event()
+
+    def waiter():
+        i = 0
+        while not (done.is_set() and i >= len(tickets)):
+            if i < len(tickets):
+                srv.wait(tickets[i])
+                i += 1
+            else:
+                time.sleep(0.001)
+
+    th = threading.Thread(target=waiter)
+    th.start()
+    t_start = time.perf_counter()
+    for r in reqs:
+        dt = t_start + r["t"] - time.perf_counter()
+        if dt > 0:
+            time.sleep(dt)
+        tickets.append(srv.submit(r["volume"], r["beams"], grads[r["volume"]] if r["grad"] else None))
+    done.set()
+    th.join()
+    makespan = time.perf_counter() - t_start
+    st = srv.stats()
+    srv.close()
+    return {
+        "workload": f"{len(reqs)} requests, Poisson {args.serve_rate:g}/s, phantoms "
+                    + ", ".join("x".join(str(n) for n in s) for s in inputs.SERVING_SHAPES)
+                    + " @2mm, 1-40 beams, fluence 16^2-64^2 @2.5mm, dose or dose+gradient",
+        "beams": nbeams, "slots": args.serve_slots,
+        "served": {"beams_per_s": nbeams / makespan, "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
+                   "completed": st["completed"], "makespan_s": makespan},
+        "plain": plain,
+        "served_over_plain": (nbeams / makespan) / plain["beams_per_s"],
+    }
 
 
 def cpu_reference_sample(vol, phys, beams, steps=1, warmup=0, nthreads=None):
@@ -355,6 +457,11 @@ def main():
         cpu = {"value": 1.0 / t_cpu, "unit": UNIT, "cores": cores, "kind": "port",
                "sample": "1 beam forward + adjoint (FP32 OpenMP restatement, 24-radius table walk)"}
 
+    serving = None
+    if not args.no_serve and rank == 0:
+        eng.synchronize()
+        serving = serving_leg(args, local, phys)
+
     lat_ms = np.array(lat) * 1e3
     if rank == 0:
         line = {
@@ -374,6 +481,7 @@ def main():
             "batched_over_plain": value / plain,
             "pipeline": {"value": pipeline_value, "unit": UNIT, "note": "same batch, direct call (host geometry read-back per chunk)"},
             "plan": plan_info,
+            "serving": serving,
             "gpu_launches": gpu_launches,
             "roofline": roof,
             "clocks": clk,

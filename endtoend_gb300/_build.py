@@ -14,7 +14,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 OUT_DIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(OUT_DIR, "libee_cccs.so")
-SOURCES = ["ee_kernels.cu", "ee_api.cpp", "ee_noalloc.cu"]
+SOURCES = ["ee_kernels.cu", "ee_api.cpp", "ee_noalloc.cu", "ee_server.cpp"]
 HEADERS = ["ee_internal.h", os.path.join("..", "..", "include", "ee_cccs.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -59,7 +59,7 @@ def build(verbose=False, force=False):
         if p.wait() != 0:
             raise RuntimeError("nvcc compilation of the CCCS engine failed")
     tmp = LIB + ".tmp"
-    cmd = [nvcc] + ARCH + ["-shared", "-cudart", "static", "-o", tmp] + objs
+    cmd = [nvcc] + ARCH + ["-shared", "-cudart", "static", "-o", tmp] + objs + ["-lpthread"]
     if verbose:
         print(" ".join(cmd), flush=True)
     if subprocess.call(cmd) != 0:

@@ -386,6 +386,8 @@ struct PipeArgs {
     const ee_loss* loss = nullptr;       // or: gradient of the EndtoEnd dose terms
     float* d_fgrad = nullptr;            // adjoint output (nullptr: no adjoint)
     double* loss_acc = nullptr;          // device accumulator [3] for loss terms
+    const int* group = nullptr;          // host: output volume index of each beam (grouped sums)
+    int ngroups = 1;
 };
 
 // One call of the CCCS chain over a list of beams:
@@ -409,6 +411,8 @@ int pipeline(ee_context* c, const PipeArgs& A) {
     EE_CUDA(c->h_specs.ensure(n));
     EE_CUDA(c->h_geoms.ensure(n));
     build_specs(c->P, A.beams, n, c->h_specs.p);
+    if (A.group)
+        for (int b = 0; b < n; b++) c->h_specs.p[b].out_off = (long long)A.group[b] * nfull;
     long long tvol_total = 0;
     for (int b = 0; b < n; b++) tvol_total += tvol_of(c->h_specs.p[b]);
     EE_CUDA(grow(c, c->d_specs, n));
@@ -425,7 +429,8 @@ int pipeline(ee_context* c, const PipeArgs& A) {
     std::vector<ChunkDims> dims(nchunks);
     c->last_geoms.clear();
     c->last_specs.assign(c->h_specs.p, c->h_specs.p + n);
-    if (fwd && A.dose_mode == EE_DOSE_SUM) EE_CUDA(cudaMemsetAsync(A.d_dose, 0, sizeof(float) * nfull, s));
+    if (fwd && A.dose_mode == EE_DOSE_SUM)
+        EE_CUDA(cudaMemsetAsync(A.d_dose, 0, sizeof(float) * nfull * (A.group ? A.ngroups : 1), s));
     if (fwd && A.dose_mode == EE_DOSE_PER_BEAM) EE_CUDA(cudaMemsetAsync(A.d_dose, 0, sizeof(float) * nfull * n, s));
 
     // ---- geometry + forward, chunk by chunk
@@ -1289,3 +1294,28 @@ void ee_internal_build_spec(const EeParams& P, const ee_beam& beam, EeBeamSpec* 
 const char* ee_internal_status_text(int st) { return status_text(st); }
 
 int ee_internal_fail(int code, const char* msg) { return fail(code, "%s", msg); }
+
+// Grouped forward (+adjoint) used by the request server: beam b's dose is
+// summed into volume group[b] of d_dose (ngroups volumes) and its adjoint
+// reads volume group[b] of d_dose_grad.
+int ee_internal_pipeline_grouped(ee_context* c, const ee_beam* beams, int nbeams, const float* d_fluence, float* d_dose,
+                                 const int* group, int ngroups, const float* d_dose_grad, float* d_fgrad) {
+    std::lock_guard<std::mutex> lk(c->mu);
+    PipeArgs A;
+    A.beams = beams; A.nbeams = nbeams; A.d_fluence = d_fluence; A.d_dose = d_dose; A.dose_mode = EE_DOSE_SUM;
+    A.d_dose_grad = d_dose_grad; A.d_fgrad = d_fgrad; A.group = group; A.ngroups = ngroups;
+    return pipeline(c, A);
+}
+
+// Device bytes the context's resident data and scratch occupy.
+long long ee_internal_context_bytes(ee_context* c) {
+    std::lock_guard<std::mutex> lk(c->mu);
+    long long b = 0;
+    b += 4ll * (c->density.n + c->cumkern.n + c->expp.n + c->terma.n + c->unit.n + c->rev.n + c->rev_grad.n +
+                c->terma_grad.n + c->io_fluence.n + c->io_dose.n + c->io_grad.n + c->xf.n + c->xg.n + c->spread_w.n +
+                c->bl_idx.n);
+    b += 8ll * (c->samples.n + c->acc.n);
+    b += (long long)sizeof(EeBeamSpec) * c->d_specs.n + (long long)sizeof(EeBeamGeom) * c->d_geoms.n;
+    if (c->dens_array) b += 4ll * c->density.n;
+    return b;
+}

@@ -70,6 +70,9 @@ struct EeBeamSpec {
     // plan_cap == 0: the arena is sized after the geometry read-back
     long long plan_off;
     long long plan_cap;
+    // element offset of this beam's dose (and dose-gradient) volume: grouped
+    // outputs of the request server; 0 otherwise
+    long long out_off;
 };
 
 // Per-cone geometry of one beam, computed on the device.

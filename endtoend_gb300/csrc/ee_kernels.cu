@@ -1067,7 +1067,7 @@ __global__ void __launch_bounds__(ROW_WARPS * 32) k_gather(EeParams P, const EeB
     const EeBeamSpec& S = specs[b];
     int x0, x1;
     if (!row_span(P, S, G, y, z, x0, x1)) return;
-    float* out = dose + (mode == 2 ? (long long)b * nfull : 0ll);
+    float* out = dose + S.out_off + (mode == 2 ? (long long)b * nfull : 0ll);
     const long long rbase = (long long)P.size[0] * (y + (long long)P.size[1] * z);
     for (int x = x0 + lane; x <= x1; x += 32) {
         float acc = beam_voxel_dose(P, S, G, rev, x, y, z);
@@ -1104,7 +1104,7 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
     float gd = 0.f;
     f3 bi = mk(0.f, 0.f, 0.f);
     if (x < G.gx0 + G.gnx && y < G.gy0 + G.gny && z < G.gz0 + G.gnz) {
-        gd = __ldg(dose_grad + x + (long long)P.size[0] * (y + (long long)P.size[1] * z));
+        gd = __ldg(dose_grad + S.out_off + x + (long long)P.size[0] * (y + (long long)P.size[1] * z));
         bi = mv(S.MB, mk((float)x - G.lim_off[0], (float)y - G.lim_off[1], (float)z - G.lim_off[2]));
         if (bi.x < -2.f || bi.y < -2.f || bi.z < -2.f || bi.x > G.bev[0] + 2.f || bi.y > G.bev[1] + 2.f ||
             bi.z > G.bev[2] + 2.f)

@@ -38,6 +38,9 @@ DOSE_SUM = 0
 DOSE_ACCUMULATE = 1
 DOSE_PER_BEAM = 2
 
+REQ_DOSE = 0
+REQ_DOSE_AND_GRAD = 1
+
 
 class EEError(RuntimeError):
     def __init__(self, code, msg):
@@ -86,6 +89,12 @@ class BeamInfo(C.Structure):
                 ("status", C.c_int)]
 
 
+class Request(C.Structure):
+    _fields_ = [("volume_id", C.c_int), ("kind", C.c_int), ("beams", C.POINTER(EEBeam)), ("nbeams", C.c_int),
+                ("fluence", C.c_void_p), ("dose_grad", C.c_void_p), ("dose_out", C.c_void_p),
+                ("fluence_grad_out", C.c_void_p)]
+
+
 # every symbol include/ee_cccs.h declares, with its ctypes signature
 _SIGS = {
     "ee_create": (C.c_int, [C.c_int, C.POINTER(C.c_void_p)]),
@@ -121,6 +130,17 @@ _SIGS = {
     "ee_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
     "ee_set_scratch_limit": (C.c_int, [C.c_void_p, C.c_longlong]),
     "ee_read_profile": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_longlong), C.c_int]),
+    "ee_server_create": (C.c_int, [C.c_int, C.c_int, C.c_longlong, C.c_int, C.POINTER(C.c_void_p)]),
+    "ee_server_set_physics": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                        C.POINTER(ConvParams), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                        C.c_void_p]),
+    "ee_server_add_volume": (C.c_int, [C.c_void_p, C.POINTER(Frame), C.c_void_p, C.POINTER(C.c_int)]),
+    "ee_server_submit": (C.c_int, [C.c_void_p, C.POINTER(Request), C.POINTER(C.c_longlong)]),
+    "ee_server_wait": (C.c_int, [C.c_void_p, C.c_longlong, C.c_double, C.POINTER(C.c_int)]),
+    "ee_server_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_longlong),
+                                  C.POINTER(C.c_double)]),
+    "ee_server_reset_stats": (C.c_int, [C.c_void_p]),
+    "ee_server_destroy": (C.c_int, [C.c_void_p]),
 }
 
 STAGES = ["terma", "geometry", "cone", "gather", "gather_T", "cone_T", "terma_T"]
@@ -167,6 +187,25 @@ def to_ee_beams(beams) -> "C.Array":
     return arr
 
 
+def _frame_of(vol) -> Frame:
+    f = Frame()
+    f.size[:] = [int(v) for v in vol.size]
+    f.voxel[:] = [float(v) for v in vol.voxel]
+    f.start[:] = [float(v) for v in vol.start]
+    f.bbox_start[:] = [int(v) for v in vol.bbox_start]
+    f.bbox_size[:] = [int(v) for v in vol.bbox_size]
+    return f
+
+
+def _raise_status(lib, st):
+    if st == EE_OK:
+        return
+    msg = lib.ee_last_error().decode(errors="replace")
+    cls = {EE_ERR_REV_SIZE: ArraySizeError, EE_ERR_CROPBOX: CropBoxError,
+           EE_ERR_NOT_READY: NotReadyError}.get(st, EEError)
+    raise cls(st, msg)
+
+
 def concat_fluence(beams) -> np.ndarray:
     return np.ascontiguousarray(np.concatenate([np.asarray(b.fluence, np.float32).ravel() for b in beams]))
 
@@ -187,23 +226,12 @@ class Engine:
 
     # -- errors
     def _check(self, st):
-        if st == EE_OK:
-            return
-        msg = self.lib.ee_last_error().decode(errors="replace")
-        cls = {EE_ERR_REV_SIZE: ArraySizeError, EE_ERR_CROPBOX: CropBoxError,
-               EE_ERR_NOT_READY: NotReadyError}.get(st, EEError)
-        raise cls(st, msg)
+        _raise_status(self.lib, st)
 
     # -- set-up
     def set_volume(self, vol):
-        f = Frame()
-        f.size[:] = [int(v) for v in vol.size]
-        f.voxel[:] = [float(v) for v in vol.voxel]
-        f.start[:] = [float(v) for v in vol.start]
-        f.bbox_start[:] = [int(v) for v in vol.bbox_start]
-        f.bbox_size[:] = [int(v) for v in vol.bbox_size]
         d = np.ascontiguousarray(vol.density, dtype=np.float32)
-        self._check(self.lib.ee_set_volume(self.h, C.byref(f), _ptr(d)))
+        self._check(self.lib.ee_set_volume(self.h, C.byref(_frame_of(vol)), _ptr(d)))
         self.vol = vol
 
     def set_physics(self, phys, mode: str = "exp", max_rev_size=(0, 0, 0)):
@@ -385,6 +413,110 @@ class Plan:
             self.close()
         except Exception:
             pass
+
+
+class Server:
+    """Continuous-batching request server on one GPU (ee_server_*).
+
+    ``submit`` copies a request's inputs and returns a ticket at once;
+    ``wait`` returns its summed dose (and, for gradient requests, the
+    per-beam fluence gradients)."""
+
+    def __init__(self, device: int = 0, slots: int = 2, hbm_budget: int = 0, max_batch_beams: int = 256):
+        self.lib = load_library()
+        h = C.c_void_p()
+        _raise_status(self.lib, self.lib.ee_server_create(int(device), int(slots), int(hbm_budget),
+                                                          int(max_batch_beams), C.byref(h)))
+        self.h = h
+        self.volumes = []
+        self._pending = {}
+
+    def set_physics(self, phys, mode: str = "exp"):
+        f32 = lambda a: np.ascontiguousarray(np.asarray(a, dtype=np.float32))
+        E, fl, mu, muen = f32(phys.energy), f32(phys.fluence), f32(phys.mu), f32(phys.mu_en)
+        cp = ConvParams()
+        cp.ntheta, cp.nphi, cp.nradii = phys.ntheta, phys.nphi, phys.nradii
+        cp.rev_latspacing, cp.rev_longspacing, cp.penumbra = phys.rev_latspacing, phys.rev_longspacing, phys.penumbra
+        cp.max_rev_size[:] = [0, 0, 0]
+        radii, ck, th, ph = f32(phys.radii), f32(phys.cumkern), f32(phys.theta_deg), f32(phys.phi_deg)
+        ep = f32(phys.exp_params) if mode == "exp" else None
+        _raise_status(self.lib, self.lib.ee_server_set_physics(
+            self.h, len(E), _ptr(E), _ptr(fl), _ptr(mu), _ptr(muen), C.byref(cp), _ptr(radii), _ptr(ck), _ptr(th),
+            _ptr(ph), _ptr(ep) if ep is not None else None))
+
+    def add_volume(self, vol) -> int:
+        d = np.ascontiguousarray(vol.density, dtype=np.float32)
+        vid = C.c_int()
+        _raise_status(self.lib, self.lib.ee_server_add_volume(self.h, C.byref(_frame_of(vol)), _ptr(d),
+                                                              C.byref(vid)))
+        self.volumes.append(vol)
+        return vid.value
+
+    def submit(self, volume_id: int, beams: Sequence, dose_grad: np.ndarray = None) -> int:
+        vol = self.volumes[volume_id]
+        eb = to_ee_beams(beams)
+        fl = concat_fluence(beams)
+        dose = np.zeros(vol.density.shape, np.float32)
+        q = Request()
+        q.volume_id, q.nbeams, q.beams = int(volume_id), len(beams), eb
+        q.fluence, q.dose_out = fl.ctypes.data, dose.ctypes.data
+        fg = g = None
+        if dose_grad is not None:
+            g = np.ascontiguousarray(dose_grad, dtype=np.float32)
+            assert g.shape == vol.density.shape
+            fg = np.zeros_like(fl)
+            q.kind, q.dose_grad, q.fluence_grad_out = REQ_DOSE_AND_GRAD, g.ctypes.data, fg.ctypes.data
+        else:
+            q.kind = REQ_DOSE
+        t = C.c_longlong()
+        _raise_status(self.lib, self.lib.ee_server_submit(self.h, C.byref(q), C.byref(t)))
+        self._pending[t.value] = (beams, dose, fg)
+        return t.value
+
+    def wait(self, ticket: int, timeout: float = None):
+        """(dose, fluence_grads or None); None while still pending after `timeout` s."""
+        st = C.c_int()
+        r = self.lib.ee_server_wait(self.h, C.c_longlong(ticket), -1.0 if timeout is None else float(timeout),
+                                    C.byref(st))
+        if r == EE_OK and st.value < 0:
+            return None
+        beams, dose, fg = self._pending.pop(ticket)
+        _raise_status(self.lib, r)
+        if fg is None:
+            return dose, None
+        out, o = [], 0
+        for b in beams:
+            n = int(b.fmap_size[0]) * int(b.fmap_size[1])
+            out.append(fg[o:o + n].reshape(int(b.fmap_size[1]), int(b.fmap_size[0])))
+            o += n
+        return dose, out
+
+    def stats(self) -> dict:
+        p50, p99, bps = C.c_double(), C.c_double(), C.c_double()
+        n = C.c_longlong()
+        _raise_status(self.lib, self.lib.ee_server_stats(self.h, C.byref(p50), C.byref(p99), C.byref(n),
+                                                         C.byref(bps)))
+        return {"p50_ms": p50.value, "p99_ms": p99.value, "completed": n.value, "beams_per_s": bps.value}
+
+    def reset_stats(self):
+        _raise_status(self.lib, self.lib.ee_server_reset_stats(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.ee_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
 
 
 def beam_source(beam):

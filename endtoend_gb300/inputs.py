@@ -268,3 +268,37 @@ def config1(n_beams: int = 1024, shape=(200, 200, 160)):
     """200x200x160 head-and-neck-like phantom at 2 mm with n_beams candidates."""
     vol = head_neck_phantom(shape=shape, voxel_cm=0.2)
     return vol, make_physics(seed=0, spacing_cm=0.2), candidate_beams(n_beams)
+
+
+SERVING_SHAPES = [(96, 96, 96), (128, 128, 128), (160, 160, 160), (256, 256, 192)]
+
+
+def serving_workload(n_requests: int = 100, rate_hz: float = 50.0, seed: int = 9, beamlet_cm: float = 0.25):
+    """Serving-loop workload: head-and-neck-like phantoms at 2 mm of the four
+    SERVING_SHAPES, and n_requests requests with Poisson arrival times
+    (rate_hz), each on a phantom drawn uniformly, with 1-40 beams of fluence
+    grids n x n, 16 <= n <= 64 (U(0,1) in the projected disc), half of them
+    dose-only and half dose + fluence gradient (kind drawn per request).
+    Returns (volumes, requests) with requests as dicts
+    {t: arrival s, volume: index, beams: [Beam], grad: bool}."""
+    rng = np.random.default_rng(seed)
+    vols = [head_neck_phantom(shape=s, voxel_cm=0.2, seed=seed + k) for k, s in enumerate(SERVING_SHAPES)]
+    t = np.cumsum(rng.exponential(1.0 / rate_hz, n_requests))
+    reqs = []
+    for k in range(n_requests):
+        nb = int(rng.integers(1, 41))
+        angs = four_pi_angles(nb, seed=int(rng.integers(1 << 30)))
+        beams = []
+        for g, c in angs:
+            n = int(rng.integers(16, 65))
+            yy, xx = np.mgrid[0:n, 0:n]
+            rr = np.hypot(xx + 0.5 - n / 2, yy + 0.5 - n / 2)
+            fl = rng.uniform(0.0, 1.0, (n, n)).astype(np.float32)
+            fl[rr > n / 2] = 0.0
+            fl[n // 2, n // 2] = max(fl[n // 2, n // 2], 0.5)
+            b = single_beam(fmap=(n, n), beamlet_cm=beamlet_cm, gantry_deg=float(g), couch_deg=float(c))
+            b.fluence = fl
+            beams.append(b)
+        reqs.append({"t": float(t[k]), "volume": int(rng.integers(0, len(vols))), "beams": beams,
+                     "grad": bool(rng.integers(0, 2))})
+    return vols, reqs

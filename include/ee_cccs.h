@@ -220,6 +220,49 @@ int ee_plan_status(ee_plan *plan, int *nfailed);
 int ee_plan_info(ee_plan *plan, int *lane_block, long long *device_bytes, int *nchunks);
 int ee_plan_destroy(ee_plan *plan);
 
+/* ---- request server (continuous batching) ----
+ * No counterpart in the reference (dosecalc-beam is a one-shot batch job):
+ * a serving loop for many small dose / dose+gradient requests on one GPU.
+ * `slots` worker threads, each with its own stream and a cache of
+ * device-resident volume contexts (density texture, kernels, scratch),
+ * least recently used first out when the HBM budget (bytes; <= 0: 80% of the
+ * free memory) would be exceeded.  A free slot takes the oldest queued
+ * request plus every other queued request for the same volume and kind (up
+ * to max_batch_beams beams) and computes them in one pass of the chain, each
+ * request's beams summed into its own dose volume.  Results equal those of
+ * ee_dose_and_adjoint on the same request alone.  Host buffers of a request
+ * are copied at submit (inputs) and written before its wait returns
+ * (outputs). */
+typedef struct ee_server ee_server;
+enum { EE_REQ_DOSE = 0, EE_REQ_DOSE_AND_GRAD = 1 };
+typedef struct {
+    int            volume_id;          /* from ee_server_add_volume                 */
+    int            kind;               /* EE_REQ_*                                  */
+    const ee_beam *beams;
+    int            nbeams;
+    const float   *fluence;            /* host, concatenated fluence maps           */
+    const float   *dose_grad;          /* host, full grid (EE_REQ_DOSE_AND_GRAD)    */
+    float         *dose_out;           /* host, full grid, summed over the beams    */
+    float         *fluence_grad_out;   /* host, like fluence (EE_REQ_DOSE_AND_GRAD) */
+} ee_request;
+int ee_server_create(int device, int slots, long long hbm_budget_bytes, int max_batch_beams, ee_server **server);
+/* Physics shared by every volume (ee_set_spectrum + ee_set_kernel_table +
+ * ee_set_kernel_exp when exp_params is non-null); before the first submit. */
+int ee_server_set_physics(ee_server *server, int nE, const float *energy, const float *fluence, const float *mu,
+                          const float *mu_en, const ee_conv_params *conv, const float *radii, const float *cumkern,
+                          const float *theta_deg, const float *phi_deg, const float *exp_params);
+int ee_server_add_volume(ee_server *server, const ee_frame *frame, const float *density, int *volume_id);
+int ee_server_submit(ee_server *server, const ee_request *request, long long *ticket);
+/* Wait for a ticket (timeout_s < 0: forever).  *status = -1 while still
+ * pending (the ticket stays valid), else the request's final status, which is
+ * also the return value. */
+int ee_server_wait(ee_server *server, long long ticket, double timeout_s, int *status);
+/* Latency percentiles (submit -> outputs written) and throughput since the
+ * last reset. */
+int ee_server_stats(ee_server *server, double *p50_ms, double *p99_ms, long long *completed, double *beams_per_s);
+int ee_server_reset_stats(ee_server *server);
+int ee_server_destroy(ee_server *server);
+
 /* ---- diagnostics ---- */
 /* Stage ids for ee_read_profile. */
 #define EE_STAGE_TERMA 0     /* k_terma (+crop-box reduction)           */
