@@ -14,8 +14,8 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 OUT_DIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(OUT_DIR, "libee_cccs.so")
-SOURCES = ["ee_kernels.cu", "ee_api.cpp", "ee_noalloc.cu", "ee_server.cpp"]
-HEADERS = ["ee_internal.h", os.path.join("..", "..", "include", "ee_cccs.h")]
+SOURCES = ["ee_kernels.cu", "ee_api.cpp", "ee_noalloc.cu", "ee_server.cpp", "ee_beamlet.cu"]
+HEADERS = ["ee_internal.h", "ee_device.cuh", os.path.join("..", "..", "include", "ee_cccs.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -187,6 +187,9 @@ struct ee_context {
     std::vector<cudaEvent_t> event_pool;
     double stage_ms[EE_NSTAGES] = {0};
     long long stage_launches[EE_NSTAGES] = {0};
+    // beamlet-column path: options and its own device workspace
+    EeBeamletOptions bl_opt{2.0f, {500, 500, 500}};
+    void* beamlet_ws = nullptr;
 };
 
 namespace {
@@ -759,6 +762,8 @@ int ee_destroy(ee_context* c) {
     c->io_fluence.release(); c->io_dose.release(); c->io_grad.release();
     c->xf.release(); c->xg.release(); c->spread_w.release(); c->acc.release();
     c->h_specs.release(); c->h_geoms.release();
+    ee_beamlet_free(c->beamlet_ws);
+    c->beamlet_ws = nullptr;
     drain_profile(c);
     for (auto e : c->event_pool) cudaEventDestroy(e);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -1271,6 +1276,62 @@ int ee_beam_source(const ee_beam* b, float source[3], float direction[3]) {
     reconfigure(*b, az, zen, s, d);
     source[0] = (float)s.x; source[1] = (float)s.y; source[2] = (float)s.z;
     direction[0] = (float)d.x; direction[1] = (float)d.y; direction[2] = (float)d.z;
+    return EE_OK;
+}
+
+// ---- beamlet dose columns (dosecalc-beamlet) ----
+int ee_set_beamlet_options(ee_context* c, float kernel_extent_cm, const int max_rev_size[3]) {
+    if (!c || !(kernel_extent_cm >= 0.f)) return fail(EE_ERR_INVALID_ARG, "bad beamlet options");
+    std::lock_guard<std::mutex> lk(c->mu);
+    c->bl_opt.kernel_extent = kernel_extent_cm;
+    if (max_rev_size)
+        for (int a = 0; a < 3; a++) {
+            if (max_rev_size[a] <= 0) return fail(EE_ERR_INVALID_ARG, "bad max_rev_size");
+            c->bl_opt.max_rev[a] = max_rev_size[a];
+        }
+    return EE_OK;
+}
+
+int ee_beamlet_columns_device(ee_context* c, const ee_beam* beam, const float* fluence, float thresh, ee_csr* out) {
+    int st = check_ready(c);
+    if (st) return st;
+    if (!out || !fluence) return fail(EE_ERR_INVALID_ARG, "null argument");
+    if ((st = check_beams(beam, 1))) return st;
+    if (!(thresh >= 0.f)) return fail(EE_ERR_INVALID_ARG, "threshold must be >= 0");
+    std::lock_guard<std::mutex> lk(c->mu);
+    cudaSetDevice(c->device);
+    EeBeamSpec S;
+    build_specs(c->P, beam, 1, &S);
+    return ee_beamlet_run(c->P, c->rays.data(), c->stream, &c->beamlet_ws, c->bl_opt, *beam, S, fluence, thresh, out);
+}
+
+int ee_copy_to_host(ee_context* c, void* dst, const void* src, long long bytes) {
+    if (!c || (bytes > 0 && (!dst || !src)) || bytes < 0) return fail(EE_ERR_INVALID_ARG, "bad copy arguments");
+    if (bytes == 0) return EE_OK;
+    std::lock_guard<std::mutex> lk(c->mu);
+    EE_CUDA(cudaMemcpyAsync(dst, src, (size_t)bytes, cudaMemcpyDeviceToHost, c->stream));
+    EE_CUDA(cudaStreamSynchronize(c->stream));
+    return EE_OK;
+}
+
+int ee_beamlet_columns(ee_context* c, const ee_beam* beam, const float* fluence, float thresh, long long capacity,
+                       int* beamlet_index, long long* col_ptr, int* row_index, float* value, long long* nnz,
+                       int* nbeamlets) {
+    if (!beamlet_index || !col_ptr || !nnz || !nbeamlets) return fail(EE_ERR_INVALID_ARG, "null argument");
+    ee_csr d;
+    int st = ee_beamlet_columns_device(c, beam, fluence, thresh, &d);
+    if (st) return st;
+    *nnz = d.nnz;
+    *nbeamlets = d.nbeamlets;
+    std::lock_guard<std::mutex> lk(c->mu);
+    EE_CUDA(cudaMemcpy(beamlet_index, d.beamlet_index, sizeof(int) * d.nbeamlets, cudaMemcpyDeviceToHost));
+    EE_CUDA(cudaMemcpy(col_ptr, d.col_ptr, sizeof(long long) * ((size_t)d.nbeamlets + 1), cudaMemcpyDeviceToHost));
+    if (d.nnz > capacity) return fail(EE_ERR_CAPACITY, "CSR needs %lld entries, capacity %lld", d.nnz, capacity);
+    if (d.nnz > 0) {
+        if (!row_index || !value) return fail(EE_ERR_INVALID_ARG, "null CSR output");
+        EE_CUDA(cudaMemcpy(row_index, d.row_index, sizeof(int) * d.nnz, cudaMemcpyDeviceToHost));
+        EE_CUDA(cudaMemcpy(value, d.value, sizeof(float) * d.nnz, cudaMemcpyDeviceToHost));
+    }
     return EE_OK;
 }
 

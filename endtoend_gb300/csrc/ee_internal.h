@@ -4,6 +4,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "../../include/ee_cccs.h"
+
 #define EE_MAX_RAYS 64
 #define EE_MAX_E 32
 #define EE_MAX_RADII 32
@@ -151,3 +153,12 @@ cudaError_t ee_launch_spread(const EeBeamSpec* specs, const float* in, float* ou
                              int max_pix, cudaStream_t s);
 cudaError_t ee_launch_smooth(const EeBeamSpec* specs, const float* x, float* grad, float eta, double* acc, int nbeams,
                              int max_pix, cudaStream_t s);
+
+// Beamlet-column path (ee_beamlet.cu).
+struct EeBeamletOptions {
+    float kernel_extent;  // dose kernel truncation, cm (argparser.h:27: 2 cm)
+    int max_rev[3];       // REV size limit that triggers re-batching (argparser.h:29: 500^3)
+};
+int ee_beamlet_run(const EeParams& P, const EeRayConst* rays, cudaStream_t s, void** ws, const EeBeamletOptions& opt,
+                   const ee_beam& beam, const EeBeamSpec& S, const float* fluence_host, float thresh, ee_csr* out);
+void ee_beamlet_free(void* ws);

@@ -89,6 +89,11 @@ class BeamInfo(C.Structure):
                 ("status", C.c_int)]
 
 
+class Csr(C.Structure):
+    _fields_ = [("nbeamlets", C.c_int), ("nnz", C.c_longlong), ("beamlet_index", C.c_void_p), ("col_ptr", C.c_void_p),
+                ("row_index", C.c_void_p), ("value", C.c_void_p)]
+
+
 class Request(C.Structure):
     _fields_ = [("volume_id", C.c_int), ("kind", C.c_int), ("beams", C.POINTER(EEBeam)), ("nbeams", C.c_int),
                 ("fluence", C.c_void_p), ("dose_grad", C.c_void_p), ("dose_out", C.c_void_p),
@@ -130,6 +135,12 @@ _SIGS = {
     "ee_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
     "ee_set_scratch_limit": (C.c_int, [C.c_void_p, C.c_longlong]),
     "ee_read_profile": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_longlong), C.c_int]),
+    "ee_set_beamlet_options": (C.c_int, [C.c_void_p, C.c_float, C.POINTER(C.c_int)]),
+    "ee_beamlet_columns_device": (C.c_int, [C.c_void_p, C.POINTER(EEBeam), C.c_void_p, C.c_float, C.POINTER(Csr)]),
+    "ee_beamlet_columns": (C.c_int, [C.c_void_p, C.POINTER(EEBeam), C.c_void_p, C.c_float, C.c_longlong, C.c_void_p,
+                                     C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_longlong),
+                                     C.POINTER(C.c_int)]),
+    "ee_copy_to_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_longlong]),
     "ee_server_create": (C.c_int, [C.c_int, C.c_int, C.c_longlong, C.c_int, C.POINTER(C.c_void_p)]),
     "ee_server_set_physics": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                         C.POINTER(ConvParams), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
@@ -339,6 +350,36 @@ class Engine:
                 "rev_samples": bi.rev_samples, "terma_nonzero": bi.terma_nonzero, "max_line": bi.max_line,
                 "status": bi.status}
 
+    # -- beamlet dose columns (dosecalc-beamlet)
+    def set_beamlet_options(self, kernel_extent_cm: float = 2.0, max_rev_size=None):
+        mr = None
+        if max_rev_size is not None:
+            mr = (C.c_int * 3)(*[int(v) for v in max_rev_size])
+        self._check(self.lib.ee_set_beamlet_options(self.h, float(kernel_extent_cm), mr))
+
+    def beamlet_columns_device(self, beam, thresh: float = 1e-4) -> Csr:
+        """Device CSR of one beam's beamlet columns (pointers owned by the
+        context until its next beamlet call)."""
+        eb = to_ee_beams([beam])
+        fl = np.ascontiguousarray(beam.fluence, np.float32).ravel()
+        out = Csr()
+        self._check(self.lib.ee_beamlet_columns_device(self.h, eb, _ptr(fl), float(thresh), C.byref(out)))
+        return out
+
+    def beamlet_columns(self, beam, thresh: float = 1e-4):
+        """(beamlet_index, col_ptr, row_index, value) numpy arrays of one
+        beam's sparse beamlet dose columns (dosecalc-beamlet semantics)."""
+        d = self.beamlet_columns_device(beam, thresh)
+        n, nnz = d.nbeamlets, d.nnz
+        bidx = np.zeros(n, np.int32)
+        cp = np.zeros(n + 1, np.int64)
+        rows = np.zeros(nnz, np.int32)
+        vals = np.zeros(nnz, np.float32)
+        for arr, src in ((bidx, d.beamlet_index), (cp, d.col_ptr), (rows, d.row_index), (vals, d.value)):
+            if arr.nbytes:
+                self._check(self.lib.ee_copy_to_host(self.h, _ptr(arr), C.c_void_p(src), arr.nbytes))
+        return bidx, cp, rows, vals
+
     def set_scratch_limit(self, nbytes: int):
         self._check(self.lib.ee_set_scratch_limit(self.h, int(nbytes)))
 
@@ -453,6 +494,8 @@ class Server:
         return vid.value
 
     def submit(self, volume_id: int, beams: Sequence, dose_grad: np.ndarray = None) -> int:
+        if not 0 <= int(volume_id) < len(self.volumes):
+            raise EEError(EE_ERR_INVALID_ARG, f"unknown volume id {volume_id}")
         vol = self.volumes[volume_id]
         eb = to_ee_beams(beams)
         fl = concat_fluence(beams)

@@ -220,6 +220,41 @@ int ee_plan_status(ee_plan *plan, int *nfailed);
 int ee_plan_info(ee_plan *plan, int *lane_block, long long *device_bytes, int *nchunks);
 int ee_plan_destroy(ee_plan *plan);
 
+/* ---- beamlet dose columns (dosecalc-beamlet) ----
+ * Replaces dosecalc-beamlet's radconvolveTexture (CCCS/dosecalc-beamlet/
+ * nvbbRayConvolve_host.cu:444) + the sparsify workers (CCCS/DoseCalcIO/
+ * sparse_io.cpp:22-59) for one beam: one column per active beamlet (fluence
+ * > 0, fluence-map order), the beamlet's dose on the calc bbox computed in its
+ * own pillar (kernel truncated at the kernel extent), entries kept where
+ * value > thresh * column max.  Column c holds row_index/value[col_ptr[c] ..
+ * col_ptr[c+1]), row_index = full-grid voxel index (x fastest), ascending.
+ * The kernel table and cone angles of ee_set_kernel_table are used with the
+ * reference's beamlet conventions (mean radii); ee_set_kernel_exp is not. */
+typedef struct {
+    int              nbeamlets;
+    long long        nnz;
+    const int       *beamlet_index;  /* [nbeamlets] fluence-map linear index    */
+    const long long *col_ptr;        /* [nbeamlets+1]                           */
+    const int       *row_index;      /* [nnz]                                   */
+    const float     *value;          /* [nnz]                                   */
+} ee_csr;
+/* kernel_extent_cm (default 2, argparser.h:27) and the REV size limit that
+ * splits the beamlets of a beam into batches (default 500^3, argparser.h:29;
+ * NULL keeps it). */
+int ee_set_beamlet_options(ee_context *ctx, float kernel_extent_cm, const int max_rev_size[3]);
+/* Device pointers owned by the context, valid until its next beamlet call. */
+int ee_beamlet_columns_device(ee_context *ctx, const ee_beam *beam, const float *fluence_host, float thresh,
+                              ee_csr *out);
+/* Copies `bytes` of device memory (e.g. the arrays of an ee_csr) to the
+ * host, ordered after the context's queued work. */
+int ee_copy_to_host(ee_context *ctx, void *dst, const void *src, long long bytes);
+/* Host copy.  beamlet_index / col_ptr need fmap_size[0]*fmap_size[1] (+1)
+ * entries; row_index / value `capacity` entries.  *nnz and *nbeamlets are
+ * always set; EE_ERR_CAPACITY when nnz > capacity (nothing else copied). */
+int ee_beamlet_columns(ee_context *ctx, const ee_beam *beam, const float *fluence, float thresh, long long capacity,
+                       int *beamlet_index, long long *col_ptr, int *row_index, float *value, long long *nnz,
+                       int *nbeamlets);
+
 /* ---- request server (continuous batching) ----
  * No counterpart in the reference (dosecalc-beam is a one-shot batch job):
  * a serving loop for many small dose / dose+gradient requests on one GPU.

@@ -95,3 +95,63 @@ class ReferenceHarness:
         if st != 0:
             raise RuntimeError(f"reference harness status {st}")
         return dose, terma, list(info)[:3]
+
+
+_LIB_BL = None
+
+
+def _lib_beamlet():
+    global _LIB_BL
+    if _LIB_BL is None:
+        lib = C.CDLL(_build.build(which="beamlet"))
+        lib.ccref_beamlet_columns.argtypes = [C.POINTER(RefSetup), C.POINTER(RefBeam), C.POINTER(C.c_float), C.c_float,
+                                              C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_int),
+                                              C.POINTER(C.c_int)]
+        lib.ccref_beamlet_columns.restype = C.c_int
+        _LIB_BL = lib
+    return _LIB_BL
+
+
+def sparsify(column, thresh, bbox_start, size):
+    """dcio::_sparsify (CCCS/DoseCalcIO/sparse_io.cpp:22-59): keep the voxels
+    of a dense calc-bbox column whose value exceeds thresh * column max, keyed
+    by their linear index on the full grid.  Returned sorted by key."""
+    col = np.asarray(column, np.float32)
+    vmax = float(col.max()) if col.size else 0.0
+    keep = col > np.float32(thresh) * np.float32(vmax)
+    kz, ky, kx = np.nonzero(keep)
+    nx, ny = int(size[0]), int(size[1])
+    keys = ((kz + int(bbox_start[2])) * ny + (ky + int(bbox_start[1]))) * nx + (kx + int(bbox_start[0]))
+    order = np.argsort(keys, kind="stable")
+    return keys[order].astype(np.int64), col[keep][order]
+
+
+class BeamletHarness(ReferenceHarness):
+    """The reference's dosecalc-beamlet kernels (cudaBeamletRaytrace,
+    PackRowConvolve, PackedREVtoBEVdose, UnpackBEVDosePillar) run on the CPU."""
+
+    def __init__(self, vol, phys, tex_emulate=True, nthreads=None):
+        super().__init__(vol, phys, tex_emulate=tex_emulate, nthreads=nthreads)
+        self.lib = _lib_beamlet()
+
+    def columns(self, beam, kernel_extent=2.0, max_rev_size=(500, 500, 500)):
+        """(fluence-map indices of the active beamlets, dense calc-bbox
+        columns [n, bz, by, bx], info: [active, pillar dims x3, batches, ...])."""
+        b = RefBeam()
+        b.azimuth, b.zenith, b.coll = beam.azimuth, beam.zenith, beam.coll
+        b.iso[:] = [float(v) for v in beam.isocenter]
+        b.sad = beam.sad
+        b.fmap[:] = [int(v) for v in beam.fmap_size]
+        b.beamlet[:] = [float(v) for v in beam.beamlet_size]
+        fl = np.ascontiguousarray(beam.fluence, np.float32).ravel()
+        n = int((fl > 0).sum())
+        bs = self.vol.bbox_size
+        cols = np.zeros((max(n, 1), bs[2], bs[1], bs[0]), np.float32)
+        idx = np.zeros(max(n, 1), np.int32)
+        info = (C.c_int * 8)()
+        mr = (C.c_int * 3)(*[int(v) for v in max_rev_size])
+        st = self.lib.ccref_beamlet_columns(C.byref(self.setup), C.byref(b), _fp(fl), float(kernel_extent), mr, max(n, 1),
+                                            _fp(cols), idx.ctypes.data_as(C.POINTER(C.c_int)), info)
+        if st != 0:
+            raise RuntimeError(f"reference beamlet harness status {st}")
+        return idx[:n], cols[:n], list(info)

@@ -1,9 +1,10 @@
 """Build recipe for the reference harness (test infrastructure only).
 
-Compiles oracle/ref_harness/ref_harness.cpp, which includes the reference's
-own kernel sources from the reference checkout, into oracle/_ref/libccref.so
-with the host C++ compiler (kernels executed on the CPU through
-cuda_cpu_shim.h).  Needs the reference checkout; the library is git-ignored
+Compiles oracle/ref_harness/ref_harness.cpp (dosecalc-beam kernels) and
+ref_beamlet_harness.cpp (dosecalc-beamlet kernels), which include the
+reference's own kernel sources from the reference checkout, into
+oracle/_ref/libccref.so and oracle/_ref/libccref_beamlet.so with the host C++
+compiler (kernels executed on the CPU through cuda_cpu_shim.h).  Needs the reference checkout; the library is git-ignored
 and is only used to pin the oracle and to regenerate tests/golden.
 """
 import os
@@ -14,6 +15,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE = os.path.dirname(HERE)
 OUT = os.path.join(ORACLE, "_ref")
 LIB = os.path.join(OUT, "libccref.so")
+LIBS = {"beam": ("ref_harness.cpp", LIB),
+        "beamlet": ("ref_beamlet_harness.cpp", os.path.join(OUT, "libccref_beamlet.so"))}
 REF = os.environ.get("CCCS_REFERENCE", "/root/reference")
 
 
@@ -21,11 +24,12 @@ def available():
     return os.path.isdir(os.path.join(REF, "CCCS", "dosecalc-beam"))
 
 
-def build(verbose=False):
+def build(verbose=False, which="beam"):
     if not available():
         raise RuntimeError(f"reference checkout not found at {REF}")
     os.makedirs(OUT, exist_ok=True)
-    src = os.path.join(HERE, "ref_harness.cpp")
+    srcname, LIB = LIBS[which]
+    src = os.path.join(HERE, srcname)
     if os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(src),
                                                             os.path.getmtime(os.path.join(HERE, "cuda_cpu_shim.h"))):
         return LIB
@@ -44,4 +48,5 @@ def build(verbose=False):
 
 
 if __name__ == "__main__":
-    print(build(verbose=True))
+    for w in LIBS:
+        print(build(verbose=True, which=w))

@@ -1,7 +1,10 @@
 """Regenerate the golden fixtures in tests/golden/ from the reference's own
 dosecalc-beam kernel source, executed on the CPU by oracle/ref_harness
 (cudaSiddon, cudaRaytrace, RowConvolve, REV2XYZdose compiled unmodified from
-the reference checkout; texture filtering emulated with 8-bit weights).
+the reference checkout; texture filtering emulated with 8-bit weights), and
+the beamlet-column fixtures in tests/golden/beamlet/ from the reference's
+dosecalc-beamlet kernel source (cudaBeamletRaytrace, PackRowConvolve,
+PackedREVtoBEVdose, UnpackBEVDosePillar) sparsified as sparse_io.cpp does.
 
 Needs the reference checkout (default /root/reference, or $CCCS_REFERENCE).
 Each fixture stores its complete inputs, so tests never depend on the
@@ -18,7 +21,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
 from endtoend_gb300 import inputs  # noqa: E402
-from oracle.ref_harness import ReferenceHarness  # noqa: E402
+from oracle.ref_harness import BeamletHarness, ReferenceHarness, sparsify  # noqa: E402
 
 
 def cases():
@@ -38,7 +41,59 @@ def cases():
     yield "headneck48", vol, phys, [b]
 
 
+def beamlet_cases():
+    vol = inputs.slab_phantom(32, 0.25)
+    phys = inputs.make_physics(seed=7, spacing_cm=0.25)
+    b = inputs.single_beam(fmap=(3, 3), beamlet_cm=0.5, gantry_deg=30.0, couch_deg=0.0)
+    b.fluence = np.array([[1, 0.5, 0], [1, 1, 1], [0.2, 1, 1]], np.float32)
+    yield "bl_slab32", vol, phys, b, 2.0, (500, 500, 500), 1e-4
+    yield "bl_slab32_batched", vol, phys, b, 2.0, (110, 110, 110), 1e-4
+    vol = inputs.head_neck_phantom(shape=(40, 40, 32), voxel_cm=0.4, seed=3)
+    phys = inputs.make_physics(seed=5, spacing_cm=0.4)
+    rng = np.random.default_rng(77)
+    b = inputs.single_beam(fmap=(4, 4), beamlet_cm=0.4, gantry_deg=130.0, couch_deg=25.0, coll_deg=10.0)
+    f = rng.uniform(0.3, 1.0, (4, 4)).astype(np.float32)
+    f[0, 3] = 0.0
+    f[2, 1] = 0.0
+    b.fluence = f
+    yield "bl_headneck40", vol, phys, b, 1.5, (500, 500, 500), 1e-4
+
+
+def physics_fields(vol, phys):
+    return {
+        "density": vol.density, "voxel": vol.voxel, "start": vol.start, "bbox_start": vol.bbox_start,
+        "bbox_size": vol.bbox_size, "energy": phys.energy, "sp_fluence": phys.fluence, "mu": phys.mu,
+        "mu_en": phys.mu_en, "ntheta": phys.ntheta, "nphi": phys.nphi, "radii": phys.radii,
+        "exp_params": phys.exp_params, "cumkern": phys.cumkern, "theta_deg": phys.theta_deg,
+        "phi_deg": phys.phi_deg, "spacing": [phys.rev_latspacing, phys.rev_longspacing], "penumbra": phys.penumbra,
+    }
+
+
+def main_beamlet():
+    os.makedirs(os.path.join(HERE, "beamlet"), exist_ok=True)
+    for name, vol, phys, b, ke, max_rev, thresh in beamlet_cases():
+        h = BeamletHarness(vol, phys, tex_emulate=True)
+        idx, cols, info = h.columns(b, kernel_extent=ke, max_rev_size=max_rev)
+        out = physics_fields(vol, phys)
+        out.update({"beam_angles": [b.azimuth, b.zenith, b.coll], "beam_iso": b.isocenter, "beam_sad": b.sad,
+                    "beam_fmap": list(b.fmap_size), "beam_beamlet": list(b.beamlet_size), "beam_fluence": b.fluence,
+                    "kernel_extent": ke, "max_rev": list(max_rev), "thresh": thresh, "beamlet_index": idx,
+                    "info": info})
+        col_ptr, rows, vals = [0], [], []
+        for c in cols:
+            k, v = sparsify(c, thresh, vol.bbox_start, vol.size)
+            rows.append(k.astype(np.int32))
+            vals.append(v.astype(np.float32))
+            col_ptr.append(col_ptr[-1] + len(k))
+        out["col_ptr"] = np.array(col_ptr, np.int64)
+        out["row_index"] = np.concatenate(rows) if rows else np.zeros(0, np.int32)
+        out["value"] = np.concatenate(vals) if vals else np.zeros(0, np.float32)
+        print(name, "beamlets", len(idx), "nnz", int(col_ptr[-1]), "info", info)
+        np.savez_compressed(os.path.join(HERE, "beamlet", f"{name}.npz"), **out)
+
+
 def main():
+    main_beamlet()
     for name, vol, phys, beams in cases():
         h = ReferenceHarness(vol, phys, tex_emulate=True)
         out = {

@@ -36,3 +36,29 @@ def load(name):
         termas.append(z[f"beam{k}_terma"])
         bevs.append([int(v) for v in z[f"beam{k}_bev"]])
     return vol, phys, beams, doses, termas, bevs
+
+
+BEAMLET = os.path.join(GOLDEN, "beamlet")
+
+
+def beamlet_names():
+    return sorted(os.path.splitext(os.path.basename(p))[0] for p in glob.glob(os.path.join(BEAMLET, "*.npz")))
+
+
+def load_beamlet(name):
+    """(vol, phys, beam, kernel_extent, max_rev, thresh, reference CSR dict)."""
+    z = np.load(os.path.join(BEAMLET, name + ".npz"))
+    vol = inputs.Volume(density=z["density"].astype(np.float32), voxel=z["voxel"], start=z["start"],
+                        bbox_start=z["bbox_start"], bbox_size=z["bbox_size"])
+    sp = z["spacing"]
+    phys = inputs.Physics(energy=z["energy"], fluence=z["sp_fluence"], mu=z["mu"], mu_en=z["mu_en"],
+                          ntheta=int(z["ntheta"]), nphi=int(z["nphi"]), radii=z["radii"], exp_params=z["exp_params"],
+                          cumkern=z["cumkern"], theta_deg=z["theta_deg"], phi_deg=z["phi_deg"],
+                          rev_latspacing=float(sp[0]), rev_longspacing=float(sp[1]), penumbra=float(z["penumbra"]))
+    az, zen, coll = (float(v) for v in z["beam_angles"])
+    beam = inputs.Beam(azimuth=az, zenith=zen, coll=coll, isocenter=z["beam_iso"], sad=float(z["beam_sad"]),
+                       fmap_size=tuple(int(v) for v in z["beam_fmap"]),
+                       beamlet_size=tuple(float(v) for v in z["beam_beamlet"]),
+                       fluence=z["beam_fluence"].astype(np.float32))
+    ref = {k: z[k] for k in ("beamlet_index", "col_ptr", "row_index", "value", "info")}
+    return (vol, phys, beam, float(z["kernel_extent"]), tuple(int(v) for v in z["max_rev"]), float(z["thresh"]), ref)

@@ -1,0 +1,70 @@
+"""Beamlet dose columns (ee_beamlet_columns): every column of the CUDA path
+against the reference's own dosecalc-beamlet kernels (golden fixtures written
+by tests/golden/make_golden.py), plus the CSR invariants the sparsification
+defines (sorted rows, threshold, column pointers)."""
+import numpy as np
+import pytest
+
+import golden_cases
+from endtoend_gb300 import engine
+
+pytestmark = pytest.mark.gpu
+
+# max |engine - reference| over a column, relative to the column's maximum
+COLUMN_TOL = 0.005
+
+
+def densify(col_ptr, rows, vals, c, n):
+    d = np.zeros(n, np.float32)
+    a, b = int(col_ptr[c]), int(col_ptr[c + 1])
+    d[rows[a:b]] = vals[a:b]
+    return d
+
+
+def run(name):
+    vol, phys, beam, ke, max_rev, thresh, ref = golden_cases.load_beamlet(name)
+    with engine.Engine(0) as e:
+        e.set_volume(vol)
+        e.set_physics(phys, mode="table")
+        e.set_beamlet_options(ke, max_rev)
+        out = e.beamlet_columns(beam, thresh)
+    return vol, thresh, ref, out
+
+
+@pytest.mark.parametrize("name", golden_cases.beamlet_names())
+def test_beamlet_columns_match_reference(name):
+    vol, thresh, ref, (bidx, cp, rows, vals) = run(name)
+    np.testing.assert_array_equal(bidx, ref["beamlet_index"])
+    n = vol.nvoxels
+    errs = []
+    for c in range(len(bidx)):
+        r = densify(ref["col_ptr"], ref["row_index"], ref["value"], c, n)
+        g = densify(cp, rows, vals, c, n)
+        errs.append(float(np.abs(g - r).max() / r.max()))
+    print(name, "column errors", np.round(errs, 5))
+    assert max(errs) <= COLUMN_TOL, errs
+
+
+@pytest.mark.parametrize("name", golden_cases.beamlet_names())
+def test_beamlet_csr_invariants(name):
+    vol, thresh, ref, (bidx, cp, rows, vals) = run(name)
+    assert cp[0] == 0 and np.all(np.diff(cp) >= 0) and cp[-1] == len(rows) == len(vals)
+    for c in range(len(bidx)):
+        a, b = int(cp[c]), int(cp[c + 1])
+        assert b > a
+        assert np.all(np.diff(rows[a:b]) > 0)
+        v = vals[a:b]
+        assert np.all(v > np.float32(thresh) * v.max())
+        assert rows[a:b].min() >= 0 and rows[a:b].max() < vol.nvoxels
+
+
+def test_beamlet_empty_and_errors():
+    vol, phys, beam, ke, max_rev, thresh, ref = golden_cases.load_beamlet(golden_cases.beamlet_names()[0])
+    with engine.Engine(0) as e:
+        e.set_volume(vol)
+        e.set_physics(phys, mode="table")
+        beam.fluence = np.zeros_like(beam.fluence)
+        bidx, cp, rows, vals = e.beamlet_columns(beam, thresh)
+        assert len(bidx) == 0 and len(rows) == 0 and list(cp) == [0]
+        with pytest.raises(engine.EEError):
+            e.beamlet_columns(beam, -1.0)
