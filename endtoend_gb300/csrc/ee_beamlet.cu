@@ -311,6 +311,45 @@ __global__ void __launch_bounds__(BL_WARPS * 32)
     }
 }
 
+// tex3D<float> of a linear-memory volume as the texture unit filters it:
+// border addressing, linear filtering with each weight rounded to 8
+// fractional bits.  (x, y, z) are texel-space coordinates after the -0.5
+// texel-centre shift.  The reference's REV-dose and packed-dose fetches go
+// through textures (device.cu:423, 511); exact FP32 weights would move
+// beamlet columns by ~0.25% of their maximum.
+__device__ __forceinline__ float tri_border_q(const float* __restrict__ v, int nx, int ny, int nz, float x, float y,
+                                              float z) {
+    if (!(x > -1.f && x < (float)nx && y > -1.f && y < (float)ny && z > -1.f && z < (float)nz)) return 0.f;
+    const float fx = floorf(x), fy = floorf(y), fz = floorf(z);
+    const int i = (int)fx, j = (int)fy, k = (int)fz;
+    const float ax = floorf((x - fx) * 256.f + 0.5f) * (1.f / 256.f);
+    const float ay = floorf((y - fy) * 256.f + 0.5f) * (1.f / 256.f);
+    const float az = floorf((z - fz) * 256.f + 0.5f) * (1.f / 256.f);
+    const long long sxy = (long long)nx * ny;
+    float acc = 0.f;
+#pragma unroll
+    for (int dk = 0; dk < 2; dk++) {
+        const int kk = k + dk;
+        if (kk < 0 || kk >= nz) continue;
+        const float wz = dk ? az : 1.f - az;
+#pragma unroll
+        for (int dj = 0; dj < 2; dj++) {
+            const int jj = j + dj;
+            if (jj < 0 || jj >= ny) continue;
+            const float wy = dj ? ay : 1.f - ay;
+            const float* row = v + (long long)nx * jj + sxy * kk;
+#pragma unroll
+            for (int di = 0; di < 2; di++) {
+                const int ii = i + di;
+                if (ii < 0 || ii >= nx) continue;
+                const float w = (di ? ax : 1.f - ax) * wy * wz;
+                if (w != 0.f) acc += w * __ldg(row + ii);
+            }
+        }
+    }
+    return acc;
+}
+
 // PackedREVtoBEVdose (device.cu:407-431): packed voxel (pX, pY, pZ) += the
 // positive trilinear REV dose at its rotated position.  Packed layout: pY
 // fastest, then pZ, then pX.
@@ -325,7 +364,7 @@ __global__ void __launch_bounds__(256) k_bl_gather(BlGrid G, BlRayDev R, const f
     const f3 rot = mv(R.MK, mk((float)pX, (float)pY, (float)pZ));
     const float qx = fmaf(-R.rs[0], R.rcp[0], rot.x), qy = fmaf(-R.rs[1], R.rcp[1], rot.y),
                 qz = fmaf(-R.rs[2], R.rcp[2], rot.z);
-    const float d = tri_border(rev_dose, R.rev[0], R.rev[1], R.rev[2], qy, qz, qx);
+    const float d = tri_border_q(rev_dose, R.rev[0], R.rev[1], R.rev[2], qy, qz, qx);
     if (d > 0.f) packed[v] += d;
 }
 
@@ -347,7 +386,7 @@ __device__ __forceinline__ bool bl_unpack_coord(const EeParams& P, const BlGrid&
 __device__ __forceinline__ float bl_unpack_value(const BlGrid& G, const BlPillar& Q, const float* __restrict__ packed,
                                                  f3 u) {
     const float ux = u.x + (float)(Q.ix * G.pd[0]), uz = u.z + (float)(Q.iz * G.pd[2]);
-    const float d = tri_border(packed, G.gd[1], G.gd[2], G.gd[0], u.y - 0.5f, uz - 0.5f, ux - 0.5f);
+    const float d = tri_border_q(packed, G.gd[1], G.gd[2], G.gd[0], u.y - 0.5f, uz - 0.5f, ux - 0.5f);
     return d > 0.f ? d : 0.f;
 }
 

@@ -105,8 +105,8 @@ def _lib_beamlet():
     if _LIB_BL is None:
         lib = C.CDLL(_build.build(which="beamlet"))
         lib.ccref_beamlet_columns.argtypes = [C.POINTER(RefSetup), C.POINTER(RefBeam), C.POINTER(C.c_float), C.c_float,
-                                              C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_int),
-                                              C.POINTER(C.c_int)]
+                                              C.POINTER(C.c_int), C.c_float, C.c_int, C.POINTER(C.c_float),
+                                              C.POINTER(C.c_int), C.POINTER(C.c_int)]
         lib.ccref_beamlet_columns.restype = C.c_int
         _LIB_BL = lib
     return _LIB_BL
@@ -134,7 +134,7 @@ class BeamletHarness(ReferenceHarness):
         super().__init__(vol, phys, tex_emulate=tex_emulate, nthreads=nthreads)
         self.lib = _lib_beamlet()
 
-    def columns(self, beam, kernel_extent=2.0, max_rev_size=(500, 500, 500)):
+    def columns(self, beam, kernel_extent=2.0, max_rev_size=(500, 500, 500), rev_jitter=0.0):
         """(fluence-map indices of the active beamlets, dense calc-bbox
         columns [n, bz, by, bx], info: [active, pillar dims x3, batches, ...])."""
         b = RefBeam()
@@ -150,7 +150,8 @@ class BeamletHarness(ReferenceHarness):
         idx = np.zeros(max(n, 1), np.int32)
         info = (C.c_int * 8)()
         mr = (C.c_int * 3)(*[int(v) for v in max_rev_size])
-        st = self.lib.ccref_beamlet_columns(C.byref(self.setup), C.byref(b), _fp(fl), float(kernel_extent), mr, max(n, 1),
+        st = self.lib.ccref_beamlet_columns(C.byref(self.setup), C.byref(b), _fp(fl), float(kernel_extent), mr,
+                                            float(rev_jitter), max(n, 1),
                                             _fp(cols), idx.ctypes.data_as(C.POINTER(C.c_int)), info)
         if st != 0:
             raise RuntimeError(f"reference beamlet harness status {st}")

@@ -137,11 +137,12 @@ typedef struct {
 
 // Dense dose columns on the calc bbox (x fastest) of every active beamlet
 // (fluence > 0, fluence-map order), as UnpackBEVDosePillar leaves them before
-// sparsification.  columns: [max_cols][bbox voxels].  info: [0] active
+// sparsification (rev_jitter = 0).  columns: [max_cols][bbox voxels].  info: [0] active
 // beamlets, [1..3] pillar dims, [4] batches, [7] status (0 ok, 1 no anchor,
 // 2 too many beamlets, 3 rev.x > 1024, 4 more than 100 batches).
 int ccref_beamlet_columns(const ref_setup* S, const ref_beam* B, const float* fluence_map, float kernel_extent,
-                          const int* max_rev_size, int max_cols, float* columns, int* beamlet_index, int* info) {
+                          const int* max_rev_size, float rev_jitter, int max_cols, float* columns, int* beamlet_index,
+                          int* info) {
     ccsim::tex_emulate = S->tex_emulate;
     const int nth = S->nthreads > 0 ? S->nthreads : 1;
     for (int a = 0; a < 8; a++) info[a] = 0;
@@ -253,7 +254,9 @@ int ccref_beamlet_columns(const ref_setup* S, const ref_beam* B, const float* fl
                                             (unsigned)ceil(fabsf(mx3.x - mn3.x) / S->rev_latspacing));
                 if (rs.x > (unsigned)max_rev_size[0] || rs.y > (unsigned)max_rev_size[1] || rs.z > (unsigned)max_rev_size[2])
                     ok = false;
-                revs[k][r] = REV{rs, mn3};
+                // rev_jitter (cm, test sensitivity probes only; 0 = reference)
+                // moves the REV lattice origin of every direction
+                revs[k][r] = REV{rs, mn3 + make_float3(rev_jitter, -rev_jitter, rev_jitter)};
             }
         }
         if (ok) break;

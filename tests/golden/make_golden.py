@@ -85,10 +85,30 @@ def main_beamlet():
             rows.append(k.astype(np.int32))
             vals.append(v.astype(np.float32))
             col_ptr.append(col_ptr[-1] + len(k))
+        # the reference's own sensitivity: the same columns with the
+        # isocentre (or the REV lattice) moved by rounding-level amounts (1e-6 .. 1e-5 cm along
+        # several directions), per column max |change| / column max -- thin
+        # beamlets sampled on a rotated REV lattice put samples exactly on
+        # the footprint edge, where FP32 rounding decides (the reference's
+        # own GPU run, with its hardware sin/cos, lands on either side)
+        noise = np.zeros(len(idx))
+        shifts = [(1, -1, 1), (-1, 1, -1), (1, 0, 0), (0, 1, 0), (0, 0, 1), (-1, -1, 0), (0, -1, 1), (1, 1, 1)]
+        for k, sh in enumerate(shifts):
+            bp = inputs.Beam(**{**b.__dict__})
+            bp.isocenter = np.asarray(b.isocenter, np.float64) + (1e-5 if k % 2 == 0 else 1e-6) * np.array(sh, float)
+            _, cp_, _ = h.columns(bp, kernel_extent=ke, max_rev_size=max_rev)
+            for c in range(len(idx)):
+                noise[c] = max(noise[c], float(np.abs(cp_[c] - cols[c]).max() / cols[c].max()))
+        # ... and with the REV lattice origin moved by the same amounts
+        for jit in (1e-5, -1e-5, 1e-6, -1e-6):
+            _, cp_, _ = h.columns(b, kernel_extent=ke, max_rev_size=max_rev, rev_jitter=jit)
+            for c in range(len(idx)):
+                noise[c] = max(noise[c], float(np.abs(cp_[c] - cols[c]).max() / cols[c].max()))
+        out["ref_noise"] = noise
         out["col_ptr"] = np.array(col_ptr, np.int64)
         out["row_index"] = np.concatenate(rows) if rows else np.zeros(0, np.int32)
         out["value"] = np.concatenate(vals) if vals else np.zeros(0, np.float32)
-        print(name, "beamlets", len(idx), "nnz", int(col_ptr[-1]), "info", info)
+        print(name, "beamlets", len(idx), "nnz", int(col_ptr[-1]), "info", info, "ref noise", np.round(noise, 4))
         np.savez_compressed(os.path.join(HERE, "beamlet", f"{name}.npz"), **out)
 
 

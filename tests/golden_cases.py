@@ -60,5 +60,5 @@ def load_beamlet(name):
                        fmap_size=tuple(int(v) for v in z["beam_fmap"]),
                        beamlet_size=tuple(float(v) for v in z["beam_beamlet"]),
                        fluence=z["beam_fluence"].astype(np.float32))
-    ref = {k: z[k] for k in ("beamlet_index", "col_ptr", "row_index", "value", "info")}
+    ref = {k: z[k] for k in ("beamlet_index", "col_ptr", "row_index", "value", "info", "ref_noise")}
     return (vol, phys, beam, float(z["kernel_extent"]), tuple(int(v) for v in z["max_rev"]), float(z["thresh"]), ref)

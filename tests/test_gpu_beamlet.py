@@ -10,7 +10,11 @@ from endtoend_gb300 import engine
 
 pytestmark = pytest.mark.gpu
 
-# max |engine - reference| over a column, relative to the column's maximum
+# max |engine - reference| over a column, relative to the column's maximum:
+# 0.5%, plus the reference's own change under a 1e-5 cm isocentre shift
+# (stored per column in the fixture): thin beamlets sampled on a rotated
+# REV lattice put samples exactly on the footprint edge, where FP32 rounding
+# decides; columns the reference itself keeps within 0.5% must meet 0.5%
 COLUMN_TOL = 0.005
 
 
@@ -41,8 +45,11 @@ def test_beamlet_columns_match_reference(name):
         r = densify(ref["col_ptr"], ref["row_index"], ref["value"], c, n)
         g = densify(cp, rows, vals, c, n)
         errs.append(float(np.abs(g - r).max() / r.max()))
-    print(name, "column errors", np.round(errs, 5))
-    assert max(errs) <= COLUMN_TOL, errs
+    errs = np.array(errs)
+    print(name, "column errors", np.round(errs, 5), "reference noise", np.round(ref["ref_noise"], 5))
+    assert np.all(errs <= COLUMN_TOL + ref["ref_noise"]), errs
+    stable = ref["ref_noise"] <= COLUMN_TOL
+    assert np.all(errs[stable] <= COLUMN_TOL), errs
 
 
 @pytest.mark.parametrize("name", golden_cases.beamlet_names())
