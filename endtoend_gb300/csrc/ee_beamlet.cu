@@ -11,12 +11,15 @@
 // column.
 //
 // GB300 organisation:
-//   k_bl_cone    one warp per REV line: the warp computes the line's samples
-//                (pillar lookup, density texture, TERMA by a Siddon ray trace
-//                only for samples inside the beamlet's footprint -- the
-//                reference traces every sample), stages them in shared
-//                memory, and each lane walks its outputs; lines without TERMA
-//                only write zeros.
+//   k_bl_samples one thread per REV sample: pillar lookup and the beamlet
+//                test (exact only inside a box around the footprint);
+//                samples inside their beamlet are queued (the reference runs
+//                a Siddon trace for every sample).
+//   k_bl_terma   Siddon TERMA of the queued samples, lane-dense, flagging
+//                their lines.
+//   k_bl_walk    one warp per flagged REV line: densities sampled into
+//                shared memory, each lane summing its outputs over the line's
+//                TERMA samples as the walk would; other lines stay 0.
 //   k_bl_gather  packed-grid voxel += trilinear REV dose of one direction.
 //   k_bl_rows .. k_bl_emit
 //                unpack: per pillar only the calc-bbox rows its oriented box
@@ -52,6 +55,10 @@ struct BlPillar {
     int ix, iz;        // pillar position in the packed grid
     int b0[3], bn[3];  // calc-bbox-index AABB of the pillar's usable region (unpack)
     long long row0;    // first unpack row of this pillar
+    // the beamlet's footprint (the rays from the source through the corners
+    // of its fluence-map cell) in pillar-index coordinates: corner ray c is
+    // x = ex[c] + sx[c] * y, z = ez[c] + sz[c] * y
+    float ex[4], sx[4], ez[4], sz[4];
 };
 
 struct BlGrid {
@@ -187,127 +194,278 @@ __device__ __forceinline__ float kern_tex(const float* K, int nr, float x) {
     return (1.f - a) * K[i0] + a * K[i1];
 }
 
-// PackRowConvolve's walk (nvbbRayConvolve_device.cu:297-397) for output i in
-// direction `step` over a line staged in shared memory: the cumulative kernel
-// at the mean radii, interaction at voxel centres, the output voxel itself
-// counted in both directions, stopping at a wall (rho < 0) or the line end.
-__device__ __forceinline__ float bl_walk(const float* rho, const float* T, int L, int i, int step, const float* K,
-                                         const float* KR, int nr, float delr, float sum) {
-    float r_eff = 0.f, last = 0.f;
-    int idx = 0, kk = i;
-    do {
-        if (kk < 0 || kk >= L) break;
-        const float d = rho[kk];
-        if (d < 0.f) break;
-        const float de = delr * d;
-        r_eff += 0.5f * de;
-        if (r_eff > KR[nr - 1]) break;
-        while (KR[idx] < r_eff) idx++;
-        float cum;
-        if (idx <= 0) {
-            const float interp = r_eff * (1.f / KR[0]);
-            cum = kern_tex(K, nr, 0.5f) * interp;
-        } else {
-            const float interp = (r_eff - KR[idx - 1]) * (1.f / (KR[idx] - KR[idx - 1]));
-            cum = kern_tex(K, nr, (float)idx - 0.5f + interp);
-        }
-        sum += (cum - last) * T[kk];
-        last = cum;
-        if (kk != i) r_eff += 0.5f * de;
-        kk += step;
-    } while (idx < nr - 1);
-    return sum;
+// fmodf(x, y) for 0 <= x < 2^24 and an integer-valued y, given q =
+// floor(x / y) (possibly off by one from rounding): x - q*y is exact here
+// (q*y is an integer and the difference is a multiple of ulp(x) below y), and
+// one correction step lands it in [0, y) -- the value fmodf returns.
+__device__ __forceinline__ float fmod_int(float x, float y, float q) {
+    float r = fmaf(-q, y, x);
+    if (r < 0.f) r += y;
+    else if (r >= y) r -= y;
+    return r;
 }
 
 // One REV sample of the packed pillar grid (cudaBeamletRaytrace,
-// device.cu:20-246 with ss_factor 1): rho < 0 marks walls, empty pillars and
-// points outside the grid.
-__device__ __forceinline__ void bl_sample(const EeParams& P, const EeBeamSpec& S, const BlGrid& G,
-                                          const BlPillar* __restrict__ pil, const BlRayDev& R,
-                                          const float* __restrict__ fluence, int tX, int tY, int tZ, float& rho,
-                                          float& T, bool& cap) {
-    rho = -1e-12f;
-    T = 0.f;
+// device.cu:20-246 with ss_factor 1): the sample's pillar and its pillar
+// index coordinate; false for walls, empty pillars and points outside the
+// grid (the reference's INVALID density, -1e-12).
+__device__ __forceinline__ bool bl_locate(const BlGrid& G, const BlRayDev& R, int tX, int tY, int tZ, int& pidx,
+                                          f3& ip) {
     const f3 rv = mk(fmaf(R.rs[0], R.rcp[0], (float)tZ), fmaf(R.rs[1], R.rcp[1], (float)tX),
                      fmaf(R.rs[2], R.rcp[2], (float)tY));
     f3 pb = mv(R.MKi, rv);
     pb = mk(pb.x + 0.5f, pb.y + 0.5f, pb.z + 0.5f);
     if (pb.x < 0.f || pb.y < 0.f || pb.z < 0.f || pb.x >= (float)G.gd[0] || pb.y >= (float)G.gd[1] ||
         pb.z >= (float)G.gd[2])
-        return;
-    const int px = __float2int_rd(__fdiv_rn(pb.x, (float)G.pd[0]));
-    const int pz = __float2int_rd(__fdiv_rn(pb.z, (float)G.pd[2]));
-    const int pidx = px + pz * G.npx;
-    if (pidx >= G.n) return;
-    f3 ip = mk(fmodf(pb.x, (float)G.pd[0]), fmodf(pb.y, (float)G.pd[1]), fmodf(pb.z, (float)G.pd[2]));
-    if (ip.x < (float)BL_WALL || ip.y < (float)BL_WALL || ip.z < (float)BL_WALL) return;
+        return false;
+    const float qx = floorf(__fdiv_rn(pb.x, (float)G.pd[0])), qz = floorf(__fdiv_rn(pb.z, (float)G.pd[2]));
+    pidx = (int)qx + (int)qz * G.npx;
+    if (pidx >= G.n) return false;
+    // pb.y < pd.y + wall: fmodf(pb.y, pd.y) is pb.y or pb.y - pd.y (exact)
+    const float py = pb.y >= (float)G.pd[1] ? pb.y - (float)G.pd[1] : pb.y;
+    ip = mk(fmod_int(pb.x, (float)G.pd[0], qx), py, fmod_int(pb.z, (float)G.pd[2], qz));
+    if (ip.x < (float)BL_WALL || ip.y < (float)BL_WALL || ip.z < (float)BL_WALL) return false;
     ip = mk(ip.x - 0.5f, ip.y - 0.5f, ip.z - 0.5f);
-    const BlPillar& Q = pil[pidx];
-    // density at the sample (pillar index scaled, rotated, + start)
-    const f3 gd = mv(Q.M, mk(ip.x * G.vs[0], ip.y * G.vs[1], ip.z * G.vs[2]));
-    const f3 g = mk(gd.x + Q.ps[0], gd.y + Q.ps[1], gd.z + Q.ps[2]);
-    rho = tex3D<float>(P.dens_tex, __fdiv_rn(g.x - P.start[0], P.voxel[0]) + 0.5f,
-                       __fdiv_rn(g.y - P.start[1], P.voxel[1]) + 0.5f, __fdiv_rn(g.z - P.start[2], P.voxel[2]) + 0.5f);
-    // TERMA at the sample (pillar index rotated, then scaled, + start), only
-    // from this pillar's beamlet
-    const f3 tr = mv(Q.M, ip);
-    const f3 gt = mk(fmaf(tr.x, G.vs[0], Q.ps[0]), fmaf(tr.y, G.vs[1], Q.ps[1]), fmaf(tr.z, G.vs[2], Q.ps[2]));
-    int bl = beamlet_of(S, gt);
-    if (bl == -2) bl = beamlet_point_fp64(S, (double)gt.x, (double)gt.y, (double)gt.z);
-    if (bl != Q.fidx) return;
-    const float f = __ldg(fluence + bl);
-    if (!(f > 0.f)) return;
-    const f3 src = ld3(S.src);
-    const float rpl = siddon_rpl(P, gt, src, cap);
-    T = f * terma_per_fluence(P, rpl, gt, src, S.sad);
+    return true;
 }
 
+// TERMA point of a sample: pillar index rotated, then scaled, + start
+__device__ __forceinline__ f3 bl_terma_point(const BlGrid& G, const BlPillar& Q, f3 ip) {
+    const f3 tr = mv(Q.M, ip);
+    return mk(fmaf(tr.x, G.vs[0], Q.ps[0]), fmaf(tr.y, G.vs[1], Q.ps[1]), fmaf(tr.z, G.vs[2], Q.ps[2]));
+}
+
+constexpr int BL_SAMPLE_BLOCK = 256;
+
+// Can pillar-index point ip lie in the pillar's beamlet?  The footprint's
+// cross-section at pillar depth y is inside the box spanned by its four
+// corner rays there (a rotation keeps rays straight); 0.05 index units of
+// margin keep every point the exact test could accept.
+__device__ __forceinline__ bool bl_near_footprint(const BlPillar& Q, f3 ip) {
+    float x0 = 1e30f, x1 = -1e30f, z0 = 1e30f, z1 = -1e30f;
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        const float x = fmaf(Q.sx[c], ip.y, Q.ex[c]), z = fmaf(Q.sz[c], ip.y, Q.ez[c]);
+        x0 = fminf(x0, x); x1 = fmaxf(x1, x);
+        z0 = fminf(z0, z); z1 = fmaxf(z1, z);
+    }
+    return ip.x >= x0 - 0.05f && ip.x <= x1 + 0.05f && ip.z >= z0 - 0.05f && ip.z <= z1 + 0.05f;
+}
+
+// Pass 1 of a direction, one thread per REV sample (line-contiguous layout):
+// the sample's pillar and the beamlet test of its TERMA point -- the exact
+// test of the reference only near the footprint.  Samples inside their
+// pillar's beamlet are queued for the Siddon pass; nothing else is written
+// (density is sampled later, on the lines that carry TERMA).
+__global__ void __launch_bounds__(BL_SAMPLE_BLOCK)
+    k_bl_samples(EeParams P, const EeBeamSpec* __restrict__ spec, BlGrid G, const BlPillar* __restrict__ pil,
+                 BlRayDev R, int* __restrict__ queue, int* __restrict__ qcount) {
+    // REV arrays stay below 2^31 samples (checked on the host): 32-bit index
+    // arithmetic
+    const unsigned n = (unsigned)R.rev[0] * (unsigned)R.rev[1] * (unsigned)R.rev[2];
+    const unsigned v = blockIdx.x * blockDim.x + threadIdx.x;
+    bool in_beamlet = false;
+    if (v < n) {
+        const unsigned line = v / (unsigned)R.rev[0];
+        const int tX = (int)(v - line * (unsigned)R.rev[0]);
+        const unsigned zq = line / (unsigned)R.rev[1];
+        const int tY = (int)(line - zq * (unsigned)R.rev[1]), tZ = (int)zq;
+        int pidx;
+        f3 ip;
+        if (bl_locate(G, R, tX, tY, tZ, pidx, ip)) {
+            const BlPillar& Q = pil[pidx];
+            if (bl_near_footprint(Q, ip)) {
+                const f3 gt = bl_terma_point(G, Q, ip);
+                int bl = beamlet_of(*spec, gt);
+                if (bl == -2) bl = beamlet_point_fp64(*spec, (double)gt.x, (double)gt.y, (double)gt.z);
+                in_beamlet = bl == Q.fidx;
+            }
+        }
+    }
+    // warp-aggregated enqueue
+    const unsigned m = __ballot_sync(FULL, in_beamlet);
+    if (m) {
+        const int lane = threadIdx.x & 31;
+        int base = 0;
+        if (lane == __ffs(m) - 1) base = atomicAdd(qcount, __popc(m));
+        base = __shfl_sync(FULL, base, __ffs(m) - 1);
+        if (in_beamlet) queue[base + __popc(m & ((1u << lane) - 1u))] = (int)v;
+    }
+}
+
+// Density of a sample (pillar index scaled, rotated, + start; the reference's
+// INVALID -1e-12 for walls / outside).
+__device__ __forceinline__ float bl_density(const EeParams& P, const BlGrid& G, const BlPillar* __restrict__ pil,
+                                            const BlRayDev& R, int tX, int tY, int tZ) {
+    int pidx;
+    f3 ip;
+    if (!bl_locate(G, R, tX, tY, tZ, pidx, ip)) return -1e-12f;
+    const BlPillar& Q = pil[pidx];
+    const f3 gd = mv(Q.M, mk(ip.x * G.vs[0], ip.y * G.vs[1], ip.z * G.vs[2]));
+    const f3 g = mk(gd.x + Q.ps[0], gd.y + Q.ps[1], gd.z + Q.ps[2]);
+    return tex3D<float>(P.dens_tex, __fdiv_rn(g.x - P.start[0], P.voxel[0]) + 0.5f,
+                        __fdiv_rn(g.y - P.start[1], P.voxel[1]) + 0.5f, __fdiv_rn(g.z - P.start[2], P.voxel[2]) + 0.5f);
+}
+
+// Pass 2: Siddon radiological path + polyenergetic TERMA of every queued
+// sample (one thread each, so the ray traces run lane-dense), and the flag
+// of the sample's line.
+__global__ void __launch_bounds__(256)
+    k_bl_terma(EeParams P, const EeBeamSpec* __restrict__ spec, BlGrid G, const BlPillar* __restrict__ pil,
+               BlRayDev R, const float* __restrict__ fluence, const int* __restrict__ queue,
+               const int* __restrict__ qcount, float* __restrict__ t_out, unsigned char* __restrict__ line_flag,
+               int* __restrict__ status) {
+    const int nq = *qcount;
+    const EeBeamSpec& S = *spec;
+    const f3 src = ld3(S.src);
+    bool cap = false;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
+        const unsigned v = (unsigned)queue[q];
+        const unsigned line = v / (unsigned)R.rev[0];
+        const int tX = (int)(v - line * (unsigned)R.rev[0]);
+        const unsigned zq = line / (unsigned)R.rev[1];
+        const int tY = (int)(line - zq * (unsigned)R.rev[1]), tZ = (int)zq;
+        int pidx;
+        f3 ip;
+        if (!bl_locate(G, R, tX, tY, tZ, pidx, ip)) continue;
+        const BlPillar& Q = pil[pidx];
+        const f3 gt = bl_terma_point(G, Q, ip);
+        const float f = __ldg(fluence + Q.fidx);
+        if (!(f > 0.f)) continue;
+        const float rpl = siddon_rpl(P, gt, src, cap);
+        t_out[v] = f * terma_per_fluence(P, rpl, gt, src, S.sad);
+        line_flag[line] = 1;
+    }
+    if (cap) atomicOr(status, 1);
+}
+
+// Cumulative kernel at radiological distance r as PackRowConvolve reads it:
+// first mean radius >= r, texture-filtered between the two table entries
+// (device.cu:326-339).
+__device__ __forceinline__ float bl_ck(const float* K, const float* KR, int nr, float r) {
+    int lo = 0, hi = nr - 1;  // first index with KR[idx] >= r (r <= KR[nr-1])
+    while (lo < hi) {
+        const int m = (lo + hi) >> 1;
+        if (KR[m] < r) lo = m + 1;
+        else hi = m;
+    }
+    if (lo <= 0) return kern_tex(K, nr, 0.5f) * (r * (1.f / KR[0]));
+    const float interp = (r - KR[lo - 1]) * (1.f / (KR[lo] - KR[lo - 1]));
+    return kern_tex(K, nr, (float)lo - 0.5f + interp);
+}
+
+constexpr int BL_MAX_SRC = 1024;
+
+// Pass 3, one warp per flagged line (lines without TERMA keep the zeros the
+// dose array was cleared to).  The reference's walk from output i visits
+// every sample up to the next wall, adding T_k * (CK(s_k) - CK(s_k')) where
+// s_k is the radiological distance between the centres of i and k (half of
+// i's own step for k = i) and s_k' that of the previous sample; only samples
+// with TERMA contribute.  Here each lane sums those terms directly over the
+// line's TERMA samples in i's wall-bounded segment, with the distances from
+// a prefix sum of the radiological steps, under the walk's stopping rules
+// (the last radius for s_k, the one before it for s_k').
 __global__ void __launch_bounds__(BL_WARPS * 32)
-    k_bl_cone(EeParams P, const EeBeamSpec* __restrict__ spec, BlGrid G, const BlPillar* __restrict__ pil,
-              BlRayDev R, const float* __restrict__ fluence, float* __restrict__ rev_dose, int* __restrict__ status) {
+    k_bl_walk(EeParams P, BlGrid G, const BlPillar* __restrict__ pil, BlRayDev R, const float* __restrict__ t_in,
+              const unsigned char* __restrict__ line_flag, float* __restrict__ rev_dose) {
     extern __shared__ float sm[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int L = R.rev[0];
+    const int nr = P.nradii;
     float* Kf = sm;
     float* Kr = Kf + EE_MAX_RADII;
     float* KR = Kr + EE_MAX_RADII;
-    for (int k = threadIdx.x; k < P.nradii; k += blockDim.x) {
-        Kf[k] = P.cumkern[R.row_f * P.nradii + k];
-        Kr[k] = P.cumkern[R.row_r * P.nradii + k];
+    for (int k = threadIdx.x; k < nr; k += blockDim.x) {
+        Kf[k] = P.cumkern[R.row_f * nr + k];
+        Kr[k] = P.cumkern[R.row_r * nr + k];
         KR[k] = G.kr[k];
     }
     __syncthreads();
     const long long line = (long long)blockIdx.x * BL_WARPS + warp;
-    if (line >= (long long)R.rev[1] * R.rev[2]) return;
+    if (line >= (long long)R.rev[1] * R.rev[2] || !line_flag[line]) return;
+    // per warp: d[L] (radiological step, -1 for walls), pre[L+1] (prefix of
+    // steps), seg[L] (wall count before the sample), src[BL_MAX_SRC]
+    float* d = sm + 3 * EE_MAX_RADII + (size_t)warp * (3 * L + 2 + BL_MAX_SRC);
+    float* pre = d + L;
+    int* seg = (int*)(pre + L + 1);
+    int* src = seg + L;
     const int tY = (int)(line % R.rev[1]), tZ = (int)(line / R.rev[1]);
-    float* rho = sm + 3 * EE_MAX_RADII + (size_t)warp * 2 * L;
-    float* T = rho + L;
-    const EeBeamSpec& S = *spec;
-    bool cap = false, any = false;
-    for (int i = lane; i < L; i += 32) {
-        float r, t;
-        bl_sample(P, S, G, pil, R, fluence, i, tY, tZ, r, t, cap);
-        rho[i] = r;
-        T[i] = t;
-        any |= t != 0.f;
-    }
-    if (__any_sync(FULL, cap) && lane == 0) atomicOr(status, 1);
-    float* out = rev_dose + (size_t)line * L;
-    if (!__any_sync(FULL, any)) {
-        for (int i = lane; i < L; i += 32) out[i] = 0.f;
-        return;
-    }
-    __syncwarp();
+    const float* tl = t_in + (size_t)line * L;
     const float delr = P.lng;
-    const float nphi = (float)P.nphi;
-    for (int i = lane; i < L; i += 32) {
-        float d = 0.f;
-        if (!(rho[i] < 0.f)) {
-            float s = bl_walk(rho, T, L, i, -1, Kf, KR, P.nradii, delr, 0.f);
-            s = bl_walk(rho, T, L, i, +1, Kr, KR, P.nradii, delr, s);
-            d = s / nphi;
+    // prefix sums (steps of walls count 0) and the TERMA-sample list, in
+    // ascending order, 32 samples at a time
+    float carry = 0.f;
+    int wcarry = 0, ns = 0;
+    for (int i0 = 0; i0 < L; i0 += 32) {
+        const int i = i0 + lane;
+        const float rho = i < L ? bl_density(P, G, pil, R, i, tY, tZ) : 0.f;
+        const bool wall = i < L && rho < 0.f;
+        const float step = (i < L && !wall) ? delr * rho : 0.f;
+        float x = step;
+        int w = wall ? 1 : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            const float y = __shfl_up_sync(FULL, x, o);
+            const int wy = __shfl_up_sync(FULL, w, o);
+            if (lane >= o) { x += y; w += wy; }
         }
-        out[i] = d;
+        if (i < L) {
+            d[i] = wall ? -1.f : step;
+            pre[i + 1] = carry + x;
+            seg[i] = wcarry + w - (wall ? 1 : 0);
+        }
+        const bool is_src = i < L && !wall && tl[i] != 0.f;
+        const unsigned m = __ballot_sync(FULL, is_src);
+        if (is_src) {
+            const int p = ns + __popc(m & ((1u << lane) - 1u));
+            if (p < BL_MAX_SRC) src[p] = i;
+        }
+        ns += __popc(m);
+        carry = __shfl_sync(FULL, carry + x, 31);
+        wcarry = __shfl_sync(FULL, wcarry + w, 31);
+    }
+    if (lane == 0) pre[0] = 0.f;
+    ns = min(ns, BL_MAX_SRC);
+    __syncwarp();
+    const float rmax = KR[nr - 1], rstop = KR[nr - 2];
+    const float nphi = (float)P.nphi;
+    float* out = rev_dose + (size_t)line * L;
+    for (int i = lane; i < L; i += 32) {
+        const float di = d[i];
+        if (di < 0.f) continue;  // wall: stays 0
+        const float h = 0.5f * di;
+        const int si = seg[i];
+        float sum = 0.f;
+        // backward walk (kernel row P): sources k <= i
+        for (int q = 0; q < ns; q++) {
+            const int k = src[q];
+            if (k > i) break;
+            if (seg[k] != si) continue;
+            const float tk = tl[k];
+            if (k == i) {
+                if (h <= rmax) sum += bl_ck(Kf, KR, nr, h) * tk;
+                continue;
+            }
+            const float sk = h + (pre[i] - pre[k + 1]) + 0.5f * d[k];
+            const float sp = (k + 1 == i) ? h : h + (pre[i] - pre[k + 2]) + 0.5f * d[k + 1];
+            if (sk > rmax || sp > rstop) continue;
+            sum += (bl_ck(Kf, KR, nr, sk) - bl_ck(Kf, KR, nr, sp)) * tk;
+        }
+        // forward walk (kernel row ntheta-1-P): sources k >= i
+        for (int q = ns - 1; q >= 0; q--) {
+            const int k = src[q];
+            if (k < i) break;
+            if (seg[k] != si) continue;
+            const float tk = tl[k];
+            if (k == i) {
+                if (h <= rmax) sum += bl_ck(Kr, KR, nr, h) * tk;
+                continue;
+            }
+            const float sk = h + (pre[k] - pre[i + 1]) + 0.5f * d[k];
+            const float sp = (k - 1 == i) ? h : h + (pre[k - 1] - pre[i + 1]) + 0.5f * d[k - 1];
+            if (sk > rmax || sp > rstop) continue;
+            sum += (bl_ck(Kr, KR, nr, sk) - bl_ck(Kr, KR, nr, sp)) * tk;
+        }
+        out[i] = sum / nphi;
     }
 }
 
@@ -355,12 +513,13 @@ __device__ __forceinline__ float tri_border_q(const float* __restrict__ v, int n
 // fastest, then pZ, then pX.
 __global__ void __launch_bounds__(256) k_bl_gather(BlGrid G, BlRayDev R, const float* __restrict__ rev_dose,
                                                    float* __restrict__ packed) {
-    const long long n = (long long)G.gd[0] * G.gd[1] * G.gd[2];
-    const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned n = (unsigned)G.gd[0] * (unsigned)G.gd[1] * (unsigned)G.gd[2];
+    const unsigned v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= n) return;
-    const int pY = (int)(v % G.gd[1]);
-    const long long r2 = v / G.gd[1];
-    const int pZ = (int)(r2 % G.gd[2]), pX = (int)(r2 / G.gd[2]);
+    const unsigned r2 = v / (unsigned)G.gd[1];
+    const int pY = (int)(v - r2 * (unsigned)G.gd[1]);
+    const unsigned r3 = r2 / (unsigned)G.gd[2];
+    const int pZ = (int)(r2 - r3 * (unsigned)G.gd[2]), pX = (int)r3;
     const f3 rot = mv(R.MK, mk((float)pX, (float)pY, (float)pZ));
     const float qx = fmaf(-R.rs[0], R.rcp[0], rot.x), qy = fmaf(-R.rs[1], R.rcp[1], rot.y),
                 qz = fmaf(-R.rs[2], R.rcp[2], rot.z);
@@ -608,7 +767,9 @@ struct Dev {
 
 struct BlWork {
     Dev<EeBeamSpec> spec;
-    Dev<float> fluence, revd, packed, vals, out_vals;
+    Dev<float> fluence, revd, terma, packed, vals, out_vals;
+    Dev<unsigned char> line_flag;
+    Dev<int> queue, qcount;
     Dev<BlPillar> pil;
     Dev<int> len, xs, cnt, colmax, status, out_rows, out_bidx;
     Dev<long long> seg, off, out_colptr;
@@ -616,7 +777,8 @@ struct BlWork {
     long long nnz = 0;
     int ncols = 0;
     void release() {
-        spec.release(); fluence.release(); revd.release(); packed.release(); vals.release(); out_vals.release();
+        spec.release(); fluence.release(); revd.release(); terma.release(); line_flag.release();
+        queue.release(); qcount.release(); packed.release(); vals.release(); out_vals.release();
         pil.release(); len.release(); xs.release(); cnt.release(); colmax.release(); status.release();
         out_rows.release(); out_bidx.release(); seg.release(); off.release(); out_colptr.release();
         for (auto& t : scan_tmp) t.release();
@@ -841,6 +1003,30 @@ int ee_beamlet_run(const EeParams& P, const EeRayConst* rays, cudaStream_t s, vo
             std::memcpy(Q.Mi, &Mis[9 * gi], sizeof(Q.Mi));
             Q.ps[0] = pstart[gi].x; Q.ps[1] = pstart[gi].y; Q.ps[2] = pstart[gi].z;
             Q.fidx = bl[gi].fidx;
+            {
+                // corner rays of the beamlet's fluence-map cell in pillar
+                // index coordinates, ip = Mi ((p - ps) / vs)
+                const int bx = Q.fidx % fx, by = Q.fidx / fx;
+                const v3 ps = pstart[gi];
+                auto to_pil = [&](v3 p) {
+                    const v3 q = (p - ps) * v3{1.f / vs.x, 1.f / vs.y, 1.f / vs.z};
+                    const float* Mi = Q.Mi;
+                    return v3{Mi[0] * q.x + Mi[1] * q.y + Mi[2] * q.z, Mi[3] * q.x + Mi[4] * q.y + Mi[5] * q.z,
+                              Mi[6] * q.x + Mi[7] * q.y + Mi[8] * q.z};
+                };
+                const v3 a = to_pil(src);
+                for (int c = 0; c < 4; c++) {
+                    const float cx = beam.beamlet_size[0] * (-0.5f * fx + bx + (c & 1));
+                    const float cz = beam.beamlet_size[1] * (-0.5f * fy + by + (c >> 1));
+                    const v3 corner = iso + inv_rot_beam({cx, 0.f, cz}, az, zen, coll);
+                    const v3 e = to_pil(corner) - a;
+                    const float sy = std::fabs(e.y) > 1e-12f ? e.y : 1e-12f;
+                    Q.sx[c] = e.x / sy;
+                    Q.sz[c] = e.z / sy;
+                    Q.ex[c] = a.x - Q.sx[c] * a.y;
+                    Q.ez[c] = a.z - Q.sz[c] * a.y;
+                }
+            }
             Q.ix = i % G.npx;
             Q.iz = i / G.npx;
             double lo[3] = {1e30, 1e30, 1e30}, hi[3] = {-1e30, -1e30, -1e30};
@@ -873,7 +1059,17 @@ int ee_beamlet_run(const EeParams& P, const EeRayConst* rays, cudaStream_t s, vo
         long long rmax = 1;
         for (int r = 0; r < nrays; r++)
             rmax = std::max(rmax, (long long)revs[k][r].size[0] * revs[k][r].size[1] * revs[k][r].size[2]);
+        if (rmax >= (1ll << 31) || npk >= (1ll << 31))
+            return ee_internal_fail(EE_ERR_REV_SIZE, "beamlet REV / packed grid exceeds 2^31 samples");
         BL_CUDA(W.revd.ensure(rmax));
+        BL_CUDA(W.terma.ensure(rmax));
+        BL_CUDA(W.queue.ensure(rmax));
+        BL_CUDA(W.qcount.ensure(1));
+        {
+            long long lmax = 1;
+            for (int r = 0; r < nrays; r++) lmax = std::max(lmax, (long long)revs[k][r].size[1] * revs[k][r].size[2]);
+            BL_CUDA(W.line_flag.ensure(lmax));
+        }
         // per direction: REV lines, then the gather into the packed grid
         for (int r = 0; r < nrays; r++) {
             const RevBox& RB = revs[k][r];
@@ -888,9 +1084,22 @@ int ee_beamlet_run(const EeParams& P, const EeRayConst* rays, cudaStream_t s, vo
             R.row_r = P.ntheta - kw - 1;
             const long long lines = (long long)R.rev[1] * R.rev[2];
             if (lines == 0 || R.rev[0] == 0) continue;
-            const size_t smem = sizeof(float) * (3 * EE_MAX_RADII + (size_t)BL_WARPS * 2 * R.rev[0]);
-            k_bl_cone<<<(unsigned)((lines + BL_WARPS - 1) / BL_WARPS), BL_WARPS * 32, smem, s>>>(
-                P, W.spec.p, G, W.pil.p, R, W.fluence.p, W.revd.p, W.status.p);
+            const long long nsamp = (long long)R.rev[0] * lines;
+            BL_CUDA(cudaMemsetAsync(W.revd.p, 0, sizeof(float) * nsamp, s));
+            BL_CUDA(cudaMemsetAsync(W.terma.p, 0, sizeof(float) * nsamp, s));
+            BL_CUDA(cudaMemsetAsync(W.line_flag.p, 0, (size_t)lines, s));
+            BL_CUDA(cudaMemsetAsync(W.qcount.p, 0, sizeof(int), s));
+            k_bl_samples<<<(unsigned)((nsamp + BL_SAMPLE_BLOCK - 1) / BL_SAMPLE_BLOCK), BL_SAMPLE_BLOCK, 0, s>>>(
+                P, W.spec.p, G, W.pil.p, R, W.queue.p, W.qcount.p);
+            BL_CUDA(cudaGetLastError());
+            k_bl_terma<<<152 * 8, 256, 0, s>>>(P, W.spec.p, G, W.pil.p, R, W.fluence.p, W.queue.p, W.qcount.p,
+                                               W.terma.p, W.line_flag.p, W.status.p);
+            BL_CUDA(cudaGetLastError());
+            const size_t smem = sizeof(float) * (3 * EE_MAX_RADII + (size_t)BL_WARPS * (3 * R.rev[0] + 2 + BL_MAX_SRC));
+            if (smem > 48 * 1024)
+                BL_CUDA(cudaFuncSetAttribute(k_bl_walk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            k_bl_walk<<<(unsigned)((lines + BL_WARPS - 1) / BL_WARPS), BL_WARPS * 32, smem, s>>>(
+                P, G, W.pil.p, R, W.terma.p, W.line_flag.p, W.revd.p);
             BL_CUDA(cudaGetLastError());
             k_bl_gather<<<(unsigned)((npk + 255) / 256), 256, 0, s>>>(G, R, W.revd.p, W.packed.p);
             BL_CUDA(cudaGetLastError());
