@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--serve-rate", type=float, default=50.0)
     ap.add_argument("--serve-slots", type=int, default=2)
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--beamlet-beams", type=int, default=3)
+    ap.add_argument("--no-beamlet", action="store_true")
     return ap.parse_args()
 
 
@@ -134,6 +136,34 @@ def make_workload(n_beams, seed_offset=0):
     phys = inputs.make_physics(seed=0, spacing_cm=0.2)
     beams = inputs.candidate_beams(n_beams, seed=3 + seed_offset)
     return vol, phys, beams
+
+
+def beamlet_leg(args, eng):
+    """Beamlet dose columns (ee_beamlet_columns_device): beams of the 4-pi
+    candidate grid with 40x40 unit-weight beamlets of 2.5 mm, each column
+    thresholded at 1e-4 of its maximum into FP32 CSR with int32 row indices
+    (device-resident).  Host clock around each call (the call synchronises)."""
+    from endtoend_gb300 import inputs
+    angs = inputs.four_pi_angles(1162, seed=5)
+    pick = np.linspace(0, len(angs) - 1, max(1, args.beamlet_beams)).round().astype(int)
+    beams = []
+    for g, c in angs[pick]:
+        b = inputs.single_beam(fmap=(40, 40), beamlet_cm=0.25, gantry_deg=float(g), couch_deg=float(c))
+        b.fluence = np.ones((40, 40), np.float32)
+        beams.append(b)
+    eng.beamlet_columns_device(beams[0], 1e-4)  # warm-up (workspace growth)
+    nbl, nnz, t = 0, 0, 0.0
+    for b in beams:
+        t0 = time.perf_counter()
+        d = eng.beamlet_columns_device(b, 1e-4)
+        t += time.perf_counter() - t0
+        nbl += d.nbeamlets
+        nnz += d.nnz
+    out_bytes = nnz * 8 + (nbl + len(beams)) * 8
+    return {"workload": f"{len(beams)} beams of the 1162-beam 4-pi grid, 200x200x160 @2mm head-neck phantom, "
+                        "40x40 beamlets of 2.5 mm, threshold 1e-4 of each column max, FP32 CSR + int32 rows",
+            "beamlets": nbl, "seconds": t, "beamlets_per_s": nbl / t, "nnz_per_beamlet": nnz / max(nbl, 1),
+            "output_gb_per_s": out_bytes / t / 1e9}
 
 
 def serving_leg(args, device, phys):
@@ -457,6 +487,11 @@ def main():
         cpu = {"value": 1.0 / t_cpu, "unit": UNIT, "cores": cores, "kind": "port",
                "sample": "1 beam forward + adjoint (FP32 OpenMP restatement, 24-radius table walk)"}
 
+    beamlet = None
+    if not args.no_beamlet and rank == 0:
+        eng.synchronize()
+        beamlet = beamlet_leg(args, eng)
+
     serving = None
     if not args.no_serve and rank == 0:
         eng.synchronize()
@@ -482,6 +517,7 @@ def main():
             "pipeline": {"value": pipeline_value, "unit": UNIT, "note": "same batch, direct call (host geometry read-back per chunk)"},
             "plan": plan_info,
             "serving": serving,
+            "beamlet": beamlet,
             "gpu_launches": gpu_launches,
             "roofline": roof,
             "clocks": clk,
