@@ -230,11 +230,16 @@ def serving_leg(args, device, phys):
     tickets = []
     done = threading.Event()
 
+    failed = []
+
     def waiter():
         i = 0
         while not (done.is_set() and i >= len(tickets)):
             if i < len(tickets):
-                srv.wait(tickets[i])
+                try:
+                    srv.wait(tickets[i])
+                except engine.EEError as e:
+                    failed.append(str(e))
                 i += 1
             else:
                 time.sleep(0.001)
@@ -258,7 +263,7 @@ def serving_leg(args, device, phys):
                     + " @2mm, 1-40 beams, fluence 16^2-64^2 @2.5mm, dose or dose+gradient",
         "beams": nbeams, "slots": args.serve_slots,
         "served": {"beams_per_s": nbeams / makespan, "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
-                   "completed": st["completed"], "makespan_s": makespan},
+                   "completed": st["completed"], "failed": len(failed), "makespan_s": makespan},
         "plain": plain,
         "served_over_plain": (nbeams / makespan) / plain["beams_per_s"],
     }
@@ -492,9 +497,13 @@ def main():
         eng.synchronize()
         beamlet = beamlet_leg(args, eng)
 
+    # the request server runs on its own contexts: release the batch's
+    # buffers first
+    eng.synchronize()
+    plan.close()
+    eng.close()
     serving = None
     if not args.no_serve and rank == 0:
-        eng.synchronize()
         serving = serving_leg(args, local, phys)
 
     lat_ms = np.array(lat) * 1e3
@@ -525,8 +534,6 @@ def main():
             "cpu_baseline": cpu,
         }
         print(json.dumps(line), flush=True)
-    plan.close()
-    eng.close()
 
 
 if __name__ == "__main__":

@@ -65,6 +65,7 @@ struct SlotCtx {
     ee_context* ctx = nullptr;
     Clock::time_point last_use;
     long long bytes = 0;  // device bytes after its last batch
+    bool busy = false;    // pinned by a batch being admitted or computed
 };
 
 struct Slot {
@@ -74,6 +75,7 @@ struct Slot {
     size_t pin_n = 0;
     float* dbuf = nullptr;
     size_t dbuf_n = 0;
+    long long dbuf_bytes = 0;  // device staging held (read under the server lock)
 };
 
 }  // namespace
@@ -114,19 +116,21 @@ int set_physics(ee_server* S, ee_context* c) {
 // device bytes held by every slot's contexts plus admitted batches (S->mu held)
 long long bytes_in_use(ee_server* S) {
     long long b = S->reserved;
-    for (auto& sl : S->slots)
+    for (auto& sl : S->slots) {
+        b += sl->dbuf_bytes;
         for (auto& kv : sl->ctxs) b += kv.second.bytes;
+    }
     return b;
 }
 
 // upper bound of what a batch adds: staging (fluence, dose and gradient
 // volumes, in and out) and the growth of the volume's context up to
 // resident data (density + texture + TERMA boxes) plus its scratch limit
-long long batch_need(ee_server* S, const Volume& V, long long ctx_now, long long nfl, int ngroups, int nbeams,
-                     bool grad) {
+long long batch_need(ee_server* S, const Volume& V, long long ctx_now, long long staging_now, long long nfl,
+                     int ngroups, int nbeams, bool grad) {
     const long long nv = V.nvox();
     const long long bbox = (long long)V.frame.bbox_size[0] * V.frame.bbox_size[1] * V.frame.bbox_size[2];
-    const long long staging = 4ll * (2 * nfl + nv * ngroups * (grad ? 2 : 1));
+    const long long staging = std::max(0ll, 4ll * (2 * nfl + nv * ngroups * (grad ? 2 : 1)) - staging_now);
     const long long ctx_after = 12ll * nv + 12ll * bbox * nbeams + S->slot_scratch;
     return staging + std::max(0ll, ctx_after - ctx_now);
 }
@@ -159,6 +163,7 @@ void settle(ee_server* S, SlotCtx& sc, long long need) {
     S->reserved -= need;
     sc.bytes = b;
     sc.last_use = Clock::now();
+    sc.busy = false;
 }
 
 void run_batch(ee_server* S, Slot& slot, std::vector<std::shared_ptr<Request>>& batch) {
@@ -173,29 +178,38 @@ void run_batch(ee_server* S, Slot& slot, std::vector<std::shared_ptr<Request>>& 
         nb += (int)r->beams.size();
         nfl += (long long)r->fluence.size();
     }
-    // admission: the batch's footprint within the HBM budget, evicting this
-    // slot's least recently used contexts of other volumes first
+    // admission: the batch's footprint within the HBM budget, evicting the
+    // least recently used idle contexts (of any slot) first; this slot's
+    // context of the volume is pinned meanwhile
     long long need = 0;
+    std::map<int, SlotCtx>::iterator it;
+    bool have_ctx = false;
     {
         std::unique_lock<std::mutex> lk(S->mu);
         auto deadline = Clock::now() + std::chrono::seconds(120);
         for (;;) {
-            auto cur = slot.ctxs.find(vol_id);
-            need = batch_need(S, V, cur == slot.ctxs.end() ? 0 : cur->second.bytes, nfl, ng, nb, grad);
+            it = slot.ctxs.find(vol_id);
+            have_ctx = it != slot.ctxs.end();
+            if (have_ctx) it->second.busy = true;
+            need = batch_need(S, V, have_ctx ? it->second.bytes : 0, slot.dbuf_bytes, nfl, ng, nb, grad);
             if (bytes_in_use(S) + need <= S->budget) break;
+            Slot* vs = nullptr;
             int victim = -1;
             Clock::time_point oldest = Clock::time_point::max();
-            for (auto& kv : slot.ctxs)
-                if (kv.first != vol_id && kv.second.last_use < oldest) {
-                    oldest = kv.second.last_use;
-                    victim = kv.first;
-                }
-            if (victim >= 0) {
-                ee_destroy(slot.ctxs[victim].ctx);
-                slot.ctxs.erase(victim);
+            for (auto& sl : S->slots)
+                for (auto& kv : sl->ctxs)
+                    if (!kv.second.busy && kv.second.last_use < oldest) {
+                        oldest = kv.second.last_use;
+                        victim = kv.first;
+                        vs = sl.get();
+                    }
+            if (vs) {
+                ee_destroy(vs->ctxs[victim].ctx);
+                vs->ctxs.erase(victim);
                 continue;
             }
             if (S->reserved == 0 || Clock::now() > deadline) {
+                if (have_ctx) it->second.busy = false;
                 lk.unlock();
                 finish(S, batch, EE_ERR_NOMEM, "request does not fit the server's HBM budget");
                 return;
@@ -204,8 +218,7 @@ void run_batch(ee_server* S, Slot& slot, std::vector<std::shared_ptr<Request>>& 
         }
         S->reserved += need;
     }
-    auto it = slot.ctxs.find(vol_id);
-    if (it == slot.ctxs.end()) {
+    if (!have_ctx) {
         ee_context* c = nullptr;
         int st = ee_create(S->device, &c);
         if (!st) st = ee_set_volume(c, &V.frame, V.density.data());
@@ -219,7 +232,7 @@ void run_batch(ee_server* S, Slot& slot, std::vector<std::shared_ptr<Request>>& 
             return;
         }
         std::lock_guard<std::mutex> lk(S->mu);
-        it = slot.ctxs.emplace(vol_id, SlotCtx{c, Clock::now(), 0}).first;
+        it = slot.ctxs.emplace(vol_id, SlotCtx{c, Clock::now(), 0, true}).first;
     }
     SlotCtx& sc = it->second;
     ee_context* c = sc.ctx;
@@ -248,6 +261,8 @@ void run_batch(ee_server* S, Slot& slot, std::vector<std::shared_ptr<Request>>& 
         slot.dbuf_n = 0;
         if (cudaMalloc((void**)&slot.dbuf, n_dev * sizeof(float)) != cudaSuccess) return fail_batch(EE_ERR_NOMEM, "device staging");
         slot.dbuf_n = n_dev;
+        std::lock_guard<std::mutex> lk(S->mu);
+        slot.dbuf_bytes = (long long)(n_dev * sizeof(float));
     }
     std::vector<ee_beam> beams;
     std::vector<int> group;
