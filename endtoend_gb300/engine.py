@@ -89,6 +89,18 @@ class BeamInfo(C.Structure):
                 ("status", C.c_int)]
 
 
+class AnnealParams(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("step_size", C.c_float), ("sigma_deg", C.c_float),
+                ("temperature", C.c_float), ("cooling", C.c_float), ("fluence_steps", C.c_int),
+                ("seed", C.c_ulonglong)]
+
+
+class AnnealRecord(C.Structure):
+    _fields_ = [("zenith", C.c_void_p), ("azimuth", C.c_void_p), ("perturbation_loss", C.c_void_p),
+                ("possibility", C.c_void_p), ("taken", C.c_void_p), ("dose_loss", C.c_void_p),
+                ("smoothness_loss", C.c_void_p)]
+
+
 class Csr(C.Structure):
     _fields_ = [("nbeamlets", C.c_int), ("nnz", C.c_longlong), ("beamlet_index", C.c_void_p), ("col_ptr", C.c_void_p),
                 ("row_index", C.c_void_p), ("value", C.c_void_p)]
@@ -141,6 +153,12 @@ _SIGS = {
                                      C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_longlong),
                                      C.POINTER(C.c_int)]),
     "ee_copy_to_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_longlong]),
+    "ee_optimize_fluence": (C.c_int, [C.c_void_p, C.POINTER(EEBeam), C.c_int, C.c_void_p, C.POINTER(Loss), C.c_int,
+                                      C.c_float, C.c_void_p, C.c_void_p]),
+    "ee_optimize_annealing": (C.c_int, [C.c_void_p, C.POINTER(EEBeam), C.c_int, C.c_void_p, C.POINTER(Loss),
+                                        C.POINTER(AnnealParams), C.POINTER(AnnealRecord)]),
+    "ee_evaluate_proposals": (C.c_int, [C.c_void_p, C.POINTER(EEBeam), C.c_int, C.c_int, C.c_void_p, C.POINTER(Loss),
+                                        C.POINTER(C.c_double)]),
     "ee_server_create": (C.c_int, [C.c_int, C.c_int, C.c_longlong, C.c_int, C.POINTER(C.c_void_p)]),
     "ee_server_set_physics": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                         C.POINTER(ConvParams), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
@@ -315,6 +333,56 @@ class Engine:
         self._check(self.lib.ee_dose_and_adjoint_device(self.h, eb, len(beams), C.c_void_p(d_fluence),
                                                         C.c_void_p(d_dose or 0), mode, C.c_void_p(d_dose_grad or 0),
                                                         C.c_void_p(d_fluence_grad or 0)))
+
+    @staticmethod
+    def make_loss(ptv=(0, 0), oar=(0, 0), eta: float = 0.0, spread_sigma: float = 0.0) -> Loss:
+        L = Loss()
+        L.ptv_weight, L.ptv_target = ptv
+        L.oar_weight, L.oar_target = oar
+        L.eta, L.spread_sigma = float(eta), float(spread_sigma)
+        return L
+
+    def optimize_fluence(self, beams, d_x: int, loss: Loss, iterations: int, step_size: float):
+        """Projected gradient descent of the fluence (EndtoEnd
+        optimize_stationary_smoothness).  Returns (dose_loss[it],
+        smoothness_loss[it, nbeams])."""
+        eb = to_ee_beams(beams)
+        dl = np.zeros(iterations, np.float32)
+        sl = np.zeros((iterations, len(beams)), np.float32)
+        self._check(self.lib.ee_optimize_fluence(self.h, eb, len(beams), C.c_void_p(d_x), C.byref(loss), int(iterations),
+                                                 float(step_size), _ptr(dl), _ptr(sl)))
+        return dl, sl
+
+    def optimize_annealing(self, beams, d_x: int, loss: Loss, iterations: int, step_size: float = 0.0,
+                           sigma_deg: float = 5.0, temperature: float = 0.0, cooling: float = 1.0,
+                           fluence_steps: int = 1, seed: int = 0):
+        """Simulated annealing of the angles + fluence gradient descent
+        (EndtoEnd optimize_annealing_constrain).  Returns (final
+        (azimuth, zenith) per beam, record dict of the README's arrays)."""
+        n = len(beams)
+        eb = to_ee_beams(beams)
+        p = AnnealParams()
+        p.iterations, p.step_size, p.sigma_deg = int(iterations), float(step_size), float(sigma_deg)
+        p.temperature, p.cooling, p.fluence_steps, p.seed = float(temperature), float(cooling), int(fluence_steps), int(seed)
+        rec = {"zenith": np.zeros((iterations, n, 2), np.float32), "azimuth": np.zeros((iterations, n, 2), np.float32),
+               "perturbation_loss": np.zeros((iterations, n, 2), np.float32),
+               "possibility": np.zeros((iterations, n), np.float32), "taken": np.zeros((iterations, n), np.uint8),
+               "dose_loss": np.zeros(iterations, np.float32), "smoothness_loss": np.zeros((iterations, n), np.float32)}
+        r = AnnealRecord()
+        for k, v in rec.items():
+            setattr(r, k, v.ctypes.data)
+        self._check(self.lib.ee_optimize_annealing(self.h, eb, n, C.c_void_p(d_x), C.byref(loss), C.byref(p),
+                                                   C.byref(r)))
+        return [(eb[b].azimuth, eb[b].zenith) for b in range(n)], rec
+
+    def evaluate_proposals(self, proposals, d_x: int, loss: Loss) -> np.ndarray:
+        """Dose terms of the loss for each proposal (a list of beam lists of
+        equal fluence-map sizes, all sharing the fluence d_x)."""
+        nprop, n = len(proposals), len(proposals[0])
+        eb = to_ee_beams([b for prop in proposals for b in prop])
+        out = (C.c_double * nprop)()
+        self._check(self.lib.ee_evaluate_proposals(self.h, eb, nprop, n, C.c_void_p(d_x), C.byref(loss), out))
+        return np.array(list(out))
 
     def loss_and_grad_device(self, beams, d_x: int, d_dose: int, d_xgrad: int, ptv=(0, 0), oar=(0, 0),
                              eta: float = 0.0, spread_sigma: float = 0.0):

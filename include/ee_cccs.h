@@ -298,6 +298,54 @@ int ee_server_stats(ee_server *server, double *p50_ms, double *p99_ms, long long
 int ee_server_reset_stats(ee_server *server);
 int ee_server_destroy(ee_server *server);
 
+/* ---- fluence and beam-angle optimisation (EndtoEnd) ----
+ * The EndtoEnd programs optimize_stationary_smoothness and
+ * optimize_annealing_constrain (README.md:75-95; their source is not in the
+ * reference snapshot, so these follow the README's description).
+ *
+ * ee_optimize_fluence: `iterations` projected gradient steps
+ * x <- max(x - step_size * dL/dx, 0) on the device fluence d_x (in/out) with
+ * the angles fixed.  dose_loss[iterations] (PTV + OAR terms, before each step)
+ * and smoothness_loss[iterations][nbeams] (eta * ||D x_k||_1 after each step)
+ * may be NULL. */
+int ee_optimize_fluence(ee_context *ctx, const ee_beam *beams, int nbeams, float *d_x, const ee_loss *loss,
+                        int iterations, float step_size, float *dose_loss, float *smoothness_loss);
+typedef struct {
+    int                iterations;
+    float              step_size;      /* fluence gradient step                          */
+    float              sigma_deg;      /* N(0, sigma) perturbation of gantry and couch    */
+    float              temperature;    /* Metropolis temperature (loss units), 0 = greedy */
+    float              cooling;        /* temperature factor per iteration                */
+    int                fluence_steps;  /* gradient steps per iteration                    */
+    unsigned long long seed;
+} ee_anneal_params;
+/* Output arrays, each may be NULL: [iterations][nbeams][2] for zenith,
+ * azimuth and perturbation_loss (the two possibilities: keep, take),
+ * [iterations][nbeams] for possibility (probability of taking) and taken,
+ * [iterations] dose_loss, [iterations][nbeams] smoothness_loss. */
+typedef struct {
+    float         *zenith;
+    float         *azimuth;
+    float         *perturbation_loss;
+    float         *possibility;
+    unsigned char *taken;
+    float         *dose_loss;
+    float         *smoothness_loss;
+} ee_anneal_record;
+/* Simulated annealing of the beam angles + gradient descent of the fluence.
+ * Per iteration every beam gets a proposal (its gantry and couch moved by
+ * N(0, sigma)); all proposals' doses come from one batched call, and the
+ * proposals are accepted beam by beam with probability min(1,
+ * exp(-(L_take - L_keep) / T)) against the running total dose; then
+ * `fluence_steps` gradient steps.  beams (angles) and d_x are updated. */
+int ee_optimize_annealing(ee_context *ctx, ee_beam *beams, int nbeams, float *d_x, const ee_loss *loss,
+                          const ee_anneal_params *params, ee_anneal_record *record);
+/* Batched evaluation of whole-set proposals: proposals[nprop][nbeams]
+ * (same fluence-map sizes in every proposal) share the fluence d_x; losses[q]
+ * = PTV + OAR terms of proposal q's summed dose.  One grouped pipeline call. */
+int ee_evaluate_proposals(ee_context *ctx, const ee_beam *proposals, int nprop, int nbeams, const float *d_x,
+                          const ee_loss *loss, double *losses);
+
 /* ---- diagnostics ---- */
 /* Stage ids for ee_read_profile. */
 #define EE_STAGE_TERMA 0     /* k_terma (+crop-box reduction)           */
