@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--beamlet-beams", type=int, default=3)
     ap.add_argument("--no-beamlet", action="store_true")
+    ap.add_argument("--no-anneal", action="store_true")
     return ap.parse_args()
 
 
@@ -136,6 +137,78 @@ def make_workload(n_beams, seed_offset=0):
     phys = inputs.make_physics(seed=0, spacing_cm=0.2)
     beams = inputs.candidate_beams(n_beams, seed=3 + seed_offset)
     return vol, phys, beams
+
+
+def annealing_leg(args, eng, phys):
+    """Annealing loss (config 2): the head-and-neck phantom with PTV weight 1 /
+    target 1 and three OAR ellipsoids (weights 0.1-0.5, thresholds 0.3-0.6),
+    20 beams of 128x128 fluence pixels of 0.78 mm, Gaussian spread sigma 1.5
+    px, eta 1e-3.  Times ee_loss_and_grad (forward + adjoint of the 20 beams),
+    a batch of 64 proposals (every angle moved by N(0, 5 deg), one grouped
+    call over 1280 beams) and one annealing iteration (20 per-beam proposals,
+    sequential acceptance, one fluence step)."""
+    import torch
+    from endtoend_gb300 import inputs
+    vol = inputs.head_neck_phantom(shape=(200, 200, 160), voxel_cm=0.2, with_oars=True)
+    eng.set_volume(vol)
+    rng = np.random.default_rng(21)
+    ptv = vol.masks["PTV"].astype(np.float32)
+    ow = np.zeros_like(ptv)
+    ot = np.zeros_like(ptv)
+    for k in range(3):
+        m = vol.masks[f"OAR{k}"]
+        ow[m] += rng.uniform(0.1, 0.5)
+        ot[m] = rng.uniform(0.3, 0.6)
+    dv = lambda a: torch.from_numpy(np.ascontiguousarray(a, np.float32).ravel()).cuda()
+    t = {"pw": dv(ptv), "pt": dv(ptv), "ow": dv(ow), "ot": dv(ot)}
+    L = eng.make_loss(ptv=(t["pw"].data_ptr(), t["pt"].data_ptr()), oar=(t["ow"].data_ptr(), t["ot"].data_ptr()),
+                      eta=1e-3, spread_sigma=1.5)
+    beams = []
+    for g, c in inputs.four_pi_angles(20, step_deg=18.0, seed=8):
+        b = inputs.single_beam(fmap=(128, 128), beamlet_cm=0.078, gantry_deg=float(g), couch_deg=float(c))
+        b.fluence = rng.uniform(0.0, 1.0, (128, 128)).astype(np.float32)
+        beams.append(b)
+    x = dv(engine_concat(beams))
+    dose = torch.zeros(vol.nvoxels, device="cuda")
+    grad = torch.zeros_like(x)
+
+    def lg():
+        return eng.loss_and_grad_device(beams, x.data_ptr(), dose.data_ptr(), grad.data_ptr(),
+                                        ptv=(t["pw"].data_ptr(), t["pt"].data_ptr()),
+                                        oar=(t["ow"].data_ptr(), t["ot"].data_ptr()), eta=1e-3, spread_sigma=1.5)
+
+    lg()
+    t0 = time.perf_counter()
+    for _ in range(3):
+        lg()
+    t_lg = (time.perf_counter() - t0) / 3
+    props = []
+    for q in range(64):
+        prop = []
+        for b in beams:
+            c = inputs.Beam(**{**b.__dict__})
+            c.azimuth = b.azimuth + float(rng.normal(0, np.radians(5)))
+            c.zenith = b.zenith + float(rng.normal(0, np.radians(5)))
+            prop.append(c)
+        props.append(prop)
+    eng.evaluate_proposals(props[:2], x.data_ptr(), L)
+    t0 = time.perf_counter()
+    eng.evaluate_proposals(props, x.data_ptr(), L)
+    t_prop = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    eng.optimize_annealing(beams, x.data_ptr(), L, iterations=1, step_size=1e-3, sigma_deg=5.0, temperature=1e-3,
+                           fluence_steps=1, seed=3)
+    t_it = time.perf_counter() - t0
+    return {"workload": "200x200x160 @2mm head-neck phantom, PTV + 3 OARs, 20 beams x 128^2 fluence @0.78 mm, "
+                        "spread sigma 1.5 px, eta 1e-3; 64 proposals of N(0,5 deg) angle moves",
+            "loss_and_grad_ms": t_lg * 1e3, "loss_and_grad_beam_doses_per_s": 20 / t_lg,
+            "proposals_per_s": 64 / t_prop, "proposal_beam_doses_per_s": 64 * 20 / t_prop,
+            "anneal_iteration_s": t_it}
+
+
+def engine_concat(beams):
+    from endtoend_gb300 import engine
+    return engine.concat_fluence(beams)
 
 
 def beamlet_leg(args, eng):
@@ -497,6 +570,12 @@ def main():
         eng.synchronize()
         beamlet = beamlet_leg(args, eng)
 
+    annealing = None
+    if not args.no_anneal and rank == 0:
+        eng.synchronize()
+        plan.close()
+        annealing = annealing_leg(args, eng, phys)
+
     # the request server runs on its own contexts: release the batch's
     # buffers first
     eng.synchronize()
@@ -527,6 +606,7 @@ def main():
             "plan": plan_info,
             "serving": serving,
             "beamlet": beamlet,
+            "annealing": annealing,
             "gpu_launches": gpu_launches,
             "roofline": roof,
             "clocks": clk,
