@@ -549,6 +549,8 @@ __device__ __forceinline__ float sample_rho(const EeParams& P, const EeBeamSpec&
     return tex3D<float>(P.dens_tex, g.x + 0.5f, g.y + 0.5f, g.z + 0.5f);
 }
 
+constexpr int CONE_U = 4;
+
 template <int LANE_BLOCK>
 __global__ void __launch_bounds__(LANE_BLOCK) k_cone_lane(EeParams P, const EeBeamSpec* __restrict__ specs,
                                                           const EeBeamGeom* __restrict__ geoms,
@@ -576,22 +578,36 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_lane(EeParams P, const EeBe
     float2* smp = samples + G.arena_off + R.offset + line;
     const EeRayConst& RC = P.rays[ray];
     const float delr = P.lng;
+    // samples are gathered CONE_U at a time before the recurrence consumes
+    // them, so each lane keeps several independent loads in flight
+    const int iend = i0 + n;
     {   // forward direction: contributions from k < i, kernel row P
         const float* prm = P.expp + 4 * RC.row_fwd;
         const float c1 = prm[0] / prm[1], c2 = prm[2] / prm[3];
         const float e1 = -0.5f * prm[1] * delr, e2 = -0.5f * prm[3] * delr;
         float Y1 = 0.f, Y2 = 0.f, tm = 0.f, hm1 = 1.f, hm2 = 1.f;
-        for (int i = i0; i < i0 + n; i++) {
-            float t;
-            const float r = sample_rho(P, S, G, F, i, tb, t);
-            const bool v = r >= 0.f;
-            const float h1 = v ? __expf(e1 * r) : 1.f, h2 = v ? __expf(e2 * r) : 1.f;
-            if (!v) t = 0.f;
-            smp[i * nl] = make_float2(r, t);
-            out[i * nl] = v ? c1 * (Y1 + tm * (1.f - hm1)) + c2 * (Y2 + tm * (1.f - hm2)) : 0.f;
-            Y1 = fmaf(h1 * h1, Y1, tm * h1 * (1.f - hm1 * h1));
-            Y2 = fmaf(h2 * h2, Y2, tm * h2 * (1.f - hm2 * h2));
-            tm = t; hm1 = h1; hm2 = h2;
+        for (int ib = i0; ib < iend; ib += CONE_U) {
+            float rr[CONE_U], tt[CONE_U];
+#pragma unroll
+            for (int j = 0; j < CONE_U; j++) {
+                rr[j] = -1.f;
+                tt[j] = 0.f;
+                if (ib + j < iend) rr[j] = sample_rho(P, S, G, F, ib + j, tb, tt[j]);
+            }
+#pragma unroll
+            for (int j = 0; j < CONE_U; j++) {
+                const int i = ib + j;
+                if (i >= iend) break;
+                const float r = rr[j];
+                const bool v = r >= 0.f;
+                const float h1 = v ? __expf(e1 * r) : 1.f, h2 = v ? __expf(e2 * r) : 1.f;
+                const float t = v ? tt[j] : 0.f;
+                smp[i * nl] = make_float2(r, t);
+                out[i * nl] = v ? c1 * (Y1 + tm * (1.f - hm1)) + c2 * (Y2 + tm * (1.f - hm2)) : 0.f;
+                Y1 = fmaf(h1 * h1, Y1, tm * h1 * (1.f - hm1 * h1));
+                Y2 = fmaf(h2 * h2, Y2, tm * h2 * (1.f - hm2 * h2));
+                tm = t; hm1 = h1; hm2 = h2;
+            }
         }
     }
     {   // reverse direction: contributions from k > i, kernel row ntheta-1-P
@@ -600,18 +616,32 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_lane(EeParams P, const EeBe
         const float e1 = -0.5f * prm[1] * delr, e2 = -0.5f * prm[3] * delr;
         const float inv_nphi = 1.f / (float)P.nphi;
         float Y1 = 0.f, Y2 = 0.f, tm = 0.f, hm1 = 1.f, hm2 = 1.f;
-        for (int i = i0 + n - 1; i >= i0; i--) {
-            const float2 rt = smp[i * nl];
-            const float r = rt.x;
-            float t = rt.y;
-            const bool v = r >= 0.f;
-            const float h1 = v ? __expf(e1 * r) : 1.f, h2 = v ? __expf(e2 * r) : 1.f;
-            if (!v) t = 0.f;
-            const float d = c1 * (Y1 + tm * (1.f - hm1)) + c2 * (Y2 + tm * (1.f - hm2));
-            out[i * nl] = v ? (out[i * nl] + d) * inv_nphi : 0.f;
-            Y1 = fmaf(h1 * h1, Y1, tm * h1 * (1.f - hm1 * h1));
-            Y2 = fmaf(h2 * h2, Y2, tm * h2 * (1.f - hm2 * h2));
-            tm = t; hm1 = h1; hm2 = h2;
+        for (int ib = iend - 1; ib >= i0; ib -= CONE_U) {
+            float2 rt[CONE_U];
+            float ov[CONE_U];
+#pragma unroll
+            for (int j = 0; j < CONE_U; j++) {
+                rt[j] = make_float2(-1.f, 0.f);
+                ov[j] = 0.f;
+                if (ib - j >= i0) {
+                    rt[j] = smp[(ib - j) * nl];
+                    ov[j] = out[(ib - j) * nl];
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < CONE_U; j++) {
+                const int i = ib - j;
+                if (i < i0) break;
+                const float r = rt[j].x;
+                const bool v = r >= 0.f;
+                const float t = v ? rt[j].y : 0.f;
+                const float h1 = v ? __expf(e1 * r) : 1.f, h2 = v ? __expf(e2 * r) : 1.f;
+                const float d = c1 * (Y1 + tm * (1.f - hm1)) + c2 * (Y2 + tm * (1.f - hm2));
+                out[i * nl] = v ? (ov[j] + d) * inv_nphi : 0.f;
+                Y1 = fmaf(h1 * h1, Y1, tm * h1 * (1.f - hm1 * h1));
+                Y2 = fmaf(h2 * h2, Y2, tm * h2 * (1.f - hm2 * h2));
+                tm = t; hm1 = h1; hm2 = h2;
+            }
         }
     }
 }
@@ -656,10 +686,23 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_T_lane(EeParams P, const Ee
         float h1 = v ? __expf(e1 * r) : 1.f, h2 = v ? __expf(e2 * r) : 1.f;
         float Z1 = 0.f, Z2 = 0.f;
         sA[i1 * nl] = make_float2(0.f, r);
-        for (int i = i1; i >= i0; i--) {
-            const float gi = v ? gin[i * nl] * inv_nphi : 0.f;
-            if (i > i0) {
-                const float rm = sample_rho(P, S, G, F, i - 1, nullptr, dummy);
+        // inputs gathered CONE_U samples ahead of the recurrence
+        for (int ib = i1; ib >= i0; ib -= CONE_U) {
+            float gl[CONE_U], rl[CONE_U];
+#pragma unroll
+            for (int j = 0; j < CONE_U; j++) {
+                const int i = ib - j;
+                gl[j] = 0.f;
+                rl[j] = -1.f;
+                if (i >= i0) gl[j] = gin[i * nl];
+                if (i > i0) rl[j] = sample_rho(P, S, G, F, i - 1, nullptr, dummy);
+            }
+#pragma unroll
+            for (int j = 0; j < CONE_U; j++) {
+                const int i = ib - j;
+                if (i <= i0) break;
+                const float gi = v ? gl[j] * inv_nphi : 0.f;
+                const float rm = rl[j];
                 const bool vm = rm >= 0.f;
                 const float hm1 = vm ? __expf(e1 * rm) : 1.f, hm2 = vm ? __expf(e2 * rm) : 1.f;
                 sA[(i - 1) * nl] = make_float2(vm ? c1 * gi * (1.f - hm1) + Z1 * h1 * (1.f - hm1 * h1) +
@@ -682,25 +725,40 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_T_lane(EeParams P, const Ee
         bool v = r >= 0.f;
         float h1 = v ? __expf(e1 * r) : 1.f, h2 = v ? __expf(e2 * r) : 1.f;
         float Z1 = 0.f, Z2 = 0.f, cprev = 0.f;
-        for (int i = i0; i <= i1; i++) {
-            const float gi = v ? gin[i * nl] * inv_nphi : 0.f;
-            const float tot = a.x + cprev;
-            if (v && tot != 0.f) {
-                f3 gp = F.gl + F.gx * (float)i;
-                tri_border_scatter(tg, S.tn[0], S.tn[1], S.tn[2], gp.x - (float)S.t0[0], gp.y - (float)S.t0[1],
-                                   gp.z - (float)S.t0[2], tot);
+        for (int ib = i0; ib <= i1; ib += CONE_U) {
+            float gl[CONE_U];
+            float2 al[CONE_U];
+#pragma unroll
+            for (int j = 0; j < CONE_U; j++) {
+                const int i = ib + j;
+                gl[j] = 0.f;
+                al[j] = make_float2(0.f, -1.f);
+                if (i <= i1) gl[j] = gin[i * nl];
+                if (i < i1) al[j] = sA[(i + 1) * nl];
             }
-            if (i < i1) {
-                a = sA[(i + 1) * nl];
-                const float rm = a.y;
-                const bool vm = rm >= 0.f;
-                const float hm1 = vm ? __expf(e1 * rm) : 1.f, hm2 = vm ? __expf(e2 * rm) : 1.f;
-                cprev = vm ? c1 * gi * (1.f - hm1) + Z1 * h1 * (1.f - hm1 * h1) + c2 * gi * (1.f - hm2) +
-                                 Z2 * h2 * (1.f - hm2 * h2)
-                           : 0.f;
-                Z1 = fmaf(h1 * h1, Z1, c1 * gi);
-                Z2 = fmaf(h2 * h2, Z2, c2 * gi);
-                v = vm; h1 = hm1; h2 = hm2;
+#pragma unroll
+            for (int j = 0; j < CONE_U; j++) {
+                const int i = ib + j;
+                if (i > i1) break;
+                const float gi = v ? gl[j] * inv_nphi : 0.f;
+                const float tot = a.x + cprev;
+                if (v && tot != 0.f) {
+                    f3 gp = F.gl + F.gx * (float)i;
+                    tri_border_scatter(tg, S.tn[0], S.tn[1], S.tn[2], gp.x - (float)S.t0[0], gp.y - (float)S.t0[1],
+                                       gp.z - (float)S.t0[2], tot);
+                }
+                if (i < i1) {
+                    a = al[j];
+                    const float rm = a.y;
+                    const bool vm = rm >= 0.f;
+                    const float hm1 = vm ? __expf(e1 * rm) : 1.f, hm2 = vm ? __expf(e2 * rm) : 1.f;
+                    cprev = vm ? c1 * gi * (1.f - hm1) + Z1 * h1 * (1.f - hm1 * h1) + c2 * gi * (1.f - hm2) +
+                                     Z2 * h2 * (1.f - hm2 * h2)
+                               : 0.f;
+                    Z1 = fmaf(h1 * h1, Z1, c1 * gi);
+                    Z2 = fmaf(h2 * h2, Z2, c2 * gi);
+                    v = vm; h1 = hm1; h2 = hm2;
+                }
             }
         }
     }
@@ -947,7 +1005,7 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
                             for (int d0 = 0; d0 < 2; d0++) {
                                 int k0 = i0 + d0 - l0;
                                 if (i0 + d0 >= R.rev[0] || k0 < 0 || k0 >= n0) continue;
-                                atomicAdd(acc + k0 + n0 * (k1 + n1 * k2), (d0 ? a0 : 1.f - a0) * w1);
+                                atomicAdd(acc + k1 + n1 * (k0 + n0 * k2), (d0 ? a0 : 1.f - a0) * w1);
                             }
                         }
                     }
@@ -958,7 +1016,9 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
             for (int k = t; k < nbox; k += blockDim.x) {
                 float v = acc[k];
                 if (v != 0.f) {
-                    int k0 = k % n0, k1 = (k / n0) % n1, k2 = k / (n0 * n1);
+                    // tile order k1 (tY) fastest: consecutive threads add to
+                    // consecutive arena addresses
+                    int k1 = k % n1, k0 = (k / n1) % n0, k2 = k / (n0 * n1);
                     atomicAdd(rb + (l1 + k1) + (long long)R.rev[1] * ((l2 + k2) + (long long)R.rev[2] * (l0 + k0)), v);
                 }
             }
