@@ -159,6 +159,10 @@ _SIGS = {
                                         C.POINTER(AnnealParams), C.POINTER(AnnealRecord)]),
     "ee_evaluate_proposals": (C.c_int, [C.c_void_p, C.POINTER(EEBeam), C.c_int, C.c_int, C.c_void_p, C.POINTER(Loss),
                                         C.POINTER(C.c_double)]),
+    "ee_ct_to_density": (C.c_int, [C.c_int, C.POINTER(Frame), C.c_void_p, C.c_float, C.c_void_p, C.c_void_p, C.c_int,
+                                   C.c_void_p, C.POINTER(C.c_int)]),
+    "ee_fluence_projection": (C.c_int, [C.c_int, C.POINTER(Frame), C.c_void_p, C.POINTER(EEBeam), C.c_int, C.c_int,
+                                        C.c_int, C.c_void_p]),
     "ee_server_create": (C.c_int, [C.c_int, C.c_int, C.c_longlong, C.c_int, C.POINTER(C.c_void_p)]),
     "ee_server_set_physics": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                         C.POINTER(ConvParams), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
@@ -628,6 +632,55 @@ class Server:
 
     def __exit__(self, *a):
         self.close()
+
+
+# ---- preprocessing (dosecalc-preprocess) ----
+SIEMENS_LUT = (  # HU -> g/cc, the reference's default table (dosecalc-preprocess/main.cu:187-200)
+    [-969.8, -712.9, -536.5, -95.6, -45.6, -5.6, -1.9, 25.7, 65.6, 207.5, 220.7, 429.9, 775.3, 1173.7],
+    [0.0, 0.290, 0.450, 0.943, 0.985, 1.000, 1.016, 1.052, 1.089, 1.145, 1.159, 1.335, 1.560, 1.823])
+
+
+def ct_to_density(hu: np.ndarray, voxel_cm, iso_voxel_cm: float, lut=SIEMENS_LUT, start_cm=(0.0, 0.0, 0.0),
+                  device: int = 0):
+    """Isotropic density volume [nz, ny, nx] from a CT in HU (ee_ct_to_density);
+    lut=None selects the linear HU rule."""
+    lib = load_library()
+    h = np.ascontiguousarray(hu, np.float32)
+    f = Frame()
+    f.size[:] = [h.shape[2], h.shape[1], h.shape[0]]
+    f.voxel[:] = [float(v) for v in voxel_cm]
+    f.start[:] = [float(v) for v in start_cm]
+    f.bbox_size[:] = list(f.size)
+    if lut is not None:
+        lh, ld = np.ascontiguousarray(lut[0], np.float32), np.ascontiguousarray(lut[1], np.float32)
+        n = len(lh)
+    else:
+        lh = ld = np.zeros(1, np.float32)
+        n = 0
+    os_ = (C.c_int * 3)()
+    _raise_status(lib, lib.ee_ct_to_density(int(device), C.byref(f), None, float(iso_voxel_cm), _ptr(lh), _ptr(ld), n,
+                                            None, os_))
+    out = np.zeros((os_[2], os_[1], os_[0]), np.float32)
+    _raise_status(lib, lib.ee_ct_to_density(int(device), C.byref(f), _ptr(h), float(iso_voxel_cm), _ptr(lh), _ptr(ld),
+                                            n, _ptr(out), os_))
+    return out
+
+
+def fluence_projection(mask_vol, beams, supersample: bool = True, aperture_ready: bool = False, device: int = 0):
+    """Binary conformal fluence maps of the beams through a mask volume
+    (an inputs.Volume whose density holds the mask); list of [fy, fx]."""
+    lib = load_library()
+    m = np.ascontiguousarray(mask_vol.density, np.float32)
+    eb = to_ee_beams(beams)
+    out = np.zeros(sum(int(b.fmap_size[0]) * int(b.fmap_size[1]) for b in beams), np.float32)
+    _raise_status(lib, lib.ee_fluence_projection(int(device), C.byref(_frame_of(mask_vol)), _ptr(m), eb, len(beams),
+                                                 int(bool(supersample)), int(bool(aperture_ready)), _ptr(out)))
+    res, o = [], 0
+    for b in beams:
+        n = int(b.fmap_size[0]) * int(b.fmap_size[1])
+        res.append(out[o:o + n].reshape(int(b.fmap_size[1]), int(b.fmap_size[0])))
+        o += n
+    return res
 
 
 def beam_source(beam):

@@ -346,6 +346,25 @@ int ee_optimize_annealing(ee_context *ctx, ee_beam *beams, int nbeams, float *d_
 int ee_evaluate_proposals(ee_context *ctx, const ee_beam *proposals, int nprop, int nbeams, const float *d_x,
                           const ee_loss *loss, double *losses);
 
+/* ---- preprocessing (dosecalc-preprocess) ----
+ * ee_ct_to_density: the CT volume (HU, x fastest, frame `ct`: size, voxel in
+ * cm) resampled onto an isotropic grid of iso_voxel_cm through linear
+ * filtering, converted with the HU -> mass-density table (lut_hu ascending,
+ * nlut in [2, 64]; outside it: clamped below, extrapolated from the last two
+ * points above) or, with nlut == 0, by max((HU + 1024) / 1024, 0.05)
+ * (replaces read_dicom / cudaCreateTexIso, dosecalc-preprocess/
+ * cudaMemFunctions.cu:32-176).  out_size = ceil(voxel * size / iso_voxel);
+ * density == NULL only returns out_size.  The density keeps the CT's start.
+ * ee_fluence_projection: the binary conformal fluence map of every beam
+ * through the PTV mask (findFluenceProjection, cudaMemFunctions.cu:308-388):
+ * a pixel opens when any of its sub-rays (3x3 with supersample, else the
+ * centre) crosses the mask; aperture_ready fills each row's holes
+ * (fmap_post_apertureready).  fluence: the concatenated maps. */
+int ee_ct_to_density(int device, const ee_frame *ct, const float *hu, float iso_voxel_cm, const float *lut_hu,
+                     const float *lut_density, int nlut, float *density, int out_size[3]);
+int ee_fluence_projection(int device, const ee_frame *mask_frame, const float *mask, const ee_beam *beams, int nbeams,
+                          int supersample, int aperture_ready, float *fluence);
+
 /* ---- diagnostics ---- */
 /* Stage ids for ee_read_profile. */
 #define EE_STAGE_TERMA 0     /* k_terma (+crop-box reduction)           */

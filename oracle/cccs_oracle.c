@@ -172,8 +172,12 @@ static void beam_reconfigure(const orc_beam *b, r3 *src, r3 *dir, real *az, real
 }
 
 /* ---------------- texture emulation ---------------- */
+/* emulate: 0 exact weights, 1 rounded to 8 fractional bits, 2 truncated to
+ * 8 fractional bits (the two readings of the texture unit's 9-bit fixed
+ * point weight with 8 fractional bits) */
 static inline real quant_w(real a, int emulate) {
     if (!emulate) return a;
+    if (emulate == 2) return (real)(floor((double)a * 256.0) / 256.0);
     return (real)(floor((double)a * 256.0 + 0.5) / 256.0);
 }
 /* tex3D<float>, unnormalised coordinates, linear filter, border address
@@ -873,6 +877,104 @@ void orc_row_convolve_T(const orc_setup *S, const real *dens, const real *g, int
     row_convolve_T(S, dens, g, L, P, gT, work);
     free(work);
 }
+/* ---------------- preprocessing: CCCS/dosecalc-preprocess ---------------- */
+/* cudaMakeIsotropicWithLUT / cudaMakeIsotropic + deviceHU2dens
+ * (dosecalc-preprocess/kernels.cuh:12-102, cudaMemFunctions.cu:82-176): the
+ * CT (HU, x fastest, frame ct_size / ct_voxel) resampled at iso voxel
+ * centres (X,Y,Z)*iso_voxel / ct_voxel through a border-0 linear texture,
+ * then converted by the sorted LUT (clamped below, linear extrapolation from
+ * the last two points above) or, when nlut == 0, by max((HU+1024)/1024,
+ * 0.05).  out_size = ceil(ct_voxel*ct_size/iso_voxel) per axis. */
+void orc_iso_size(const int ct_size[3], const double ct_voxel[3], double iso_voxel, int out_size[3]) {
+    for (int a = 0; a < 3; a++) out_size[a] = (int)ceilf((float)ct_voxel[a] * ((float)ct_size[a] / (float)iso_voxel));
+}
+
+int orc_ct_to_density(const float *hu, const int ct_size[3], const double ct_voxel[3], double iso_voxel,
+                      const double *lut_hu, const double *lut_dens, int nlut, int tex_emulate, real *out) {
+    int os[3];
+    orc_iso_size(ct_size, ct_voxel, iso_voxel, os);
+    for (int i = 1; i < nlut; i++)
+        if (!(lut_hu[i] > lut_hu[i - 1])) return ORC_ERR_ARG;
+    const long n = (long)os[0] * os[1] * os[2];
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+    for (long v = 0; v < n; v++) {
+        const int X = (int)(v % os[0]), Y = (int)((v / os[0]) % os[1]), Z = (int)(v / ((long)os[0] * os[1]));
+        const real px = (real)X * (real)iso_voxel / (real)ct_voxel[0];
+        const real py = (real)Y * (real)iso_voxel / (real)ct_voxel[1];
+        const real pz = (real)Z * (real)iso_voxel / (real)ct_voxel[2];
+        /* tex3d_border_f takes texture coordinates (before the -0.5 shift) */
+        real val = tex3d_border_f(hu, ct_size, px + (real)0.5, py + (real)0.5, pz + (real)0.5, tex_emulate);
+        if (nlut > 0) {
+            if (val <= lut_hu[0]) val = lut_dens[0];
+            else if (val >= lut_hu[nlut - 1])
+                val = lut_dens[nlut - 2] + (val - lut_hu[nlut - 2]) * (lut_dens[nlut - 1] - lut_dens[nlut - 2]) /
+                                               (lut_hu[nlut - 1] - lut_hu[nlut - 2]);
+            else {
+                int lo = 0;
+                while (lut_hu[lo] < val && lo < nlut - 1) lo++;
+                lo--;
+                val = lut_dens[lo] + (val - lut_hu[lo]) * (lut_dens[lo + 1] - lut_dens[lo]) / (lut_hu[lo + 1] - lut_hu[lo]);
+            }
+        } else {
+            val = (val + (real)1024) / (real)1024;
+            if (val < (real)0.05) val = (real)0.05;
+        }
+        out[v] = val;
+    }
+    return ORC_OK;
+}
+
+/* cudaRaycast (kernels.cuh:138-224): a fluence pixel is 1 when any of its
+ * sub-rays (3x3 at half-beamlet offsets with supersampling, else the centre
+ * ray) from the source to three times the bixel centre on the isocentre
+ * plane accumulates a positive radiological path through the mask (the
+ * Siddon trace of cudaSiddon.cu:20-115 on the mask frame in S). */
+int orc_fluence_projection(const orc_setup *S, const orc_beam *b, int supersample, float *fmap) {
+    r3 src, dir;
+    real az, zen;
+    beam_reconfigure(b, &src, &dir, &az, &zen);
+    const r3 start = mk3((real)S->start[0], (real)S->start[1], (real)S->start[2]);
+    const r3 voxel = mk3((real)S->voxel[0], (real)S->voxel[1], (real)S->voxel[2]);
+    const r3 end = mk3(start.x + (real)S->size[0] * voxel.x, start.y + (real)S->size[1] * voxel.y,
+                       start.z + (real)S->size[2] * voxel.z);
+    const r3 iso = mk3((real)b->iso[0], (real)b->iso[1], (real)b->iso[2]);
+    const int fx = b->fmap[0], fy = b->fmap[1], nsub = supersample ? 9 : 1;
+    int err = 0;
+    for (int Z = 0; Z < fy; Z++)
+        for (int X = 0; X < fx; X++) {
+            float hit = 0.f;
+            for (int k = 0; k < nsub && hit == 0.f; k++) {
+                const int sx = supersample ? k % 3 - 1 : 0, sz = supersample ? k / 3 - 1 : 0;
+                r3 f = mk3((real)b->beamlet[0] * ((real)X + (real)0.5 * sx - (real)fx * (real)0.5 + (real)0.5), 0,
+                           (real)b->beamlet[1] * ((real)Z + (real)0.5 * sz - (real)fy * (real)0.5 + (real)0.5));
+                r3 c = add3(inv_rot_beam(f, az, zen, (real)b->coll), iso);
+                c = add3(c, mk3((real)1e-9, (real)1e-9, (real)1e-9));
+                const r3 sink = add3(src, scl3(sub3(c, src), 3));
+                if (siddon_rpl(S, sink, start, end, voxel, src, &err) > 0) hit = 1.f;
+            }
+            fmap[X + fx * Z] = hit;
+        }
+    return err ? ORC_ERR_ITER : ORC_OK;
+}
+
+/* fmap_post_apertureready (dosecalc-preprocess/fmapProcessing.cpp:33-48):
+ * per fluence-map row, the zero pixels between its first and last non-zero
+ * pixels are set to fill. */
+void orc_aperture_ready(float *fmap, int fx, int fy, float fill) {
+    for (int y = 0; y < fy; y++) {
+        int a = -1, z = -1;
+        for (int x = 0; x < fx; x++)
+            if (fmap[fx * y + x] != 0.f) {
+                if (a < 0) a = x;
+                z = x;
+            }
+        for (int x = a + 1; a >= 0 && x < z; x++)
+            if (fmap[fx * y + x] == 0.f) fmap[fx * y + x] = fill;
+    }
+}
+
 int orc_sizeof_real(void) { return (int)sizeof(real); }
 int orc_sizeof_info(void) { return (int)sizeof(orc_beam_info); }
 int orc_sizeof_setup(void) { return (int)sizeof(orc_setup); }

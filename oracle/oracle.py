@@ -78,6 +78,15 @@ def _lib(precision: int = 64):
         lib.orc_row_convolve_T.restype = None
         lib.orc_rotate.argtypes = [C.c_int, C.POINTER(C.c_double), C.c_double, C.c_double, C.c_double, C.POINTER(C.c_double)]
         lib.orc_rotate.restype = None
+        lib.orc_iso_size.argtypes = [C.POINTER(C.c_int), C.POINTER(C.c_double), C.c_double, C.POINTER(C.c_int)]
+        lib.orc_iso_size.restype = None
+        lib.orc_ct_to_density.argtypes = [C.POINTER(C.c_float), C.POINTER(C.c_int), C.POINTER(C.c_double), C.c_double,
+                                          C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int, C.c_int, rp]
+        lib.orc_ct_to_density.restype = C.c_int
+        lib.orc_fluence_projection.argtypes = [C.POINTER(OrcSetup), C.POINTER(OrcBeam), C.c_int, C.POINTER(C.c_float)]
+        lib.orc_fluence_projection.restype = C.c_int
+        lib.orc_aperture_ready.argtypes = [C.POINTER(C.c_float), C.c_int, C.c_int, C.c_float]
+        lib.orc_aperture_ready.restype = None
         assert lib.orc_sizeof_info() == C.sizeof(OrcBeamInfo), "OrcBeamInfo layout mismatch"
         assert lib.orc_sizeof_setup() == C.sizeof(OrcSetup), "OrcSetup layout mismatch"
         lib._real = real
@@ -218,3 +227,59 @@ def rotate(which, vec, a, b, c=0.0, precision=64):
     out = np.zeros(3)
     lib.orc_rotate(int(which), _dp(v), float(a), float(b), float(c), _dp(out))
     return out
+
+
+# ---- preprocessing (CCCS/dosecalc-preprocess) ----
+def ct_to_density(hu, voxel, iso_voxel, lut=None, tex_emulate=1, precision=64):
+    """Isotropic density from a CT volume [nz, ny, nx] in HU (cudaMakeIsotropicWithLUT,
+    or the linear HU rule without a LUT).  lut: (hu values, densities), sorted.
+    tex_emulate: 0 exact, 1 rounded, 2 truncated 8-bit filter weights."""
+    lib = _lib(precision)
+    hu = np.ascontiguousarray(hu, np.float32)
+    size = (C.c_int * 3)(hu.shape[2], hu.shape[1], hu.shape[0])
+    vox = (C.c_double * 3)(*[float(np.float32(v)) for v in voxel])
+    out_size = (C.c_int * 3)()
+    lib.orc_iso_size(size, vox, float(np.float32(iso_voxel)), out_size)
+    nx, ny, nz = list(out_size)
+    out = np.zeros((nz, ny, nx), dtype=lib._np)
+    if lut is not None:
+        lh = np.ascontiguousarray(np.asarray(lut[0], np.float32).astype(np.float64))
+        ld = np.ascontiguousarray(np.asarray(lut[1], np.float32).astype(np.float64))
+        n = len(lh)
+    else:
+        lh = ld = np.zeros(1)
+        n = 0
+    st = lib.orc_ct_to_density(hu.ctypes.data_as(C.POINTER(C.c_float)), size, vox, float(np.float32(iso_voxel)),
+                               _dp(lh), _dp(ld), n, int(tex_emulate), _rp(lib, out))
+    if st != 0:
+        raise RuntimeError(f"oracle ct_to_density failed with status {st}")
+    return out
+
+
+def fluence_projection(mask_vol, beam, supersample=True, tex_emulate=True, precision=64):
+    """Binary conformal fluence map of `beam` through the mask volume
+    (cudaRaycast); mask_vol is an inputs.Volume whose density is the mask."""
+    o = Oracle(mask_vol, _dummy_physics(), tex_emulate=tex_emulate, precision=precision)
+    ob, _ = o._beam(beam)
+    fm = np.zeros((int(beam.fmap_size[1]), int(beam.fmap_size[0])), np.float32)
+    st = o.lib.orc_fluence_projection(C.byref(o.setup), C.byref(ob), int(bool(supersample)),
+                                      fm.ctypes.data_as(C.POINTER(C.c_float)))
+    if st != 0:
+        raise RuntimeError(f"oracle fluence_projection failed with status {st}")
+    return fm
+
+
+def aperture_ready(fmap, fill=1.0):
+    """fmap_post_apertureready on a [fy, fx] map (returns a copy)."""
+    lib = _lib(64)
+    f = np.ascontiguousarray(fmap, np.float32).copy()
+    lib.orc_aperture_ready(f.ctypes.data_as(C.POINTER(C.c_float)), f.shape[1], f.shape[0], float(fill))
+    return f
+
+
+def _dummy_physics():
+    import types
+    z = np.zeros(1)
+    return types.SimpleNamespace(energy=z + 1, fluence=z + 1, mu=z, mu_en=z, ntheta=2, nphi=1, nradii=1, radii=z + 1,
+                                 cumkern=np.zeros((2, 1)), exp_params=np.zeros((2, 4)) + 1, theta_deg=z, phi_deg=z,
+                                 rev_latspacing=1.0, rev_longspacing=1.0, penumbra=1.0)
