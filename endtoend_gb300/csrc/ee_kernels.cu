@@ -77,27 +77,16 @@ __global__ void __launch_bounds__(256) k_terma(EeParams P, const EeBeamSpec* __r
         kmax1 = max(kmax1, __shfl_xor_sync(FULL, kmax1, o));
         kmax2 = max(kmax2, __shfl_xor_sync(FULL, kmax2, o));
     }
-    __shared__ int sred[8][8];
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (lane == 0) {
-        sred[w][0] = kmin0; sred[w][1] = kmin1; sred[w][2] = kmin2;
-        sred[w][3] = kmax0; sred[w][4] = kmax1; sred[w][5] = kmax2;
-        sred[w][6] = (int)cnt; sred[w][7] = anycap ? 1 : 0;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int r[8] = {INT_MAX, INT_MAX, INT_MAX, INT_MIN, INT_MIN, INT_MIN, 0, 0};
-        for (int i = 0; i < (int)(blockDim.x >> 5); i++) {
-            for (int a = 0; a < 3; a++) { r[a] = min(r[a], sred[i][a]); r[3 + a] = max(r[3 + a], sred[i][3 + a]); }
-            r[6] += sred[i][6];
-            r[7] |= sred[i][7];
-        }
+    // one lane per warp merges into the beam's keys: no block barrier, so a
+    // warp whose rays are short does not wait for the block's longest trace
+    if ((threadIdx.x & 31) == 0) {
         EeBeamGeom& G = geoms[b];
-        if (r[6] > 0) {
-            for (int a = 0; a < 3; a++) { atomicMin(&G.key_min[a], r[a]); atomicMax(&G.key_max[a], r[3 + a]); }
-            atomicAdd(&G.nnz, (unsigned)r[6]);
+        if (cnt > 0) {
+            atomicMin(&G.key_min[0], kmin0); atomicMin(&G.key_min[1], kmin1); atomicMin(&G.key_min[2], kmin2);
+            atomicMax(&G.key_max[0], kmax0); atomicMax(&G.key_max[1], kmax1); atomicMax(&G.key_max[2], kmax2);
+            atomicAdd(&G.nnz, cnt);
         }
-        if (r[7]) atomicExch(&G.status, 7 /* EE_ERR_SIDDON_ITER */);
+        if (anycap) atomicExch(&G.status, 7 /* EE_ERR_SIDDON_ITER */);
     }
 }
 
