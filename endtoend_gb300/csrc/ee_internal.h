@@ -86,6 +86,7 @@ struct EeRayGeom {
     float G0[3], Gx[3], Gy[3], Gz[3];  // REV (tX,tY,tZ) -> patient voxel index
     float B0[3], Bx[3], By[3], Bz[3];  // REV (tX,tY,tZ) -> BEV crop-box index
     float M[9];            // BEV -> REV (copy of MK for the gather)
+    float A[9];            // patient index step -> REV step (MK MB), row-major
 };
 
 // Per-beam geometry computed on the device (crop box + REV frames).

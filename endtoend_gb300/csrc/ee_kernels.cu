@@ -173,6 +173,9 @@ __global__ void k_geometry(EeParams P, const EeBeamSpec* __restrict__ specs, EeB
         R.Gy[0] = Gy.x; R.Gy[1] = Gy.y; R.Gy[2] = Gy.z;
         R.Gz[0] = Gz.x; R.Gz[1] = Gz.y; R.Gz[2] = Gz.z;
         for (int i = 0; i < 9; i++) R.M[i] = RC.MK[i];
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++)
+                R.A[3 * i + j] = RC.MK[3 * i] * S.MB[j] + RC.MK[3 * i + 1] * S.MB[3 + j] + RC.MK[3 * i + 2] * S.MB[6 + j];
     }
     __syncthreads();
     if (threadIdx.x == 0 && G.status == 0) {
@@ -937,34 +940,31 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
             gd = 0.f;
     }
     if (!__syncthreads_or(gd != 0.f)) return;
-    // BEV index of the tile origin and the BEV steps of a unit patient step
-    const f3 b0 = mv(S.MB, mk((float)ox - G.lim_off[0], (float)oy - G.lim_off[1], (float)oz - G.lim_off[2]));
+    // tile origin relative to the crop box, in patient index units
+    const float o0 = (float)ox - G.lim_off[0], o1 = (float)oy - G.lim_off[1], o2 = (float)oz - G.lim_off[2];
     float* base = rev_grad + G.arena_off;
     for (int r = 0; r < P.nrays; r++) {
         const EeRayGeom& R = G.ray[r];
-        // q(v) = M (MB (v - lim_off)) - q0; columns of A = M MB
-        if (t == 0) {
-            f3 q0 = mv(R.M, b0) - ld3(R.q0);
-            float qa[3] = {q0.x, q0.y, q0.z}, lo[3], hi[3];
-            f3 cx = mv(R.M, mk(S.MB[0], S.MB[3], S.MB[6])), cy = mv(R.M, mk(S.MB[1], S.MB[4], S.MB[7])),
-               cz = mv(R.M, mk(S.MB[2], S.MB[5], S.MB[8]));
-            float c[3][3] = {{cx.x, cy.x, cz.x}, {cx.y, cy.y, cz.y}, {cx.z, cy.z, cz.z}};
+        // REV footprint of the tile: q(v) = A (v - lim_off) - q0, one REV
+        // axis per thread; bounds widened by 1e-3 so that the per-voxel q
+        // (formed in another order) never falls outside
+        if (t < 3) {
+            const int a = t;
             const float ext[3] = {(float)(GT_TX - 1), (float)(GT_TY - 1), (float)(GT_TZ - 1)};
-            for (int a = 0; a < 3; a++) {
-                lo[a] = hi[a] = qa[a];
-                for (int k = 0; k < 3; k++) {
-                    float d = c[a][k] * ext[k];
-                    lo[a] += fminf(d, 0.f);
-                    hi[a] += fmaxf(d, 0.f);
-                }
+            const float* Ar = R.A + 3 * a;
+            float lo = Ar[0] * o0 + Ar[1] * o1 + Ar[2] * o2 - R.q0[a], hi = lo;
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                const float d = Ar[k] * ext[k];
+                lo += fminf(d, 0.f);
+                hi += fmaxf(d, 0.f);
             }
             // REV axes: q.y -> rev[0] (along the line), q.z -> rev[1], q.x -> rev[2]
-            int l0 = max(0, (int)floorf(lo[1])), h0 = min(R.rev[0] - 1, (int)floorf(hi[1]) + 1);
-            int l1 = max(0, (int)floorf(lo[2])), h1 = min(R.rev[1] - 1, (int)floorf(hi[2]) + 1);
-            int l2 = max(0, (int)floorf(lo[0])), h2 = min(R.rev[2] - 1, (int)floorf(hi[0]) + 1);
-            s_box[0] = l0; s_box[1] = h0 - l0 + 1;
-            s_box[2] = l1; s_box[3] = h1 - l1 + 1;
-            s_box[4] = l2; s_box[5] = h2 - l2 + 1;
+            const int dim = a == 1 ? R.rev[0] : (a == 2 ? R.rev[1] : R.rev[2]);
+            const int slot = a == 1 ? 0 : (a == 2 ? 2 : 4);
+            const int l = max(0, (int)floorf(lo - 1e-3f)), h = min(dim - 1, (int)floorf(hi + 1e-3f) + 1);
+            s_box[slot] = l;
+            s_box[slot + 1] = h - l + 1;
         }
         __syncthreads();
         const int l0 = s_box[0], n0 = s_box[1], l1 = s_box[2], n1 = s_box[3], l2 = s_box[4], n2 = s_box[5];
@@ -1002,12 +1002,18 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
             }
             __syncthreads();
             float* rb = base + R.offset;
+            // (k + 0.5) / n is at least 1/(2n) away from an integer, far above
+            // the FP32 error for these sizes: the float quotient is exact
+            const float inv1 = 1.f / (float)n1, inv0 = 1.f / (float)n0;
             for (int k = t; k < nbox; k += blockDim.x) {
                 float v = acc[k];
                 if (v != 0.f) {
                     // tile order k1 (tY) fastest: consecutive threads add to
                     // consecutive arena addresses
-                    int k1 = k % n1, k0 = (k / n1) % n0, k2 = k / (n0 * n1);
+                    const int q1 = __float2int_rd(((float)k + 0.5f) * inv1);
+                    const int k1 = k - q1 * n1;
+                    const int k2 = __float2int_rd(((float)q1 + 0.5f) * inv0);
+                    const int k0 = q1 - k2 * n0;
                     atomicAdd(rb + (l1 + k1) + (long long)R.rev[1] * ((l2 + k2) + (long long)R.rev[2] * (l0 + k0)), v);
                 }
             }
