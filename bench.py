@@ -380,6 +380,14 @@ def run_reference(args, ws, rank):
     print(json.dumps(line), flush=True)
 
 
+# DRAM bytes (read + write) per crop-box voxel of each stage, from an ncu
+# capture of all six chain kernels on eight beams of this workload (dram__bytes
+# of both chunks' launches / sum of V_beam = 12.37 M); roofline.traffic scales
+# the dominant stage's figure to the profiled step.
+DRAM_BYTES_PER_VBEAM = {"terma": 0.6, "cone": 433.7, "gather": 80.1, "gather_T": 118.4, "cone_T": 292.7,
+                        "terma_T": 3.1, "geometry": 0.0}
+
+
 def algorithmic_bytes(infos):
     """Per-solve algorithmic bytes: 392 * V_beam per beam (TERMA 8 B/voxel,
     each of 24 cone directions 8 B/voxel read + 8 B/voxel dose RMW)."""
@@ -528,8 +536,13 @@ def main():
     peak = float(peaks.get("hbm_gbs", 6800.0))
     dom_ms, dom_launches = prof[dom]
     achieved = stage_bytes.get(dom, 0.0) / (dom_ms / 1e3) / 1e9 if dom_ms > 0 else 0.0
+    # traffic and achieved refer to the same unit of work: the dominant
+    # stage over all beams of one step
+    traffic = DRAM_BYTES_PER_VBEAM.get(dom, 0.0) * vb
     roof = {"bound": "hbm", "kernel": f"k_{dom}", "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "traffic": None,
+            "frac": achieved / peak, "traffic": traffic,
+            "traffic_unit": "bytes per step of the dominant stage (ncu dram bytes per V_beam voxel x sum V_beam)",
+            "algorithmic_bytes": stage_bytes.get(dom, 0.0),
             "peak_source": "measured" if peaks else "fallback",
             "stage_ms": {k: round(v[0], 3) for k, v in prof.items()},
             "chain_frac": (2 * alg_bytes / (sum(step_ms) / len(step_ms) / 1e3) / 1e9) / peak}
