@@ -204,6 +204,8 @@ __global__ void k_geometry(EeParams P, const EeBeamSpec* __restrict__ specs, EeB
             mls = max(mls, G.ray[r].nlines);
         }
         G.rev_total = off;
+        // the gather addresses a cone's REV array with a 32-bit offset
+        if (off > 2147483647ll) G.status = 4;  // EE_ERR_REV_SIZE
         G.max_line = ml;
         G.max_lines = mls;
         if (G.arena_cap > 0 && off > G.arena_cap) G.status = 8;
@@ -827,32 +829,6 @@ __global__ void __launch_bounds__(CONE_WARPS * 32) k_cone_T(EeParams P, const Ee
 }
 
 // ------------------------------------------------------------- gather ----
-// REV2XYZdose (device.cu:222-261) for all cones at once.  The patient
-// voxel's BEV index b = MB (t - lim_off) is formed once per beam; voxels more
-// than 2 BEV voxels outside the crop box see only zero REV samples and skip
-// the cone loop.
-__device__ __forceinline__ float beam_voxel_dose(const EeParams& P, const EeBeamSpec& S, const EeBeamGeom& G,
-                                                 const float* __restrict__ rev, int x, int y, int z) {
-    f3 d = mk((float)x - G.lim_off[0], (float)y - G.lim_off[1], (float)z - G.lim_off[2]);
-    f3 bi = mv(S.MB, d);
-    if (bi.x < -2.f || bi.y < -2.f || bi.z < -2.f || bi.x > G.bev[0] + 2.f || bi.y > G.bev[1] + 2.f ||
-        bi.z > G.bev[2] + 2.f)
-        return 0.f;
-    float acc = 0.f;
-    const float* base = rev + G.arena_off;
-    for (int r = 0; r < P.nrays; r++) {
-        const EeRayGeom& R = G.ray[r];
-        f3 q = mv(R.M, bi) - ld3(R.q0);
-        // q.y along the line (rev[0]), q.z -> rev[1], q.x -> rev[2]
-        if (q.y >= (float)R.rev[0] || q.z >= (float)R.rev[1] || q.x >= (float)R.rev[2] || q.x < 0.f || q.y < 0.f ||
-            q.z < 0.f)
-            continue;
-        // REV arena layout [i][tZ][tY]: x = tY (q.z), y = tZ (q.x), z = i (q.y)
-        acc += tri_border(base + R.offset, R.rev[1], R.rev[2], R.rev[0], q.z, q.x, q.y);
-    }
-    return acc;
-}
-
 // Voxel range [x0, x1] of patient row (y, z) whose BEV index lies within the
 // crop box dilated by 2 voxels (the BEV index is affine in x), widened by one
 // voxel for rounding and clipped to the calc bbox.
@@ -881,8 +857,10 @@ __device__ __forceinline__ bool row_span(const EeParams& P, const EeBeamSpec& S,
 
 constexpr int ROW_WARPS = 8;
 
-// One warp per patient row of one beam's AABB; lanes sweep the row's span.
-// mode 0/1: atomic accumulation into dose; mode 2: dose[b] written directly.
+// REV2XYZdose (device.cu:222-261) for all cones at once: one warp per
+// patient row of one beam's AABB, lanes sweeping the row's span; a voxel
+// sums the trilinear REV dose of every cone.  mode 0/1: atomic accumulation
+// into dose; mode 2: dose[b] written directly.
 __global__ void __launch_bounds__(ROW_WARPS * 32) k_gather(EeParams P, const EeBeamSpec* __restrict__ specs,
                                                            const EeBeamGeom* __restrict__ geoms,
                                                            const float* __restrict__ rev, float* __restrict__ dose,
@@ -890,6 +868,22 @@ __global__ void __launch_bounds__(ROW_WARPS * 32) k_gather(EeParams P, const EeB
     const int b = blockIdx.z;
     const EeBeamGeom& G = geoms[b];
     if (G.status != 0) return;
+    // the beam's cone maps, staged once per block: rows of [A | -q0] (REV
+    // from crop-box-relative patient index) and (rev sizes, arena offset)
+    __shared__ float4 s_ray[EE_MAX_RAYS][4];
+    for (int k = threadIdx.x; k < P.nrays * 4; k += blockDim.x) {
+        const int r = k >> 2, c = k & 3;
+        const EeRayGeom& R = G.ray[r];
+        float4 v;
+        if (c < 3) {
+            v = make_float4(R.A[3 * c], R.A[3 * c + 1], R.A[3 * c + 2], -R.q0[c]);
+        } else {
+            v = make_float4(__int_as_float(R.rev[0]), __int_as_float(R.rev[1]), __int_as_float(R.rev[2]),
+                            __int_as_float((int)R.offset));
+        }
+        s_ray[r][c] = v;
+    }
+    __syncthreads();
     const int row = blockIdx.x * ROW_WARPS + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (row >= G.rows) return;
     const int y = G.gy0 + row % G.gny, z = G.gz0 + row / G.gny;
@@ -898,14 +892,34 @@ __global__ void __launch_bounds__(ROW_WARPS * 32) k_gather(EeParams P, const EeB
     if (!row_span(P, S, G, y, z, x0, x1)) return;
     float* out = dose + S.out_off + (mode == 2 ? (long long)b * nfull : 0ll);
     const long long rbase = (long long)P.size[0] * (y + (long long)P.size[1] * z);
+    const float* base = rev + G.arena_off;
+    const float dy = (float)y - G.lim_off[1], dz = (float)z - G.lim_off[2];
     for (int x = x0 + lane; x <= x1; x += 32) {
-        float acc = beam_voxel_dose(P, S, G, rev, x, y, z);
+        const float dx = (float)x - G.lim_off[0];
+        // voxels more than 2 BEV voxels outside the crop box see no REV dose
+        const f3 bi = mv(S.MB, mk(dx, dy, dz));
+        float acc = 0.f;
+        if (!(bi.x < -2.f || bi.y < -2.f || bi.z < -2.f || bi.x > G.bev[0] + 2.f || bi.y > G.bev[1] + 2.f ||
+              bi.z > G.bev[2] + 2.f)) {
+            for (int r = 0; r < P.nrays; r++) {
+                const float4 a0 = s_ray[r][0], a1 = s_ray[r][1], a2 = s_ray[r][2], rv = s_ray[r][3];
+                const float qx = fmaf(a0.x, dx, fmaf(a0.y, dy, fmaf(a0.z, dz, a0.w)));
+                const float qy = fmaf(a1.x, dx, fmaf(a1.y, dy, fmaf(a1.z, dz, a1.w)));
+                const float qz = fmaf(a2.x, dx, fmaf(a2.y, dy, fmaf(a2.z, dz, a2.w)));
+                const int n0 = __float_as_int(rv.x), n1 = __float_as_int(rv.y), n2 = __float_as_int(rv.z);
+                // q.y along the line (rev[0]), q.z -> rev[1], q.x -> rev[2]
+                if (qy >= (float)n0 || qz >= (float)n1 || qx >= (float)n2 || qx < 0.f || qy < 0.f || qz < 0.f)
+                    continue;
+                // REV arena layout [i][tZ][tY]: x = tY (q.z), y = tZ (q.x), z = i (q.y)
+                acc += tri_border(base + __float_as_int(rv.w), n1, n2, n0, qz, qx, qy);
+            }
+        }
         if (mode == 2) out[rbase + x] = acc;
         else if (acc != 0.f) atomicAdd(out + rbase + x, acc);
     }
 }
 
-// Transpose of beam_voxel_dose: rev_grad += S^T dose_grad, one block per
+// Transpose of k_gather's per-voxel sum: rev_grad += S^T dose_grad, one block per
 // 8x8x4 tile of patient voxels.  For each cone the tile's trilinear
 // footprint in the REV grid (an AABB computed from the tile's corners under
 // the affine patient -> REV map) is accumulated in shared memory first, then
