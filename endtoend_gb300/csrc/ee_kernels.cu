@@ -933,7 +933,8 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
                                                                    const float* __restrict__ dose_grad,
                                                                    float* __restrict__ rev_grad) {
     extern __shared__ float acc[];
-    __shared__ int s_box[6];
+    __shared__ int s_box[9];
+    __shared__ float4 s_A[3];
     const int b = blockIdx.z;
     const EeBeamGeom& G = geoms[b];
     if (G.status != 0 || (int)blockIdx.x >= G.tiles) return;
@@ -945,10 +946,10 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
     const int t = threadIdx.x;
     const int x = ox + t % GT_TX, y = oy + (t / GT_TX) % GT_TY, z = oz + t / (GT_TX * GT_TY);
     float gd = 0.f;
-    f3 bi = mk(0.f, 0.f, 0.f);
+    const float dx = (float)x - G.lim_off[0], dy = (float)y - G.lim_off[1], dz = (float)z - G.lim_off[2];
     if (x < G.gx0 + G.gnx && y < G.gy0 + G.gny && z < G.gz0 + G.gnz) {
         gd = __ldg(dose_grad + S.out_off + x + (long long)P.size[0] * (y + (long long)P.size[1] * z));
-        bi = mv(S.MB, mk((float)x - G.lim_off[0], (float)y - G.lim_off[1], (float)z - G.lim_off[2]));
+        const f3 bi = mv(S.MB, mk(dx, dy, dz));
         if (bi.x < -2.f || bi.y < -2.f || bi.z < -2.f || bi.x > G.bev[0] + 2.f || bi.y > G.bev[1] + 2.f ||
             bi.z > G.bev[2] + 2.f)
             gd = 0.f;
@@ -979,6 +980,10 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
             const int l = max(0, (int)floorf(lo - 1e-3f)), h = min(dim - 1, (int)floorf(hi + 1e-3f) + 1);
             s_box[slot] = l;
             s_box[slot + 1] = h - l + 1;
+            // this cone's map for the voxels: the row [A | -q0] of REV axis a
+            // (the forward gather forms q in the same order)
+            s_A[a] = make_float4(Ar[0], Ar[1], Ar[2], -R.q0[a]);
+            s_box[6 + a] = R.rev[a];
         }
         __syncthreads();
         const int l0 = s_box[0], n0 = s_box[1], l1 = s_box[2], n1 = s_box[3], l2 = s_box[4], n2 = s_box[5];
@@ -988,26 +993,30 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
             for (int k = t; k < nbox; k += blockDim.x) acc[k] = 0.f;
             __syncthreads();
             if (gd != 0.f) {
-                f3 q = mv(R.M, bi) - ld3(R.q0);
-                if (!(q.y >= (float)R.rev[0] || q.z >= (float)R.rev[1] || q.x >= (float)R.rev[2] || q.x < 0.f ||
-                      q.y < 0.f || q.z < 0.f)) {
+                const float4 a0 = s_A[0], a1 = s_A[1], a2 = s_A[2];
+                const f3 q = mk(fmaf(a0.x, dx, fmaf(a0.y, dy, fmaf(a0.z, dz, a0.w))),
+                                fmaf(a1.x, dx, fmaf(a1.y, dy, fmaf(a1.z, dz, a1.w))),
+                                fmaf(a2.x, dx, fmaf(a2.y, dy, fmaf(a2.z, dz, a2.w))));
+                const int rv0 = s_box[6], rv1 = s_box[7], rv2 = s_box[8];
+                if (!(q.y >= (float)rv0 || q.z >= (float)rv1 || q.x >= (float)rv2 || q.x < 0.f || q.y < 0.f ||
+                      q.z < 0.f)) {
                     float f0 = floorf(q.y), f1 = floorf(q.z), f2 = floorf(q.x);
                     int i0 = (int)f0, i1 = (int)f1, i2 = (int)f2;
                     float a0 = q.y - f0, a1 = q.z - f1, a2 = q.x - f2;
 #pragma unroll
                     for (int d2 = 0; d2 < 2; d2++) {
                         int k2 = i2 + d2 - l2;
-                        if (i2 + d2 >= R.rev[2] || k2 < 0 || k2 >= n2) continue;
+                        if (i2 + d2 >= rv2 || k2 < 0 || k2 >= n2) continue;
                         float w2 = (d2 ? a2 : 1.f - a2) * gd;
 #pragma unroll
                         for (int d1 = 0; d1 < 2; d1++) {
                             int k1 = i1 + d1 - l1;
-                            if (i1 + d1 >= R.rev[1] || k1 < 0 || k1 >= n1) continue;
+                            if (i1 + d1 >= rv1 || k1 < 0 || k1 >= n1) continue;
                             float w1 = (d1 ? a1 : 1.f - a1) * w2;
 #pragma unroll
                             for (int d0 = 0; d0 < 2; d0++) {
                                 int k0 = i0 + d0 - l0;
-                                if (i0 + d0 >= R.rev[0] || k0 < 0 || k0 >= n0) continue;
+                                if (i0 + d0 >= rv0 || k0 < 0 || k0 >= n0) continue;
                                 atomicAdd(acc + k1 + n1 * (k0 + n0 * k2), (d0 ? a0 : 1.f - a0) * w1);
                             }
                         }
@@ -1034,7 +1043,10 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
         } else if (nbox > GT_SMEM && gd != 0.f) {
             // footprint too large for shared memory (not expected for 8x8x4
             // tiles): scatter directly
-            f3 q = mv(R.M, bi) - ld3(R.q0);
+            const float4 a0 = s_A[0], a1 = s_A[1], a2 = s_A[2];
+            const f3 q = mk(fmaf(a0.x, dx, fmaf(a0.y, dy, fmaf(a0.z, dz, a0.w))),
+                            fmaf(a1.x, dx, fmaf(a1.y, dy, fmaf(a1.z, dz, a1.w))),
+                            fmaf(a2.x, dx, fmaf(a2.y, dy, fmaf(a2.z, dz, a2.w))));
             if (!(q.y >= (float)R.rev[0] || q.z >= (float)R.rev[1] || q.x >= (float)R.rev[2] || q.x < 0.f ||
                   q.y < 0.f || q.z < 0.f))
                 tri_border_scatter(base + R.offset, R.rev[1], R.rev[2], R.rev[0], q.z, q.x, q.y, gd);
