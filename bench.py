@@ -382,10 +382,10 @@ def run_reference(args, ws, rank):
 
 # DRAM bytes (read + write) per crop-box voxel of each stage, from an ncu
 # capture of all six chain kernels on eight beams of this workload (dram__bytes
-# of both chunks' launches / sum of V_beam = 12.37 M); roofline.traffic scales
+# of one call's launches / sum of V_beam = 12.37 M); roofline.traffic scales
 # the dominant stage's figure to the profiled step.
-DRAM_BYTES_PER_VBEAM = {"terma": 0.6, "cone": 433.7, "gather": 80.1, "gather_T": 118.4, "cone_T": 292.7,
-                        "terma_T": 3.1, "geometry": 0.0}
+DRAM_BYTES_PER_VBEAM = {"terma": 1.1, "cone": 359.4, "gather": 67.5, "gather_T": 99.0, "cone_T": 243.0,
+                        "terma_T": 3.8, "geometry": 0.0}
 
 
 def algorithmic_bytes(infos):
