@@ -30,6 +30,7 @@ EE_ERR_NOMEM = 5
 EE_ERR_NOT_READY = 6
 EE_ERR_SIDDON_ITER = 7
 EE_ERR_CAPACITY = 8
+EE_ERR_IO = 9
 
 KERNEL_TABLE = 0
 KERNEL_EXP = 1
@@ -163,6 +164,14 @@ _SIGS = {
                                    C.c_void_p, C.POINTER(C.c_int)]),
     "ee_fluence_projection": (C.c_int, [C.c_int, C.POINTER(Frame), C.c_void_p, C.POINTER(EEBeam), C.c_int, C.c_int,
                                         C.c_int, C.c_void_p]),
+    "ee_read_spectrum_file": (C.c_int, [C.c_char_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                        C.c_char_p, C.c_int, C.POINTER(C.c_int)]),
+    "ee_read_mono_kernel": (C.c_int, [C.c_char_p, C.c_void_p]),
+    "ee_read_kernel_radii": (C.c_int, [C.c_char_p, C.c_void_p]),
+    "ee_cumulative_kernel": (C.c_int, [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                       C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                       C.c_void_p]),
+    "ee_fit_exp_kernel": (C.c_int, [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ee_server_create": (C.c_int, [C.c_int, C.c_int, C.c_longlong, C.c_int, C.POINTER(C.c_void_p)]),
     "ee_server_set_physics": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                         C.POINTER(ConvParams), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
@@ -693,3 +702,94 @@ def beam_source(beam):
     if st:
         raise EEError(st, lib.ee_last_error().decode())
     return np.array(list(s)), np.array(list(d))
+
+
+# ------------------------------------------------ kernel tables (dsa files) --
+DSA_NRADII, DSA_NANGLES, DSA_NCATEGORIES = 24, 48, 5
+
+
+def read_spectrum_file(path: str, capacity: int = 64):
+    """Spectrum file (ee_read_spectrum_file): energy, fluence (normalised to
+    unit sum), mu, mu_en as float32 arrays and the kernel file names."""
+    lib = load_library()
+    a = [np.zeros(capacity, np.float32) for _ in range(4)]
+    stride = 256
+    names = C.create_string_buffer(capacity * stride)
+    n = C.c_int(0)
+    _raise_status(lib, lib.ee_read_spectrum_file(os.fsencode(path), capacity, *[_ptr(x) for x in a], names, stride,
+                                                 C.byref(n)))
+    k = n.value
+    nm = [names.raw[i * stride:(i + 1) * stride].split(b"\0", 1)[0].decode() for i in range(k)]
+    return a[0][:k].copy(), a[1][:k].copy(), a[2][:k].copy(), a[3][:k].copy(), nm
+
+
+def read_mono_kernel(path: str) -> np.ndarray:
+    """dsa point-kernel file (ee_read_mono_kernel): [5][48][24] float32."""
+    out = np.zeros((DSA_NCATEGORIES, DSA_NANGLES, DSA_NRADII), np.float32)
+    lib = load_library()
+    _raise_status(lib, lib.ee_read_mono_kernel(os.fsencode(path), _ptr(out)))
+    return out
+
+
+def read_kernel_radii(path: str) -> np.ndarray:
+    """radii.dat (ee_read_kernel_radii): the 24 radial boundaries [cm]."""
+    out = np.zeros(DSA_NRADII, np.float32)
+    lib = load_library()
+    _raise_status(lib, lib.ee_read_kernel_radii(os.fsencode(path), _ptr(out)))
+    return out
+
+
+def cumulative_kernel(energy, fluence, mu, mono, ntheta: int = 8, nphi: int = 6, device: int = 0) -> dict:
+    """The cumulative kernel tables on the GPU (ee_cumulative_kernel).
+    mono: [nE][5][48][24].  Returns cum_total [ntheta][24], cum_weights
+    [5][ntheta][24], poly_total [48][24], poly_weights [5][48][24], conv_theta
+    and conv_phi (degrees, nphi*ntheta/2)."""
+    lib = load_library()
+    e, f, m = (np.ascontiguousarray(x, np.float32) for x in (energy, fluence, mu))
+    k = np.ascontiguousarray(mono, np.float32)
+    n = len(e)
+    if k.shape != (n, DSA_NCATEGORIES, DSA_NANGLES, DSA_NRADII) or len(f) != n or len(m) != n:
+        raise ValueError("mono must be [nE][5][48][24] with nE spectrum entries")
+    nang = nphi * (ntheta // 2)
+    out = dict(cum_total=np.zeros((ntheta, DSA_NRADII), np.float32),
+               cum_weights=np.zeros((DSA_NCATEGORIES, ntheta, DSA_NRADII), np.float32),
+               poly_total=np.zeros((DSA_NANGLES, DSA_NRADII), np.float32),
+               poly_weights=np.zeros((DSA_NCATEGORIES, DSA_NANGLES, DSA_NRADII), np.float32),
+               conv_theta=np.zeros(max(nang, 1), np.float32), conv_phi=np.zeros(max(nang, 1), np.float32))
+    _raise_status(lib, lib.ee_cumulative_kernel(int(device), n, _ptr(e), _ptr(f), _ptr(m), _ptr(k), int(ntheta),
+                                                int(nphi), *[_ptr(out[x]) for x in ("cum_total", "cum_weights",
+                                                                                    "poly_total", "poly_weights",
+                                                                                    "conv_theta", "conv_phi")]))
+    return out
+
+
+def fit_exp_kernel(radii, cum_total):
+    """Per-cone double-exponential fit of a cumulative table
+    (ee_fit_exp_kernel): params [ntheta][4] = (A, a, B, b) and the maximum
+    fit error of each cone relative to its table maximum."""
+    lib = load_library()
+    r = np.ascontiguousarray(radii, np.float32)
+    K = np.ascontiguousarray(cum_total, np.float32)
+    nt = K.shape[0]
+    params = np.zeros((nt, 4), np.float32)
+    err = np.zeros(nt, np.float32)
+    _raise_status(lib, lib.ee_fit_exp_kernel(nt, K.shape[1], _ptr(r), _ptr(K), _ptr(params), _ptr(err)))
+    return params, err
+
+
+def physics_from_kernel_files(spectrum_path: str, kernel_dir: str, ntheta: int = 8, nphi: int = 6,
+                              spacing_cm: float = 0.25, penumbra_cm: float = 1.0, device: int = 0):
+    """inputs.Physics from a spectrum file and its dsa point kernels (the
+    files in kernel_dir, with radii.dat): the cumulative table built on the
+    GPU, the double-exponential fit of it for the exp fast path."""
+    from . import inputs
+    energy, fluence, mu, mu_en, names = read_spectrum_file(spectrum_path)
+    mono = np.stack([read_mono_kernel(os.path.join(kernel_dir, n)) for n in names])
+    radii = read_kernel_radii(os.path.join(kernel_dir, "radii.dat"))
+    t = cumulative_kernel(energy, fluence, mu, mono, ntheta, nphi, device)
+    params, _ = fit_exp_kernel(radii, t["cum_total"])
+    return inputs.Physics(energy=energy, fluence=fluence, mu=mu, mu_en=mu_en, ntheta=ntheta, nphi=nphi,
+                          radii=radii.astype(np.float64), exp_params=params.astype(np.float64),
+                          cumkern=t["cum_total"].astype(np.float64), theta_deg=t["conv_theta"].astype(np.float64),
+                          phi_deg=t["conv_phi"].astype(np.float64), rev_latspacing=spacing_cm,
+                          rev_longspacing=spacing_cm, penumbra=penumbra_cm)

@@ -50,7 +50,8 @@ typedef enum {
     EE_ERR_NOT_READY = 6,     /* volume, spectrum or kernel not set             */
     EE_ERR_SIDDON_ITER = 7,   /* ray trace hit its iteration cap
                                  (reference: assert, cudaSiddon.cu:112)         */
-    EE_ERR_CAPACITY = 8       /* caller-provided scratch too small              */
+    EE_ERR_CAPACITY = 8,      /* caller-provided scratch too small              */
+    EE_ERR_IO = 9             /* input file missing or malformed                */
 } ee_status;
 
 /* line-convolution kernel representation */
@@ -364,6 +365,44 @@ int ee_ct_to_density(int device, const ee_frame *ct, const float *hu, float iso_
                      const float *lut_density, int nlut, float *density, int out_size[3]);
 int ee_fluence_projection(int device, const ee_frame *mask_frame, const float *mask, const ee_beam *beams, int nbeams,
                           int supersample, int aperture_ready, float *fluence);
+
+/* ---- kernel tables from measured point kernels (dosecalc-preprocess) ----
+ * Replace read_spectrum_file (CCCS/DoseCalcIO/spectra.cpp:7-62), read_kernel
+ * (CCCS/DoseCalcIO/kernel.cpp:27-122), make_poly_kernel (kernel.cpp:123-258)
+ * and make_cumulative_kernel (kernel.cpp:260-431); the outputs are what the
+ * reference stores in cumulative_kernel.h5 (total_weights, weights) and
+ * convolution_{theta,phi}_angles.raw, bit for bit.
+ * ee_read_spectrum_file: records "energy fluence mu mu_en kernel_file" until
+ * the first that does not parse; fluence divided by its FP32 sum; kernel file
+ * names NUL-terminated at kernel_names + i * name_stride (may be NULL).  *n
+ * is the record count (EE_ERR_CAPACITY when above capacity).
+ * ee_read_mono_kernel: a dsa kernel file, 48 polar x 24 radial cells of seven
+ * (value, uncertainty) pairs; weights = the five category values as
+ * [5][48][24] (primary, first scatter, second scatter, multiple scatter,
+ * bremsstrahlung + annihilation).
+ * ee_read_kernel_radii: radii.dat, the 24 radial boundaries [cm].
+ * ee_cumulative_kernel (GPU): mono = [nkernels][5][48][24]; poly kernel
+ * weighted by fluence*energy*mu per category, total = sum of categories,
+ * 48/ntheta polar bins summed per cone, running sum over radius.
+ * cum_total [ntheta][24] is what ee_set_kernel_table takes; cum_weights
+ * [5][ntheta][24], poly_total [48][24], poly_weights [5][48][24] and the
+ * nphi*ntheta/2 cone angles may be NULL.  ntheta even and a divisor of 48.
+ * ee_fit_exp_kernel (host): per cone the least-squares (A, a, B, b), A, B >= 0,
+ * of A/a (1 - e^{-a r}) + B/b (1 - e^{-b r}) to the cumulative table at the
+ * radii: the ee_set_kernel_exp parameters for these kernels.  max_rel_err[t]
+ * (may be NULL) = max |fit - table| / max |table| of cone t. */
+#define EE_DSA_NRADII 24
+#define EE_DSA_NANGLES 48
+#define EE_DSA_NCATEGORIES 5
+int ee_read_spectrum_file(const char *path, int capacity, float *energy, float *fluence, float *mu, float *mu_en,
+                          char *kernel_names, int name_stride, int *n);
+int ee_read_mono_kernel(const char *path, float *weights);
+int ee_read_kernel_radii(const char *path, float *radii);
+int ee_cumulative_kernel(int device, int nkernels, const float *energy, const float *fluence, const float *mu,
+                         const float *mono, int ntheta, int nphi, float *cum_total, float *cum_weights,
+                         float *poly_total, float *poly_weights, float *conv_theta_deg, float *conv_phi_deg);
+int ee_fit_exp_kernel(int ntheta, int nradii, const float *radii, const float *cum_total, float *params,
+                      float *max_rel_err);
 
 /* ---- diagnostics ---- */
 /* Stage ids for ee_read_profile. */

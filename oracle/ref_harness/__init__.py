@@ -156,3 +156,38 @@ class BeamletHarness(ReferenceHarness):
         if st != 0:
             raise RuntimeError(f"reference beamlet harness status {st}")
         return idx[:n], cols[:n], list(info)
+
+
+_LIB_KT = None
+
+
+def _lib_kernel():
+    global _LIB_KT
+    if _LIB_KT is None:
+        lib = C.CDLL(_build.build(which="kernel"))
+        lib.ccref_kernel_build.restype = C.c_int
+        _LIB_KT = lib
+    return _LIB_KT
+
+
+def kernel_build(data_dir: str, spectrum: str, ntheta: int = 8, nphi: int = 6) -> dict:
+    """The reference's own spectrum + kernel-table build (read_spectrum_file,
+    read_kernel, make_poly_kernel, make_cumulative_kernel) run on the CPU on
+    data_dir/spectra/<spectrum>.spec and data_dir/dsa/*."""
+    lib = _lib_kernel()
+    tmp = os.path.join(_build.OUT, "tmp")
+    os.makedirs(tmp, exist_ok=True)
+    z = lambda *s: np.zeros(s, np.float32)
+    nang = nphi * (ntheta // 2)
+    sp = [z(64) for _ in range(4)]
+    out = dict(poly_total=z(48, 24), poly_weights=z(5, 48, 24), cum_total=z(ntheta, 24),
+               cum_weights=z(5, ntheta, 24), radii=z(24), ang_bounds=z(ntheta), conv_theta=z(nang), conv_phi=z(nang))
+    p = lambda a: a.ctypes.data_as(C.c_void_p)
+    n = lib.ccref_kernel_build(os.fsencode(data_dir), os.fsencode(tmp), spectrum.encode(), int(nphi), int(ntheta),
+                               *[p(a) for a in sp], *[p(out[k]) for k in ("poly_total", "poly_weights", "cum_total",
+                                                                          "cum_weights", "radii", "ang_bounds",
+                                                                          "conv_theta", "conv_phi")])
+    if n <= 0:
+        raise RuntimeError(f"reference kernel build failed for {spectrum} ({n})")
+    out.update(energy=sp[0][:n].copy(), fluence=sp[1][:n].copy(), mu=sp[2][:n].copy(), mu_en=sp[3][:n].copy())
+    return out

@@ -1,9 +1,10 @@
 """Build recipe for the reference harness (test infrastructure only).
 
-Compiles oracle/ref_harness/ref_harness.cpp (dosecalc-beam kernels) and
-ref_beamlet_harness.cpp (dosecalc-beamlet kernels), which include the
-reference's own kernel sources from the reference checkout, into
-oracle/_ref/libccref.so and oracle/_ref/libccref_beamlet.so with the host C++
+Compiles oracle/ref_harness/ref_harness.cpp (dosecalc-beam kernels),
+ref_beamlet_harness.cpp (dosecalc-beamlet kernels) and ref_kernel_harness.cpp
+(spectrum + kernel-table build), which include the reference's own sources
+from the reference checkout, into oracle/_ref/libccref.so,
+libccref_beamlet.so and libccref_kernel.so with the host C++
 compiler (kernels executed on the CPU through cuda_cpu_shim.h).  Needs the reference checkout; the library is git-ignored
 and is only used to pin the oracle and to regenerate tests/golden.
 """
@@ -16,7 +17,8 @@ ORACLE = os.path.dirname(HERE)
 OUT = os.path.join(ORACLE, "_ref")
 LIB = os.path.join(OUT, "libccref.so")
 LIBS = {"beam": ("ref_harness.cpp", LIB),
-        "beamlet": ("ref_beamlet_harness.cpp", os.path.join(OUT, "libccref_beamlet.so"))}
+        "beamlet": ("ref_beamlet_harness.cpp", os.path.join(OUT, "libccref_beamlet.so")),
+        "kernel": ("ref_kernel_harness.cpp", os.path.join(OUT, "libccref_kernel.so"))}
 REF = os.environ.get("CCCS_REFERENCE", "/root/reference")
 
 
@@ -30,8 +32,8 @@ def build(verbose=False, which="beam"):
     os.makedirs(OUT, exist_ok=True)
     srcname, LIB = LIBS[which]
     src = os.path.join(HERE, srcname)
-    if os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(src),
-                                                            os.path.getmtime(os.path.join(HERE, "cuda_cpu_shim.h"))):
+    deps = [src] + [os.path.join(HERE, h) for h in ("cuda_cpu_shim.h", "H5Cpp.h")]
+    if os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(d) for d in deps):
         return LIB
     cuda_inc = "/usr/local/cuda/include"
     cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-w",

@@ -10,7 +10,12 @@ Needs the reference checkout (default /root/reference, or $CCCS_REFERENCE).
 Each fixture stores its complete inputs, so tests never depend on the
 generators in endtoend_gb300/inputs.py staying unchanged.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py          # every fixture
+    python tests/golden/make_golden.py kernel   # the kernel-table fixtures only
+
+The kernel-table fixtures in tests/golden/kernel come from the reference's
+spectrum and kernel-table build (spectra.cpp, kernel.cpp) run on the CPU by
+oracle/ref_harness/ref_kernel_harness.cpp.
 """
 import os
 import sys
@@ -19,9 +24,11 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+sys.path.insert(0, os.path.dirname(HERE))
 
 from endtoend_gb300 import inputs  # noqa: E402
-from oracle.ref_harness import BeamletHarness, ReferenceHarness, sparsify  # noqa: E402
+from oracle.ref_harness import BeamletHarness, ReferenceHarness, kernel_build, sparsify  # noqa: E402
+import golden_cases  # noqa: E402
 
 
 def cases():
@@ -112,7 +119,41 @@ def main_beamlet():
         np.savez_compressed(os.path.join(HERE, "beamlet", f"{name}.npz"), **out)
 
 
+KT_KEYS = ("energy", "fluence", "mu", "mu_en", "poly_total", "poly_weights", "cum_total", "cum_weights", "radii",
+           "ang_bounds", "conv_theta", "conv_phi")
+
+
+def main_kernel():
+    """Kernel-table fixtures from the reference's read_spectrum_file /
+    read_kernel / make_poly_kernel / make_cumulative_kernel: seeded synthetic
+    point kernels (inputs stored) in every (ntheta, nphi) of KERNEL_CONFIGS,
+    and the outputs only of the 6 MV spectrum with the measured dsa kernels."""
+    os.makedirs(golden_cases.KERNEL, exist_ok=True)
+    ref = os.environ.get("CCCS_REFERENCE", "/root/reference")
+    scratch = os.path.join(os.path.dirname(os.path.dirname(HERE)), "oracle", "_ref", "tmp")
+    for seed in (11, 12):
+        spec, mono = golden_cases.synthetic_dsa(seed)
+        d = os.path.join(scratch, f"synth{seed}")
+        golden_cases.write_dsa_files(d, spec, mono)
+        out = {"spec": spec, "mono": mono}
+        for nt, nph in golden_cases.KERNEL_CONFIGS:
+            r = kernel_build(d, golden_cases.SYNTH_SPECTRUM, nt, nph)
+            for k in KT_KEYS:   # the spectrum and poly kernel do not depend on the cones
+                once = k in ("energy", "fluence", "mu", "mu_en", "poly_total", "poly_weights", "radii")
+                out[k if once else f"nt{nt}_np{nph}_{k}"] = r[k]
+        np.savez_compressed(os.path.join(golden_cases.KERNEL, f"synth{seed}.npz"), **out)
+        print("kernel fixture synth", seed, "cum_total[0,-1]", float(out["nt8_np6_cum_total"][0, -1]))
+    r = kernel_build(os.path.join(ref, "CCCS", "data"), "spec_6X", 8, 6)
+    np.savez_compressed(os.path.join(golden_cases.KERNEL, "spec_6X_measured.npz"),
+                        **{f"nt8_np6_{k}": r[k] for k in KT_KEYS if k not in ("poly_weights",)})
+    print("kernel fixture spec_6X", r["cum_total"][:, -1])
+
+
 def main():
+    if sys.argv[1:] == ["kernel"]:
+        main_kernel()
+        return
+    main_kernel()
     main_beamlet()
     for name, vol, phys, beams in cases():
         h = ReferenceHarness(vol, phys, tex_emulate=True)

@@ -62,3 +62,61 @@ def load_beamlet(name):
                        fluence=z["beam_fluence"].astype(np.float32))
     ref = {k: z[k] for k in ("beamlet_index", "col_ptr", "row_index", "value", "info", "ref_noise")}
     return (vol, phys, beam, float(z["kernel_extent"]), tuple(int(v) for v in z["max_rev"]), float(z["thresh"]), ref)
+
+
+# ---------------------------------------------------- kernel-table fixtures --
+KERNEL = os.path.join(GOLDEN, "kernel")
+KERNEL_CONFIGS = [(8, 6), (12, 8), (4, 4), (48, 2)]   # (ntheta, nphi)
+SYNTH_SPECTRUM = "spec_synth"
+
+
+def synthetic_dsa(seed, nE=4):
+    """Seeded FP32 inputs of a kernel-table build with the magnitudes of the
+    measured kernels (forward-peaked, falling with radius, five categories):
+    spectrum rows (energy, raw fluence, mu, mu_en) and mono [nE][5][48][24]."""
+    rng = np.random.default_rng(seed)
+    E = np.sort(rng.uniform(0.2, 6.0, nE))
+    spec = np.stack([E, rng.uniform(0.01, 0.1, nE), 0.07 * E ** -0.48, 0.03 * E ** -0.08], 1).astype(np.float32)
+    r = inputs.KERNEL_RADII_CM
+    th = (np.arange(48) + 0.5) * np.pi / 48
+    dr = np.diff(np.concatenate([[0.0], r]))
+    fwd = np.exp(-3.0 * th)[None, :, None] * rng.uniform(0.8, 1.2, (nE, 48, 1))
+    mono = np.zeros((nE, 5, 48, 24))
+    for e in range(nE):
+        mono[e, 0] = np.exp(-(4.0 + e) * r)[None, :] * dr * rng.uniform(0.5, 1.5, (48, 24))
+        for c in (1, 2, 3):
+            mono[e, c] = 0.1 * np.exp(-0.4 * r)[None, :] * dr * rng.uniform(0.5, 1.5, (48, 24))
+        mono[e, 4] = 1e-4 * rng.uniform(0.0, 1.0, (48, 24))
+        mono[e] *= fwd[e][None]
+    return spec, mono.astype(np.float32)
+
+
+def write_dsa_files(data_dir, spec, mono):
+    """The inputs as the reference's text files: spectra/spec_synth.spec,
+    dsa/synth<e>, dsa/radii.dat, dsa/polar.dat.  Every FP32 value is printed
+    with nine significant digits, so any reader gets it back exactly."""
+    os.makedirs(os.path.join(data_dir, "spectra"), exist_ok=True)
+    os.makedirs(os.path.join(data_dir, "dsa"), exist_ok=True)
+    f9 = lambda v: "%.8E" % float(v)
+    lines = ["%s %s %s %s synth%d" % (f9(a), f9(b), f9(c), f9(d), e) for e, (a, b, c, d) in enumerate(spec)]
+    open(os.path.join(data_dir, "spectra", SYNTH_SPECTRUM + ".spec"), "w").write("\n".join(lines) + "\n")
+    radii = inputs.KERNEL_RADII_CM.astype(np.float32)
+    open(os.path.join(data_dir, "dsa", "radii.dat"), "w").write("".join(" %s\n" % f9(v) for v in radii))
+    open(os.path.join(data_dir, "dsa", "polar.dat"), "w").write(
+        "".join("  %s\n" % f9(np.float32((j + 0.5) * np.pi / 48)) for j in range(48)))
+    for e in range(mono.shape[0]):
+        rows = []
+        for j in range(48):
+            for i in range(24):
+                vals = list(mono[e, :, j, i]) + [radii[i], np.float32((j + 0.5) * 3.75)]
+                rows += ["  %s    %s" % (f9(v), f9(0.0)) for v in vals]
+        open(os.path.join(data_dir, "dsa", "synth%d" % e), "w").write("\n".join(rows) + "\n")
+    return os.path.join(data_dir, "spectra", SYNTH_SPECTRUM + ".spec"), os.path.join(data_dir, "dsa")
+
+
+def kernel_names():
+    return sorted(os.path.splitext(os.path.basename(p))[0] for p in glob.glob(os.path.join(KERNEL, "*.npz")))
+
+
+def load_kernel(name):
+    return dict(np.load(os.path.join(KERNEL, name + ".npz")))
