@@ -1,8 +1,10 @@
-"""In-tree build of the CUDA engine library ``endtoend_gb300/_lib/libee_cccs.so``.
+"""In-tree build of the CUDA engine library ``endtoend_gb300/_lib/libee_cccs.so``
+and of the ``dosecalc-beam`` command-line program on top of it.
 
-nvcc, one ``-gencode`` for sm_103a, the two translation units compiled in
+nvcc, one ``-gencode`` for sm_103a, the translation units compiled in
 parallel, then linked as a shared library with the C ABI of include/ee_cccs.h.
-No torch, no cmake: the result loads with ctypes (or any C FFI).
+No torch, no cmake: the result loads with ctypes (or any C FFI).  The
+program (csrc/ee_dosecalc_beam.cpp) is host C++ that uses only that ABI.
 """
 import os
 import shutil
@@ -17,6 +19,8 @@ LIB = os.path.join(OUT_DIR, "libee_cccs.so")
 SOURCES = ["ee_kernels.cu", "ee_api.cpp", "ee_noalloc.cu", "ee_server.cpp", "ee_beamlet.cu", "ee_anneal.cu", "ee_preprocess.cu", "ee_kernel_tables.cu"]
 HEADERS = ["ee_internal.h", "ee_device.cuh", os.path.join("..", "..", "include", "ee_cccs.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+CLI_SRC = os.path.join(CSRC, "ee_dosecalc_beam.cpp")
+CLI = os.path.join(OUT_DIR, "dosecalc-beam")
 
 
 def nvcc_path():
@@ -36,6 +40,26 @@ def _stale():
     deps = [os.path.join(CSRC, s) for s in SOURCES] + [os.path.normpath(os.path.join(CSRC, h)) for h in HEADERS]
     deps.append(os.path.abspath(__file__))
     return any(os.path.getmtime(d) > t for d in deps)
+
+
+def build_cli(verbose=False, force=False):
+    """The dosecalc-beam program (host C++ over the C ABI; rpath $ORIGIN)."""
+    build(verbose=verbose, force=force)
+    if not force and os.path.exists(CLI) and os.path.getmtime(CLI) >= max(
+            os.path.getmtime(p) for p in (CLI_SRC, LIB, os.path.join(ROOT, "include", "ee_cccs.h"))):
+        return CLI
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if not cxx:
+        raise RuntimeError("a host C++ compiler is required to build dosecalc-beam")
+    tmp = CLI + ".tmp"
+    cmd = [cxx, "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"), CLI_SRC, "-o", tmp, "-L", OUT_DIR,
+           "-lee_cccs", "-Wl,-rpath,$ORIGIN"]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    if subprocess.call(cmd) != 0:
+        raise RuntimeError("building dosecalc-beam failed")
+    os.replace(tmp, CLI)
+    return CLI
 
 
 def build(verbose=False, force=False):
@@ -70,3 +94,4 @@ def build(verbose=False, force=False):
 
 if __name__ == "__main__":
     print(build(verbose=True, force="-f" in sys.argv))
+    print(build_cli(verbose=True, force="-f" in sys.argv))

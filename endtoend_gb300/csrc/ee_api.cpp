@@ -407,6 +407,9 @@ int pipeline(ee_context* c, const PipeArgs& A) {
     const bool adj = A.d_fgrad != nullptr;
     if (adj && !A.d_dose_grad && !A.loss) return fail(EE_ERR_INVALID_ARG, "adjoint needs a dose gradient or a loss");
     if (A.loss && (!fwd || A.dose_mode != EE_DOSE_SUM)) return fail(EE_ERR_INVALID_ARG, "loss needs the summed dose");
+    if (adj && c->P.ss > 1)
+        return fail(EE_ERR_INVALID_ARG, "TERMA supersampling (ss_factor %d) is forward-only; set it to 1 for adjoints",
+                    c->P.ss);
     EE_CUDA(cudaSetDevice(c->device));
     cudaStream_t s = c->stream;
     const int n = A.nbeams;
@@ -746,6 +749,7 @@ int ee_create(int device, ee_context** out) {
         return fail(EE_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
     }
     c->P.mode = EE_KERNEL_TABLE;
+    c->P.ss = 1;
     *out = c;
     return EE_OK;
 }
@@ -905,6 +909,14 @@ int ee_set_kernel_mode(ee_context* c, int mode) {
     if (mode != EE_KERNEL_TABLE && mode != EE_KERNEL_EXP) return fail(EE_ERR_INVALID_ARG, "bad kernel mode %d", mode);
     if (mode == EE_KERNEL_EXP && !c->have_exp) return fail(EE_ERR_NOT_READY, "ee_set_kernel_exp has not been called");
     c->P.mode = mode;
+    return EE_OK;
+}
+
+int ee_set_terma_supersampling(ee_context* c, int ss_factor) {
+    if (!c) return fail(EE_ERR_INVALID_ARG, "null context");
+    if (ss_factor < 1 || ss_factor > 8) return fail(EE_ERR_INVALID_ARG, "ss_factor %d outside [1, 8]", ss_factor);
+    std::lock_guard<std::mutex> lk(c->mu);
+    c->P.ss = ss_factor;
     return EE_OK;
 }
 

@@ -26,6 +26,7 @@
 
 namespace {
 
+template <bool SUPERSAMPLE>
 __global__ void __launch_bounds__(256) k_terma(EeParams P, const EeBeamSpec* __restrict__ specs,
                                                EeBeamGeom* __restrict__ geoms, const float* __restrict__ fluence,
                                                float* __restrict__ terma, float* __restrict__ unit, int* __restrict__ bl_idx) {
@@ -42,9 +43,34 @@ __global__ void __launch_bounds__(256) k_terma(EeParams P, const EeBeamSpec* __r
         int z = S.t0[2] + (int)(v / ((long long)S.tn[0] * S.tn[1]));
         f3 vox = mk(P.start[0] + x * P.voxel[0], P.start[1] + y * P.voxel[1], P.start[2] + z * P.voxel[2]);
         f3 src = ld3(S.src);
-        int bl = beamlet_of(S, vox);
-        if (bl == -2) bl = beamlet_of_fp64(P, S, x, y, z);
         float t = 0.f, u = 0.f;
+        int bl = -1;
+        if (SUPERSAMPLE) {
+            // supersampled TERMA (cudaSiddon.cu:248-258, 297-306): the mean
+            // over ss^3 sub-voxel centres, each with its own beamlet lookup
+            // and ray trace, summed x fastest (forward only: unit and bl_idx
+            // are not requested)
+            const int ss = P.ss, nsub = ss * ss * ss;
+            const float sv0 = P.voxel[0] / (float)ss, sv1 = P.voxel[1] / (float)ss, sv2 = P.voxel[2] / (float)ss;
+            float acc = 0.f;
+            for (int ii = 0; ii < nsub; ii++) {
+                const int sx = ii % ss, sy = (ii / ss) % ss, sz = ii / (ss * ss);
+                const f3 p = mk(P.start[0] + ((float)x - 0.5f) * P.voxel[0] + ((float)sx + 0.5f) * sv0,
+                                P.start[1] + ((float)y - 0.5f) * P.voxel[1] + ((float)sy + 0.5f) * sv1,
+                                P.start[2] + ((float)z - 0.5f) * P.voxel[2] + ((float)sz + 0.5f) * sv2);
+                int bs = beamlet_of(S, p);
+                if (bs == -2) bs = beamlet_point_fp64(S, (double)p.x, (double)p.y, (double)p.z);
+                if (bs < 0) continue;
+                const float fl = __ldg(fluence + S.fl_off + bs);
+                if (!(fl > 0.f)) continue;
+                const float rpl = siddon_rpl(P, p, src, cap);
+                acc += fl * terma_per_fluence(P, rpl, p, src, S.sad);
+            }
+            t = acc / (float)nsub;
+        } else {
+            bl = beamlet_of(S, vox);
+            if (bl == -2) bl = beamlet_of_fp64(P, S, x, y, z);
+        }
         if (bl >= 0) {
             float fl = __ldg(fluence + S.fl_off + bl);
             if (fl > 0.f || unit) {
@@ -1101,7 +1127,8 @@ cudaError_t ee_launch_terma(const EeParams& P, const EeBeamSpec* specs, EeBeamGe
                             float* terma, float* unit, int* beamlet_idx, int nbeams, long long max_tvol,
                             cudaStream_t s) {
     dim3 grid(grid1(max_tvol, 256), 1, nbeams);
-    k_terma<<<grid, 256, 0, s>>>(P, specs, geoms, fluence, terma, unit, beamlet_idx);
+    if (P.ss > 1) k_terma<true><<<grid, 256, 0, s>>>(P, specs, geoms, fluence, terma, unit, beamlet_idx);
+    else k_terma<false><<<grid, 256, 0, s>>>(P, specs, geoms, fluence, terma, unit, beamlet_idx);
     return cudaGetLastError();
 }
 

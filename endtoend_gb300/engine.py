@@ -124,6 +124,7 @@ _SIGS = {
     "ee_set_kernel_table": (C.c_int, [C.c_void_p, C.POINTER(ConvParams), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ee_set_kernel_exp": (C.c_int, [C.c_void_p, C.c_void_p]),
     "ee_set_kernel_mode": (C.c_int, [C.c_void_p, C.c_int]),
+    "ee_set_terma_supersampling": (C.c_int, [C.c_void_p, C.c_int]),
     "ee_beam_dose": (C.c_int, [C.c_void_p, C.POINTER(EEBeam), C.c_int, C.c_void_p, C.c_void_p, C.c_int]),
     "ee_beam_dose_device": (C.c_int, [C.c_void_p, C.POINTER(EEBeam), C.c_int, C.c_void_p, C.c_void_p, C.c_int]),
     "ee_beam_dose_adjoint": (C.c_int, [C.c_void_p, C.POINTER(EEBeam), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -293,6 +294,10 @@ class Engine:
 
     def set_mode(self, mode: str):
         self._check(self.lib.ee_set_kernel_mode(self.h, KERNEL_EXP if mode == "exp" else KERNEL_TABLE))
+
+    def set_terma_supersampling(self, ss_factor: int):
+        """TERMA supersampling (omni-header ss_factor), forward dose only."""
+        self._check(self.lib.ee_set_terma_supersampling(self.h, int(ss_factor)))
 
     # -- forward dose
     def beam_dose(self, beams: Sequence, per_beam: bool = False, accumulate_into: np.ndarray = None) -> np.ndarray:

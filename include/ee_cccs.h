@@ -136,6 +136,12 @@ int ee_set_kernel_table(ee_context *ctx, const ee_conv_params *conv, const float
 /* params: [ntheta][4] = (A, a, B, b); selects EE_KERNEL_EXP. */
 int ee_set_kernel_exp(ee_context *ctx, const float *params);
 int ee_set_kernel_mode(ee_context *ctx, int mode);
+/* TERMA supersampling (the omni-header ss_factor; cudaSiddon.cu:248-306):
+ * each calc-bbox voxel's TERMA is the mean over ss^3 sub-voxel centres, each
+ * with its own beamlet lookup and ray trace.  1 (the default) = off; up to 8.
+ * Forward dose only: adjoint and loss calls fail with EE_ERR_INVALID_ARG while
+ * it is above 1 (a sub-sampled voxel draws on several beamlets). */
+int ee_set_terma_supersampling(ee_context *ctx, int ss_factor);
 
 /* ---- forward dose (radconvolveTexture) ----
  * fluence: concatenation of the beams' fmap_size[0]*fmap_size[1] maps.

@@ -77,6 +77,7 @@ typedef struct {
     int    max_rev_size[3];
     int    tex_emulate;
     int    nthreads;
+    int    ss_factor;   /* TERMA supersampling per axis (omni-header ss_factor); <= 1: off */
 } orc_setup;
 
 typedef struct {
@@ -340,15 +341,21 @@ static frame_t make_frame(const orc_setup *S) {
     return f;
 }
 
-/* cudaSiddon over the calc bbox (cudaSiddon.cu:210-308, ss_factor = 1).
+/* cudaSiddon over the calc bbox (cudaSiddon.cu:210-308).
  * unit != NULL additionally receives the TERMA per unit fluence and
- * beamlet != NULL the beamlet index of every bbox voxel (adjoint). */
+ * beamlet != NULL the beamlet index of every bbox voxel (adjoint; only
+ * without supersampling).  With ss_factor > 1 each voxel's TERMA is the mean
+ * over ss^3 sub-voxel centres start + (i - 1/2) voxel + (s + 1/2) voxel/ss,
+ * each traced and looked up in the fluence map on its own, summed in the
+ * sub-voxel order x fastest (cudaSiddon.cu:248-258, 297-306). */
 static int compute_terma(const orc_setup *S, const orc_beam *b, const float *fluence, real *terma,
                          real *unit, int *beamlet, r3 src, r3 dir, real az, real zen) {
     frame_t F = make_frame(S);
     const int bx = S->bbox_size[0], by = S->bbox_size[1], bz = S->bbox_size[2];
     long nv = (long)bx * by * bz;
     int iter_err = 0;
+    const int ss = S->ss_factor > 1 ? S->ss_factor : 1;
+    if (ss > 1 && (unit || beamlet)) return ORC_ERR_ARG;
 #ifdef _OPENMP
 #pragma omp parallel for schedule(dynamic, 64) num_threads(S->nthreads) reduction(|| : iter_err)
 #endif
@@ -358,6 +365,27 @@ static int compute_terma(const orc_setup *S, const orc_beam *b, const float *flu
                      F.start.y + (real)(S->bbox_start[1] + y) * F.voxel.y,
                      F.start.z + (real)(S->bbox_start[2] + z) * F.voxel.z);
         real t = 0, u = 0;
+        if (ss > 1) {
+            const int nsub = ss * ss * ss;
+            const r3 sv = mk3(F.voxel.x / (real)ss, F.voxel.y / (real)ss, F.voxel.z / (real)ss);
+            real acc = 0;
+            for (int ii = 0; ii < nsub; ii++) {
+                const int sx = ii % ss, sy = (ii / ss) % ss, sz = ii / (ss * ss);
+                r3 p = mk3(F.start.x + ((real)(S->bbox_start[0] + x) - (real)0.5) * F.voxel.x + ((real)sx + (real)0.5) * sv.x,
+                           F.start.y + ((real)(S->bbox_start[1] + y) - (real)0.5) * F.voxel.y + ((real)sy + (real)0.5) * sv.y,
+                           F.start.z + ((real)(S->bbox_start[2] + z) - (real)0.5) * F.voxel.z + ((real)sz + (real)0.5) * sv.z);
+                int bs = siddon_beamlet(b, p, src, dir, az, zen);
+                if (bs < 0) continue;
+                real fl = (real)fluence[bs];
+                if (!(fl > 0)) continue;
+                int ie = 0;
+                real rpl = siddon_rpl(S, p, F.start, F.end, F.voxel, src, &ie);
+                iter_err = iter_err || ie;
+                acc += fl * terma_unit(S, rpl, p, src, (real)b->sad);
+            }
+            terma[v] = acc / (real)nsub;
+            continue;
+        }
         int bl = siddon_beamlet(b, vox, src, dir, az, zen);
         if (beamlet) beamlet[v] = bl;
         if (bl >= 0) {

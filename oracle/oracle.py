@@ -30,7 +30,7 @@ class OrcSetup(C.Structure):
         ("kernel_mode", C.c_int),
         ("rev_latspacing", C.c_double), ("rev_longspacing", C.c_double), ("penumbra", C.c_double),
         ("max_rev_size", C.c_int * 3),
-        ("tex_emulate", C.c_int), ("nthreads", C.c_int),
+        ("tex_emulate", C.c_int), ("nthreads", C.c_int), ("ss_factor", C.c_int),
     ]
 
 
@@ -109,11 +109,12 @@ class Oracle:
     kernel_mode: 0 = cumulative table (reference), 1 = exact double
     exponential on the reference walk, 2 = O(L) recurrence (same operator as
     1 without radial truncation).  tex_emulate=True rounds texture filter
-    weights to 8 fractional bits like the GPU texture unit.
+    weights to 8 fractional bits like the GPU texture unit.  ss_factor > 1
+    supersamples TERMA with ss^3 sub-voxels per voxel (forward only).
     """
 
     def __init__(self, vol, phys, kernel_mode=0, tex_emulate=False, precision=64, nthreads=None,
-                 max_rev_size=(0, 0, 0)):
+                 max_rev_size=(0, 0, 0), ss_factor=1):
         self.lib = _lib(precision)
         self.vol, self.phys = vol, phys
         self._keep = []
@@ -149,6 +150,7 @@ class Oracle:
         s.max_rev_size[:] = list(max_rev_size)
         s.tex_emulate = int(bool(tex_emulate))
         s.nthreads = int(nthreads or os.cpu_count() or 1)
+        s.ss_factor = int(ss_factor)
         self.setup = s
 
     def _beam(self, b):

@@ -20,7 +20,7 @@ class RefSetup(C.Structure):
                 ("radii", C.POINTER(C.c_float)), ("cumkern", C.POINTER(C.c_float)),
                 ("theta_deg", C.POINTER(C.c_float)), ("phi_deg", C.POINTER(C.c_float)),
                 ("rev_latspacing", C.c_float), ("rev_longspacing", C.c_float), ("penumbra", C.c_float),
-                ("tex_emulate", C.c_int), ("nthreads", C.c_int)]
+                ("tex_emulate", C.c_int), ("nthreads", C.c_int), ("ss_factor", C.c_int)]
 
 
 class RefBeam(C.Structure):
@@ -51,7 +51,7 @@ class ReferenceHarness:
     """The reference's cudaSiddon / cudaRaytrace / RowConvolve / REV2XYZdose
     kernels (cumulative-kernel table) run on the CPU for one beam."""
 
-    def __init__(self, vol, phys, tex_emulate=True, nthreads=None):
+    def __init__(self, vol, phys, tex_emulate=True, nthreads=None, ss_factor=1):
         self.lib = _lib()
         self.vol, self.phys = vol, phys
         keep = self._keep = []
@@ -77,6 +77,7 @@ class ReferenceHarness:
         s.rev_latspacing, s.rev_longspacing, s.penumbra = phys.rev_latspacing, phys.rev_longspacing, phys.penumbra
         s.tex_emulate = int(bool(tex_emulate))
         s.nthreads = int(nthreads or os.cpu_count() or 1)
+        s.ss_factor = int(ss_factor)
         self.setup = s
 
     def beam_dose(self, beam):

@@ -86,7 +86,16 @@ inline float sample(const Tex& t, float x, float y, float z) {
 #define blockDim ccsim::bDim
 #define gridDim ccsim::gDim
 
-inline void __syncthreads() {}
+// __syncthreads for the phase-replay launch (ref_harness.cpp launch_phased):
+// a thread stops when it reaches the barrier of the current phase; with the
+// default limit every barrier is passed (threads run one after another).
+namespace ccsim {
+extern thread_local int barrier_count, phase_limit;
+struct PhaseStop {};
+}  // namespace ccsim
+inline void __syncthreads() {
+    if (++ccsim::barrier_count >= ccsim::phase_limit) throw ccsim::PhaseStop{};
+}
 
 template <class T>
 inline T tex3D(cudaTextureObject_t t, float x, float y, float z) {

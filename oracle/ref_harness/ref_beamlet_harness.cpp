@@ -34,6 +34,7 @@ thread_local float s_subterma[1024];
 namespace ccsim {
 thread_local uint3 tIdx, bIdx;
 thread_local dim3 bDim, gDim;
+thread_local int barrier_count = 0, phase_limit = 2147483647;
 int tex_emulate = 1;
 }  // namespace ccsim
 
@@ -52,6 +53,7 @@ void launch(dim3 grid, dim3 block, int nthreads, F&& body) {
             for (unsigned ty = 0; ty < block.y; ty++)
                 for (unsigned tx = 0; tx < block.x; tx++) {
                     ccsim::tIdx = make_uint3(tx, ty, tz);
+                    ccsim::barrier_count = 0;
                     body();
                 }
     }

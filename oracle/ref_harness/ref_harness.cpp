@@ -32,6 +32,7 @@ thread_local float s_subterma[1024];
 namespace ccsim {
 thread_local uint3 tIdx, bIdx;
 thread_local dim3 bDim, gDim;
+thread_local int barrier_count = 0, phase_limit = 2147483647;
 int tex_emulate = 1;
 }  // namespace ccsim
 
@@ -49,8 +50,41 @@ void launch(dim3 grid, dim3 block, int nthreads, F&& body) {
             for (unsigned ty = 0; ty < block.y; ty++)
                 for (unsigned tx = 0; tx < block.x; tx++) {
                     ccsim::tIdx = make_uint3(tx, ty, tz);
+                    ccsim::barrier_count = 0;
                     body();
                 }
+    }
+}
+
+// A block whose threads exchange values through shared memory between
+// __syncthreads calls (cudaSiddon with TERMA supersampling): the block is run
+// `phases` times; in pass p every thread runs from the start up to its p-th
+// barrier, the last pass runs to the end.  Exact for kernels whose code
+// before a barrier only (re)writes the thread's own shared-memory slots and
+// whose reader of the other slots runs before their owners in the last pass
+// (cudaSiddon: thread x == 0 averages the block's sub-voxels).
+template <class F>
+void launch_phased(dim3 grid, dim3 block, int nthreads, int phases, F&& body) {
+    const long long nb = (long long)grid.x * grid.y * grid.z;
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads)
+    for (long long b = 0; b < nb; b++) {
+        ccsim::gDim = grid;
+        ccsim::bDim = block;
+        ccsim::bIdx = make_uint3((unsigned)(b % grid.x), (unsigned)((b / grid.x) % grid.y), (unsigned)(b / ((long long)grid.x * grid.y)));
+        for (int p = 1; p <= phases; p++) {
+            ccsim::phase_limit = p < phases ? p : 2147483647;
+            for (unsigned tz = 0; tz < block.z; tz++)
+                for (unsigned ty = 0; ty < block.y; ty++)
+                    for (unsigned tx = 0; tx < block.x; tx++) {
+                        ccsim::tIdx = make_uint3(tx, ty, tz);
+                        ccsim::barrier_count = 0;
+                        try {
+                            body();
+                        } catch (const ccsim::PhaseStop&) {
+                        }
+                    }
+        }
+        ccsim::phase_limit = 2147483647;
     }
 }
 
@@ -83,6 +117,7 @@ typedef struct {
     float rev_latspacing, rev_longspacing, penumbra;
     int tex_emulate;
     int nthreads;
+    int ss_factor;  // TERMA supersampling (omni-header ss_factor); <= 1 off
 } ref_setup;
 
 typedef struct {
@@ -132,21 +167,30 @@ int ccref_beam_dose(const ref_setup* S, const ref_beam* B, const float* fluence_
     const unsigned mr = max_diag + (unsigned)(2 * (REV_PAD / min_vox + S->penumbra / min_vox)) + 100;
     const uint3 max_rev = make_uint3(mr, mr, mr);
 
-    // TERMA (cudaSiddon, host.cu:326-341,392-413; ss_factor = 1)
+    // TERMA (cudaSiddon, launch shape of host.cu:326-341, launch :392-413)
     std::vector<float> terma(nb, 0.f);
     std::vector<float> fmap(fluence_map, fluence_map + B->fmap[0] * B->fmap[1]);
     {
         dim3 blk(1, 32, 3);
+        const unsigned ss = S->ss_factor > 1 ? (unsigned)S->ss_factor : 1u;
+        if (ss > 1) {
+            const unsigned nsub = ss * ss * ss;
+            const unsigned tile = (unsigned)floorf(sqrtf(256.f / (float)nsub));
+            blk = dim3(nsub, tile, tile);
+            if (nsub * tile * tile > 1024 || tile == 0) return 4;  // beyond s_subterma / the 256-thread tile rule
+        }
         dim3 grd(bbs.z, (unsigned)ceilf((float)bbs.x / blk.y), (unsigned)ceilf((float)bbs.y / blk.z));
         const float2 bsz = make_float2(B->beamlet[0], B->beamlet[1]);
         const uint2 fsz = make_uint2(B->fmap[0], B->fmap[1]);
         float* tp = terma.data();
         float* fp = fmap.data();
-        launch(grd, blk, nth, [&] {
+        auto body = [&] {
             cudaSiddon(tp, fp, start, make_float3(size), voxel, bb0, bbs, 1.0f, source, direction, iso, B->sad, bsz,
                        fsz, az, zen, B->coll, S->nE, (cudaTextureObject_t)(uintptr_t)&texDens,
                        (cudaTextureObject_t)(uintptr_t)&texSpec, -1);
-        });
+        };
+        if (ss > 1) launch_phased(grd, blk, nth, 3, body);  // two __syncthreads in cudaSiddon
+        else launch(grd, blk, nth, body);
     }
     if (terma_out) std::copy(terma.begin(), terma.end(), terma_out);
 

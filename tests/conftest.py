@@ -10,6 +10,9 @@ if ROOT not in sys.path:
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (runs the sm_103a engine)")
+    # temporary files of the tests stay inside the repository (git-ignored)
+    if config.option.basetemp is None:
+        config.option.basetemp = os.path.join(ROOT, ".pytest_tmp")
 
 
 def _have_gpu():

@@ -12,6 +12,7 @@ generators in endtoend_gb300/inputs.py staying unchanged.
 
     python tests/golden/make_golden.py          # every fixture
     python tests/golden/make_golden.py kernel   # the kernel-table fixtures only
+    python tests/golden/make_golden.py beam [name ...]   # dosecalc-beam fixtures (all, or the named)
 
 The kernel-table fixtures in tests/golden/kernel come from the reference's
 spectrum and kernel-table build (spectra.cpp, kernel.cpp) run on the CPU by
@@ -41,6 +42,10 @@ def cases():
         b.fluence = rng.uniform(0.2, 1.0, b.fluence.shape).astype(np.float32)
         beams.append(b)
     yield "slab32", vol, phys, beams
+    # TERMA supersampling (omni-header ss_factor 3 = the preprocessing
+    # default, and 2): the same slab, two of the beams
+    yield "slab32_ss3", vol, phys, beams[:2]
+    yield "slab32_ss2", vol, phys, beams[1:2]
     vol = inputs.head_neck_phantom(shape=(48, 48, 40), voxel_cm=0.4, seed=1)
     phys = inputs.make_physics(seed=4, spacing_cm=0.4)
     b = inputs.single_beam(fmap=(12, 12), beamlet_cm=0.4, gantry_deg=130.0, couch_deg=25.0)
@@ -153,10 +158,20 @@ def main():
     if sys.argv[1:] == ["kernel"]:
         main_kernel()
         return
+    if sys.argv[1:2] == ["beam"]:
+        main_beam(sys.argv[2:] or None)
+        return
     main_kernel()
     main_beamlet()
+    main_beam()
+
+
+def main_beam(only=None):
     for name, vol, phys, beams in cases():
-        h = ReferenceHarness(vol, phys, tex_emulate=True)
+        if only and name not in only:
+            continue
+        ss = int(name.rsplit("_ss", 1)[1]) if "_ss" in name else 1
+        h = ReferenceHarness(vol, phys, tex_emulate=True, ss_factor=ss)
         out = {
             "density": vol.density, "voxel": vol.voxel, "start": vol.start, "bbox_start": vol.bbox_start,
             "bbox_size": vol.bbox_size, "energy": phys.energy, "sp_fluence": phys.fluence, "mu": phys.mu,
@@ -175,8 +190,25 @@ def main():
             out[f"beam{k}_dose"] = dose.astype(np.float32)
             out[f"beam{k}_terma"] = terma.astype(np.float32)
             out[f"beam{k}_bev"] = bev
-            print(name, k, "Dmax", float(dose.max()), "bev", bev)
+            if ss > 1:
+                # the reference's own sensitivity with supersampling: sub-voxel
+                # samples within FP32 rounding of a beamlet edge (a few per
+                # fixture) resolve by the arithmetic's rounding, moving one
+                # voxel's TERMA by up to a sub-voxel's share.  Max |change|
+                # of dose and TERMA (relative to their maxima) when the
+                # isocentre moves by 1e-6 .. 1e-5 cm along several directions.
+                dn = tn = 0.0
+                shifts = [(1, -1, 1), (-1, 1, -1), (1, 0, 0), (0, 1, 0), (0, 0, 1), (-1, -1, 0), (0, -1, 1), (1, 1, 1)]
+                for j, sh in enumerate(shifts):
+                    bp = inputs.Beam(**{**b.__dict__})
+                    bp.isocenter = np.asarray(b.isocenter, np.float64) + (1e-5 if j % 2 == 0 else 1e-6) * np.array(sh)
+                    d2, t2, _ = h.beam_dose(bp)
+                    dn = max(dn, float(np.abs(d2 - dose).max() / dose.max()))
+                    tn = max(tn, float(np.abs(t2 - terma).max() / terma.max()))
+                out[f"beam{k}_ref_noise"] = [dn, tn]
+            print(name, k, "Dmax", float(dose.max()), "bev", bev, "ref noise", out.get(f"beam{k}_ref_noise"))
         out["nbeams"] = len(beams)
+        out["ss_factor"] = ss
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
 
 

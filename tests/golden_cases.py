@@ -15,6 +15,21 @@ def names():
     return sorted(os.path.splitext(os.path.basename(p))[0] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
 
 
+def ss_factor(name):
+    """TERMA supersampling the fixture was made with (1 when not stored)."""
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    return int(z["ss_factor"]) if "ss_factor" in z else 1
+
+
+def ref_noise(name):
+    """Per beam (dose, TERMA) change of the reference itself under
+    rounding-level isocentre shifts, relative to the maxima (supersampled
+    fixtures); zeros where not stored."""
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    return [tuple(float(v) for v in z[f"beam{k}_ref_noise"]) if f"beam{k}_ref_noise" in z else (0.0, 0.0)
+            for k in range(int(z["nbeams"]))]
+
+
 def load(name):
     z = np.load(os.path.join(GOLDEN, name + ".npz"))
     vol = inputs.Volume(density=z["density"].astype(np.float32), voxel=z["voxel"], start=z["start"],

@@ -1,6 +1,11 @@
 """The oracle against golden outputs of the reference's own dosecalc-beam
 kernel source (cudaSiddon, cudaRaytrace, RowConvolve, REV2XYZdose compiled
-unmodified and run on the CPU; see tests/golden/make_golden.py).
+unmodified and run on the CPU; see tests/golden/make_golden.py), with and
+without TERMA supersampling (fixtures *_ss<k>: ss_factor k).  With
+supersampling a few sub-voxel samples per fixture sit within FP32 rounding of
+a beamlet edge and the reference's arithmetic decides them; the fixtures store
+the reference's own change under 1e-6 .. 1e-5 cm isocentre shifts (dose,
+TERMA), which is added to the bounds below.
 
 Tolerances: crop boxes identical; TERMA within 1e-4 of its maximum in
 99.9 % of voxels and within 2e-3 everywhere (FP32 vs FP64 can resolve a
@@ -18,13 +23,13 @@ from oracle.oracle import Oracle
 @pytest.mark.parametrize("name", golden_cases.names())
 def test_oracle_matches_reference_kernels(name):
     vol, phys, beams, doses, termas, bevs = golden_cases.load(name)
-    o = Oracle(vol, phys, kernel_mode=0, tex_emulate=True)
-    for b, dref, tref, bev in zip(beams, doses, termas, bevs):
+    o = Oracle(vol, phys, kernel_mode=0, tex_emulate=True, ss_factor=golden_cases.ss_factor(name))
+    for b, dref, tref, bev, (dn, tn) in zip(beams, doses, termas, bevs, golden_cases.ref_noise(name)):
         d, info, t = o.beam_dose(b, return_terma=True)
         assert list(info.bev_size) == bev
         rel = np.abs(t - tref) / tref.max()
-        assert np.mean(rel > 1e-4) <= 1e-3 and rel.max() <= 2e-3
-        assert np.abs(d - dref).max() <= 6e-4 * dref.max(), np.abs(d - dref).max() / dref.max()
+        assert np.mean(rel > 1e-4) <= 1e-3 and rel.max() <= 2e-3 + tn
+        assert np.abs(d - dref).max() <= (6e-4 + dn) * dref.max(), np.abs(d - dref).max() / dref.max()
 
 
 def test_golden_fixtures_reproduce_from_reference_source():

@@ -1,0 +1,54 @@
+"""dosecalc-beam end to end on the GPU: the program reads the reference's
+temp-directory contract (tests/dosecalc_contract.py), rebuilds the cumulative
+kernel from the spectrum and point-kernel files, and writes Dose.raw.
+
+- Its dose equals, bit for bit, the same computation made through the
+  library's Python API (same kernel tables, beams, supersampling, kernel mode).
+- Against the FP64 oracle of the same tables: <= 1e-3 of Dmax without TERMA
+  supersampling; <= 5e-3 with ss_factor 3, where a few sub-voxel samples sit
+  within FP32 rounding of a beamlet edge and FP32 and FP64 decide them
+  differently (each moves one voxel's TERMA by up to 1/27 of its share).
+"""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import dosecalc_contract as dc
+import golden_cases
+from endtoend_gb300 import _build, engine
+from oracle.oracle import Oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def _library_dose(vol, beams, data, ss, mode):
+    phys = engine.physics_from_kernel_files(os.path.join(data, "spectra", golden_cases.SYNTH_SPECTRUM + ".spec"),
+                                            os.path.join(data, "dsa"), 8, 6, spacing_cm=0.25, penumbra_cm=1.0)
+    with engine.Engine(0) as e:
+        e.set_volume(vol)
+        e.set_physics(phys, mode=mode)
+        e.set_terma_supersampling(ss)
+        return e.beam_dose([dc.as_engine_beam(d) for d in beams]), phys
+
+
+@pytest.mark.parametrize("ss,mode", [(1, "table"), (3, "table"), (1, "exp")])
+def test_cli_dose(ss, mode, tmp_path):
+    cli = _build.build_cli()
+    vol, beams = dc.slab_case()
+    temp, data = dc.write_contract(str(tmp_path), vol, beams, ss_factor=ss)
+    out = tmp_path / "results" / "Dose.h5"
+    r = subprocess.run([cli, f"--temp={temp}", f"--data={data}", f"--out={out}", f"--kernel={mode}", "--timing"],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    print(r.stdout)
+    dose = np.fromfile(tmp_path / "results" / "Dose.raw", np.float32).reshape(vol.density.shape)
+    ref, phys = _library_dose(vol, beams, data, ss, mode)
+    np.testing.assert_array_equal(dose, ref)
+    if mode == "table":
+        o = Oracle(vol, phys, kernel_mode=0, ss_factor=ss)
+        od = sum(o.beam_dose(dc.as_engine_beam(d))[0] for d in beams)
+        err = float(np.abs(dose - od).max() / od.max())
+        print(f"ss_factor {ss}: dosecalc-beam vs FP64 oracle {err:.2e} of Dmax")
+        assert err <= (1e-3 if ss == 1 else 5e-3)
