@@ -2,8 +2,10 @@
 temp-directory contract (tests/dosecalc_contract.py), rebuilds the cumulative
 kernel from the spectrum and point-kernel files, and writes Dose.raw.
 
-- Its dose equals, bit for bit, the same computation made through the
-  library's Python API (same kernel tables, beams, supersampling, kernel mode).
+- Its dose equals the same computation made through the library's Python API
+  (same kernel tables, beams, supersampling, kernel mode) to 1e-6 of Dmax:
+  beams are summed into the dose with float atomics, so the order of the
+  additions, and with it the last bit of a voxel, can differ between runs.
 - Against the FP64 oracle of the same tables: <= 1e-3 of Dmax without TERMA
   supersampling; <= 5e-3 with ss_factor 3, where a few sub-voxel samples sit
   within FP32 rounding of a beamlet edge and FP32 and FP64 decide them
@@ -45,7 +47,7 @@ def test_cli_dose(ss, mode, tmp_path):
     print(r.stdout)
     dose = np.fromfile(tmp_path / "results" / "Dose.raw", np.float32).reshape(vol.density.shape)
     ref, phys = _library_dose(vol, beams, data, ss, mode)
-    np.testing.assert_array_equal(dose, ref)
+    assert np.abs(dose - ref).max() <= 1e-6 * ref.max()
     if mode == "table":
         o = Oracle(vol, phys, kernel_mode=0, ss_factor=ss)
         od = sum(o.beam_dose(dc.as_engine_beam(d))[0] for d in beams)
