@@ -288,11 +288,12 @@ void build_specs(const EeParams& P, const ee_beam* beams, int nbeams, EeBeamSpec
         off += (long long)B.fmap_size[0] * B.fmap_size[1];
         terma_box(P, S, S.t0, S.tn);
         S.t_off = toff;
-        toff += (long long)S.tn[0] * S.tn[1] * S.tn[2];
+        toff += ee_brick_vol(S.tn);
     }
 }
 
-long long tvol_of(const EeBeamSpec& S) { return (long long)S.tn[0] * S.tn[1] * S.tn[2]; }
+// elements of the beam's bricked TERMA box (4x4x4 bricks, padded)
+long long tvol_of(const EeBeamSpec& S) { return ee_brick_vol(S.tn); }
 
 const char* status_text(int st) {
     switch (st) {
@@ -785,6 +786,11 @@ int ee_set_volume(ee_context* c, const ee_frame* f, const float* density) {
         if (fr.bbox_start[a] < 0 || fr.bbox_start[a] >= fr.size[a]) fr.bbox_start[a] = 0;
         if (fr.bbox_size[a] <= 0 || fr.bbox_size[a] + fr.bbox_start[a] > fr.size[a]) fr.bbox_size[a] = fr.size[a] - fr.bbox_start[a];
     }
+    // every TERMA box lies in the calc bbox; the kernels address a bricked
+    // box with 32-bit offsets
+    if (ee_brick_vol(fr.bbox_size) > 2147483647ll)
+        return fail(EE_ERR_INVALID_ARG, "calc bbox of %d x %d x %d voxels: bricked TERMA boxes above 2^31 elements",
+                    fr.bbox_size[0], fr.bbox_size[1], fr.bbox_size[2]);
     EE_CUDA(cudaSetDevice(c->device));
     size_t n = (size_t)fr.size[0] * fr.size[1] * fr.size[2];
     EE_CUDA(c->density.ensure(n));

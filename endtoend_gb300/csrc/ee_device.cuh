@@ -99,6 +99,100 @@ __device__ __forceinline__ void red_pair(float* p, float a, float b) {
     }
 }
 
+// ------------------------------------------------ bricked TERMA boxes ----
+// Address parts of box element (x, y, z) in the 4x4x4-brick layout
+// (ee_brick_vol): the element sits at bk_x(x) + bk_y(y) + bk_z(z).  32-bit:
+// ee_set_volume keeps the bricked calc bbox, which bounds every box, below 2^31.
+struct Brick {
+    int n0, n1, n2;
+    int sy, sz;  // 64*nbx, 64*nbx*nby
+};
+__device__ __forceinline__ Brick brick_of(const int tn[3]) {
+    Brick B;
+    B.n0 = tn[0]; B.n1 = tn[1]; B.n2 = tn[2];
+    B.sy = 64 * ((tn[0] + 3) >> 2);
+    B.sz = B.sy * ((tn[1] + 3) >> 2);
+    return B;
+}
+__device__ __forceinline__ int bk_x(int x) { return ((x >> 2) << 6) + (x & 3); }
+__device__ __forceinline__ int bk_y(const Brick& B, int y) { return (y >> 2) * B.sy + ((y & 3) << 2); }
+__device__ __forceinline__ int bk_z(const Brick& B, int z) { return (z >> 2) * B.sz + ((z & 3) << 4); }
+
+// tri_border on a bricked box: the same weights, products and order, so the
+// value is bit-identical to tri_border on the x-fastest box.
+__device__ __forceinline__ float tri_brick(const float* __restrict__ v, const Brick& B, float x, float y, float z) {
+    if (!(x > -1.f && x < (float)B.n0 && y > -1.f && y < (float)B.n1 && z > -1.f && z < (float)B.n2)) return 0.f;
+    float fx = floorf(x), fy = floorf(y), fz = floorf(z);
+    int i = (int)fx, j = (int)fy, k = (int)fz;
+    float ax = x - fx, ay = y - fy, az = z - fz;
+    if (i >= 0 && j >= 0 && k >= 0 && i + 1 < B.n0 && j + 1 < B.n1 && k + 1 < B.n2) {
+        const int x0 = bk_x(i), x1 = bk_x(i + 1), y0 = bk_y(B, j), y1 = bk_y(B, j + 1);
+        const int z0 = bk_z(B, k), z1 = bk_z(B, k + 1);
+        const float* p0 = v + z0;
+        const float* p1 = v + z1;
+        float c000 = __ldg(p0 + y0 + x0), c100 = __ldg(p0 + y0 + x1), c010 = __ldg(p0 + y1 + x0),
+              c110 = __ldg(p0 + y1 + x1);
+        float c001 = __ldg(p1 + y0 + x0), c101 = __ldg(p1 + y0 + x1), c011 = __ldg(p1 + y1 + x0),
+              c111 = __ldg(p1 + y1 + x1);
+        float c00 = c000 + ax * (c100 - c000), c10 = c010 + ax * (c110 - c010);
+        float c01 = c001 + ax * (c101 - c001), c11 = c011 + ax * (c111 - c011);
+        float c0 = c00 + ay * (c10 - c00), c1 = c01 + ay * (c11 - c01);
+        return c0 + az * (c1 - c0);
+    }
+    float acc = 0.f;
+#pragma unroll
+    for (int dk = 0; dk < 2; dk++) {
+        int kk = k + dk;
+        if (kk < 0 || kk >= B.n2) continue;
+        float wz = dk ? az : 1.f - az;
+#pragma unroll
+        for (int dj = 0; dj < 2; dj++) {
+            int jj = j + dj;
+            if (jj < 0 || jj >= B.n1) continue;
+            float wy = dj ? ay : 1.f - ay;
+#pragma unroll
+            for (int di = 0; di < 2; di++) {
+                int ii = i + di;
+                if (ii < 0 || ii >= B.n0) continue;
+                float wx = di ? ax : 1.f - ax;
+                acc += wx * wy * wz * __ldg(v + bk_x(ii) + bk_y(B, jj) + bk_z(B, kk));
+            }
+        }
+    }
+    return acc;
+}
+
+// Transpose of tri_brick (same weights as tri_border_scatter): an x-pair
+// inside a brick row is one 16-byte-quad vector reduction, a pair across a
+// brick edge two scalar atomics.
+__device__ __forceinline__ void tri_brick_scatter(float* v, const Brick& B, float x, float y, float z, float g) {
+    if (!(x > -1.f && x < (float)B.n0 && y > -1.f && y < (float)B.n1 && z > -1.f && z < (float)B.n2)) return;
+    float fx = floorf(x), fy = floorf(y), fz = floorf(z);
+    int i = (int)fx, j = (int)fy, k = (int)fz;
+    float ax = x - fx, ay = y - fy, az = z - fz;
+    const bool in0 = i >= 0, in1 = i + 1 < B.n0;
+    const int x0 = in0 ? bk_x(i) : 0, x1 = in1 ? bk_x(i + 1) : 0;
+    const bool quad = in0 && in1 && (i & 3) != 3;
+#pragma unroll
+    for (int dk = 0; dk < 2; dk++) {
+        int kk = k + dk;
+        if (kk < 0 || kk >= B.n2) continue;
+        float wz = dk ? az : 1.f - az;
+#pragma unroll
+        for (int dj = 0; dj < 2; dj++) {
+            int jj = j + dj;
+            if (jj < 0 || jj >= B.n1) continue;
+            float w = (dj ? ay : 1.f - ay) * wz * g;
+            float* row = v + bk_y(B, jj) + bk_z(B, kk);
+            if (quad) red_pair(row + x0, (1.f - ax) * w, ax * w);
+            else {
+                if (in0) atomicAdd(row + x0, (1.f - ax) * w);
+                if (in1) atomicAdd(row + x1, ax * w);
+            }
+        }
+    }
+}
+
 // Transpose of tri_border: atomically scatter g with the trilinear weights,
 // x-adjacent corner pairs as one vector reduction (see red_pair).
 __device__ __forceinline__ void tri_border_scatter(float* v, int nx, int ny, int nz, float x, float y, float z, float g) {

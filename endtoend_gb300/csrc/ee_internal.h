@@ -46,6 +46,17 @@ struct EeRayConst {
     float MKi[9];          // REV -> BEV   (inverseRotateKernelAtOriginRHS)
 };
 
+// TERMA boxes, and their unit-TERMA, beamlet-index and gradient companions,
+// are stored in 4x4x4 bricks so that the eight corners of a trilinear cell,
+// and the cells of neighbouring REV lines, share cache lines whatever the
+// cone's direction.  Box element (x, y, z) sits at bx(x) + by(y) + bz(z):
+//   bx(x) = (x>>2)*64 + (x&3),  by(y) = (y>>2)*64*nbx + (y&3)*4,
+//   bz(z) = (z>>2)*64*nbx*nby + (z&3)*16,   nb* = ceil(n*/4);
+// bricks, and so the rows of 4 x-neighbours, start on 256-byte boundaries.
+inline __host__ __device__ long long ee_brick_vol(const int tn[3]) {
+    return 64ll * ((tn[0] + 3) >> 2) * ((tn[1] + 3) >> 2) * ((tn[2] + 3) >> 2);
+}
+
 // Per-beam constants built on the host.
 struct EeBeamSpec {
     float src[3];
@@ -62,7 +73,7 @@ struct EeBeamSpec {
     // (clipped to the calc bbox); TERMA is identically zero outside it.
     int t0[3];             // origin (full-grid voxel index)
     int tn[3];             // size
-    long long t_off;       // element offset in the TERMA arena
+    long long t_off;       // element offset in the TERMA arena (a multiple of 64: bricks, below)
     // FP64 copies for re-deciding the beamlet of voxels whose FP32 fluence-map
     // coordinate lands within 1e-4 of a beamlet boundary
     double srcd[3];

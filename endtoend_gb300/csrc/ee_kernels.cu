@@ -32,15 +32,33 @@ __global__ void __launch_bounds__(256) k_terma(EeParams P, const EeBeamSpec* __r
                                                float* __restrict__ terma, float* __restrict__ unit, int* __restrict__ bl_idx) {
     const int b = blockIdx.z;
     const EeBeamSpec& S = specs[b];
-    const long long tvol = (long long)S.tn[0] * S.tn[1] * S.tn[2];
+    const long long bvol = ee_brick_vol(S.tn);
     long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     bool nz = false, cap = false;
     f3 bi = mk(0.f, 0.f, 0.f);
-    if (v < tvol) {
+    // threads walk the box brick by brick (4x4x4, ee_brick_vol): each warp
+    // traces half a brick of neighbouring rays and writes 128 contiguous bytes
+    int xr = 0, yr = 0, zr = 0;
+    bool inbox = false;
+    if (v < bvol) {
+        const long long brick = v >> 6;
+        const int w = (int)(v & 63), nbx = (S.tn[0] + 3) >> 2, nby = (S.tn[1] + 3) >> 2;
+        const long long bxy = brick % ((long long)nbx * nby);
+        xr = (int)(bxy % nbx) * 4 + (w & 3);
+        yr = (int)(bxy / nbx) * 4 + ((w >> 2) & 3);
+        zr = (int)(brick / ((long long)nbx * nby)) * 4 + (w >> 4);
+        inbox = xr < S.tn[0] && yr < S.tn[1] && zr < S.tn[2];
+        if (!inbox) {  // padding of the last bricks: never sampled, kept zero
+            terma[S.t_off + v] = 0.f;
+            if (unit) unit[S.t_off + v] = 0.f;
+            if (bl_idx) bl_idx[S.t_off + v] = -1;
+        }
+    }
+    if (inbox) {
         // full-grid voxel index of this TERMA-box voxel
-        int x = S.t0[0] + (int)(v % S.tn[0]);
-        int y = S.t0[1] + (int)((v / S.tn[0]) % S.tn[1]);
-        int z = S.t0[2] + (int)(v / ((long long)S.tn[0] * S.tn[1]));
+        int x = S.t0[0] + xr;
+        int y = S.t0[1] + yr;
+        int z = S.t0[2] + zr;
         f3 vox = mk(P.start[0] + x * P.voxel[0], P.start[1] + y * P.voxel[1], P.start[2] + z * P.voxel[2]);
         f3 src = ld3(S.src);
         float t = 0.f, u = 0.f;
@@ -295,7 +313,7 @@ __device__ __forceinline__ void gather_line(const EeParams& P, const EeBeamSpec&
             } else {
                 r = tex3D<float>(P.dens_tex, g.x + 0.5f, g.y + 0.5f, g.z + 0.5f);
                 if (terma_b)
-                    t = tri_border(terma_b, S.tn[0], S.tn[1], S.tn[2], g.x - (float)S.t0[0], g.y - (float)S.t0[1],
+                    t = tri_brick(terma_b, brick_of(S.tn), g.x - (float)S.t0[0], g.y - (float)S.t0[1],
                                    g.z - (float)S.t0[2]);
             }
         }
@@ -564,7 +582,7 @@ __device__ __forceinline__ float sample_rho(const EeParams& P, const EeBeamSpec&
         g.y >= (float)(P.bb0[1] + P.bbs[1]) || g.z < (float)P.bb0[2] || g.z >= (float)(P.bb0[2] + P.bbs[2]))
         return -2.f;
     if (terma_b)
-        t = tri_border(terma_b, S.tn[0], S.tn[1], S.tn[2], g.x - (float)S.t0[0], g.y - (float)S.t0[1],
+        t = tri_brick(terma_b, brick_of(S.tn), g.x - (float)S.t0[0], g.y - (float)S.t0[1],
                        g.z - (float)S.t0[2]);
     return tex3D<float>(P.dens_tex, g.x + 0.5f, g.y + 0.5f, g.z + 0.5f);
 }
@@ -764,7 +782,7 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_T_lane(EeParams P, const Ee
                 const float tot = a.x + cprev;
                 if (v && tot != 0.f) {
                     f3 gp = F.gl + F.gx * (float)i;
-                    tri_border_scatter(tg, S.tn[0], S.tn[1], S.tn[2], gp.x - (float)S.t0[0], gp.y - (float)S.t0[1],
+                    tri_brick_scatter(tg, brick_of(S.tn), gp.x - (float)S.t0[0], gp.y - (float)S.t0[1],
                                        gp.z - (float)S.t0[2], tot);
                 }
                 if (i < i1) {
@@ -849,7 +867,7 @@ __global__ void __launch_bounds__(CONE_WARPS * 32) k_cone_T(EeParams P, const Ee
         float v = Tb[k];
         if (rho[k] < 0.f || v == 0.f) continue;
         f3 gp = gl + gx * (float)(i0 + k);
-        tri_border_scatter(tg, S.tn[0], S.tn[1], S.tn[2], gp.x - (float)S.t0[0], gp.y - (float)S.t0[1],
+        tri_brick_scatter(tg, brick_of(S.tn), gp.x - (float)S.t0[0], gp.y - (float)S.t0[1],
                            gp.z - (float)S.t0[2], v);
     }
 }
@@ -1088,7 +1106,7 @@ __global__ void __launch_bounds__(256) k_terma_T(EeParams P, const EeBeamSpec* _
                                                  const float* __restrict__ terma_grad, float* __restrict__ fluence_grad) {
     const int b = blockIdx.z;
     const EeBeamSpec& S = specs[b];
-    const long long tvol = (long long)S.tn[0] * S.tn[1] * S.tn[2];
+    const long long tvol = ee_brick_vol(S.tn);  // padding: bl_idx -1
     long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     int bl = -1;
     float val = 0.f;

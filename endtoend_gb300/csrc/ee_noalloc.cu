@@ -100,7 +100,7 @@ extern "C" int ee_beam_dose_noalloc(ee_context* ctx, const ee_beam* beam, const 
     S.t_off = 0;
     const size_t off_geom = align256(sizeof(EeBeamSpec));
     const size_t off_terma = off_geom + align256(sizeof(EeBeamGeom));
-    const long long tvol = (long long)S.tn[0] * S.tn[1] * S.tn[2];
+    const long long tvol = ee_brick_vol(S.tn);  // bricked TERMA box
     const size_t cap_floats = (EE_NOALLOC_SCRATCH_BYTES - off_terma) / sizeof(float);
     if ((size_t)tvol > cap_floats) {
         char m[256];
