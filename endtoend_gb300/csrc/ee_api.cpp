@@ -627,9 +627,12 @@ PlanBound plan_bound(const ee_context* c, const EeBeamSpec& S) {
         long long s0 = (long long)std::ceil((mx[1] - mn[1]) / P.lng) + 2;
         long long s1 = (long long)std::ceil((mx[2] - mn[2]) / P.lat) + 2;
         long long s2 = (long long)std::ceil((mx[0] - mn[0]) / P.lat) + 2;
-        B.rev += s0 * s1 * s2;
+        // bricked REV arrays and 8 x 4 lane tiles, as k_geometry sizes them
+        B.rev += 64 * ((s0 + 3) / 4) * ((s1 + 3) / 4) * ((s2 + 3) / 4);
         B.max_line = (int)std::max<long long>(B.max_line, std::min<long long>(s0, EE_MAX_LINE));
-        B.max_lines = (int)std::max<long long>(B.max_lines, s1 * s2);
+        const long long slots = std::max(((s1 + 7) / 8) * 8 * (((s2 + 3) / 4) * 4),
+                                         ((s2 + 7) / 8) * 8 * (((s1 + 3) / 4) * 4));  // either lateral order
+        B.max_lines = (int)std::max<long long>(B.max_lines, slots);
     }
     // patient AABB of the dilated bound box: t = MBi (b + bmn) + bb0
     double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};

@@ -118,6 +118,16 @@ __device__ __forceinline__ int bk_x(int x) { return ((x >> 2) << 6) + (x & 3); }
 __device__ __forceinline__ int bk_y(const Brick& B, int y) { return (y >> 2) * B.sy + ((y & 3) << 2); }
 __device__ __forceinline__ int bk_z(const Brick& B, int z) { return (z >> 2) * B.sz + ((z & 3) << 4); }
 
+// A cone's REV arrays (dose, dose gradient) are bricked over (tY, tZ, i),
+// tY fastest: dimensions (rev[1], rev[2], rev[0]); ee_brick_vol(rev) floats.
+__device__ __forceinline__ Brick rev_brick(int n0, int n1, int n2) {  // n0 = rev[0] (along the line)
+    Brick B;
+    B.n0 = n1; B.n1 = n2; B.n2 = n0;
+    B.sy = 64 * ((n1 + 3) >> 2);
+    B.sz = B.sy * ((n2 + 3) >> 2);
+    return B;
+}
+
 // tri_border on a bricked box: the same weights, products and order, so the
 // value is bit-identical to tri_border on the x-fastest box.
 __device__ __forceinline__ float tri_brick(const float* __restrict__ v, const Brick& B, float x, float y, float z) {

@@ -242,10 +242,12 @@ __global__ void k_geometry(EeParams P, const EeBeamSpec* __restrict__ specs, EeB
         long long off = 0;
         int ml = 0, mls = 0;
         for (int r = 0; r < P.nrays; r++) {
+            // bricked REV arrays (rev_brick); the lane kernels run one lane
+            // slot per line of an 8 (tY) x 4 (tZ) tile
             G.ray[r].offset = off;
-            off += (long long)G.ray[r].rev[0] * G.ray[r].nlines;
+            off += ee_brick_vol(G.ray[r].rev);
             ml = max(ml, G.ray[r].rev[0]);
-            mls = max(mls, G.ray[r].nlines);
+            mls = max(mls, ((G.ray[r].rev[1] + 7) >> 3) * 8 * (((G.ray[r].rev[2] + 3) >> 2) * 4));
         }
         G.rev_total = off;
         // the gather addresses a cone's REV array with a 32-bit offset
@@ -517,9 +519,9 @@ __global__ void __launch_bounds__(CONE_WARPS * 32) k_cone(EeParams P, const EeBe
     float* rho = sm + (size_t)warp * 3 * maxL;
     float* T = rho + maxL;
     float* D = T + maxL;
-    // REV arena layout: [i][tZ][tY] (line index fastest)
-    const long long nl = R.nlines;
-    float* out = rev + G.arena_off + R.offset + line;
+    // bricked REV arena (rev_brick)
+    const Brick Bv = rev_brick(R.rev[0], R.rev[1], R.rev[2]);
+    float* out = rev + G.arena_off + R.offset + bk_x(tY) + bk_y(Bv, tZ);
     int i0, n;
     line_segment(P, G, R, tY, tZ, L, i0, n);
     if (n > 0) {
@@ -544,7 +546,7 @@ __global__ void __launch_bounds__(CONE_WARPS * 32) k_cone(EeParams P, const EeBe
         }
         __syncwarp();
     }
-    for (int k = lane; k < n; k += 32) out[(long long)(i0 + k) * nl] = D[k];
+    for (int k = lane; k < n; k += 32) out[bk_z(Bv, i0 + k)] = D[k];
 }
 
 // ------------------------------------------- cone: one lane per line ----
@@ -589,6 +591,18 @@ __device__ __forceinline__ float sample_rho(const EeParams& P, const EeBeamSpec&
 
 constexpr int CONE_U = 4;
 
+// Lane slot -> REV line for the one-lane-per-line kernels: the lanes of a
+// warp own an 8 (tY) x 4 (tZ) tile of lines, so at every sample index the
+// warp's reads and writes of the bricked REV arrays fall in two 64-byte brick
+// slabs.  False for slots of a tile that lie outside the cone's array.
+__device__ __forceinline__ bool lane_line(const EeRayGeom& R, int slot, int& tY, int& tZ) {
+    const int wt = slot >> 5, l = slot & 31;
+    const int nty = (R.rev[1] + 7) >> 3;
+    tY = (wt % nty) * 8 + (l & 7);
+    tZ = (wt / nty) * 4 + (l >> 3);
+    return tY < R.rev[1] && tZ < R.rev[2];
+}
+
 template <int LANE_BLOCK>
 __global__ void __launch_bounds__(LANE_BLOCK) k_cone_lane(EeParams P, const EeBeamSpec* __restrict__ specs,
                                                           const EeBeamGeom* __restrict__ geoms,
@@ -598,21 +612,22 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_lane(EeParams P, const EeBe
     const EeBeamGeom& G = geoms[b];
     if (G.status != 0) return;
     const EeRayGeom& R = G.ray[ray];
-    const int line = blockIdx.x * LANE_BLOCK + threadIdx.x;
-    if (line >= R.nlines) return;
+    int tY, tZ;
+    if (!lane_line(R, blockIdx.x * LANE_BLOCK + threadIdx.x, tY, tZ)) return;
     const int L = R.rev[0];
-    const int tY = line % R.rev[1], tZ = line / R.rev[1];
+    const int line = tZ * R.rev[1] + tY;
     int i0, n;
     line_segment(P, G, R, tY, tZ, L, i0, n);
     if (n <= 0) return;
     const EeBeamSpec& S = specs[b];
     const float* tb = terma + S.t_off;
     const LineFrame F = line_frame(R, tY, tZ);
-    // REV arena layout [i][tZ][tY]: lanes (consecutive lines) access
-    // consecutive addresses at every i
+    // bricked REV arena: this line's sample i sits at out + bk_z(i)
+    const Brick Bv = rev_brick(R.rev[0], R.rev[1], R.rev[2]);
+    float* out = rev + G.arena_off + R.offset + bk_x(tY) + bk_y(Bv, tZ);
+    // (rho, T) of each sample, kept from the forward pass for the reverse
+    // one, line-major ([i][line]) in this cone's slot of the scratch
     const long long nl = R.nlines;
-    float* out = rev + G.arena_off + R.offset + line;
-    // (rho, T) of each sample, kept from the forward pass for the reverse one
     float2* smp = samples + G.arena_off + R.offset + line;
     const EeRayConst& RC = P.rays[ray];
     const float delr = P.lng;
@@ -641,7 +656,7 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_lane(EeParams P, const EeBe
                 const float h1 = v ? __expf(e1 * r) : 1.f, h2 = v ? __expf(e2 * r) : 1.f;
                 const float t = v ? tt[j] : 0.f;
                 smp[i * nl] = make_float2(r, t);
-                out[i * nl] = v ? c1 * (Y1 + tm * (1.f - hm1)) + c2 * (Y2 + tm * (1.f - hm2)) : 0.f;
+                out[bk_z(Bv, i)] = v ? c1 * (Y1 + tm * (1.f - hm1)) + c2 * (Y2 + tm * (1.f - hm2)) : 0.f;
                 Y1 = fmaf(h1 * h1, Y1, tm * h1 * (1.f - hm1 * h1));
                 Y2 = fmaf(h2 * h2, Y2, tm * h2 * (1.f - hm2 * h2));
                 tm = t; hm1 = h1; hm2 = h2;
@@ -663,7 +678,7 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_lane(EeParams P, const EeBe
                 ov[j] = 0.f;
                 if (ib - j >= i0) {
                     rt[j] = smp[(ib - j) * nl];
-                    ov[j] = out[(ib - j) * nl];
+                    ov[j] = out[bk_z(Bv, ib - j)];
                 }
             }
 #pragma unroll
@@ -675,7 +690,7 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_lane(EeParams P, const EeBe
                 const float t = v ? rt[j].y : 0.f;
                 const float h1 = v ? __expf(e1 * r) : 1.f, h2 = v ? __expf(e2 * r) : 1.f;
                 const float d = c1 * (Y1 + tm * (1.f - hm1)) + c2 * (Y2 + tm * (1.f - hm2));
-                out[i * nl] = v ? (ov[j] + d) * inv_nphi : 0.f;
+                out[bk_z(Bv, i)] = v ? (ov[j] + d) * inv_nphi : 0.f;
                 Y1 = fmaf(h1 * h1, Y1, tm * h1 * (1.f - hm1 * h1));
                 Y2 = fmaf(h2 * h2, Y2, tm * h2 * (1.f - hm2 * h2));
                 tm = t; hm1 = h1; hm2 = h2;
@@ -698,18 +713,19 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_T_lane(EeParams P, const Ee
     const EeBeamGeom& G = geoms[b];
     if (G.status != 0) return;
     const EeRayGeom& R = G.ray[ray];
-    const int line = blockIdx.x * LANE_BLOCK + threadIdx.x;
-    if (line >= R.nlines) return;
+    int tY, tZ;
+    if (!lane_line(R, blockIdx.x * LANE_BLOCK + threadIdx.x, tY, tZ)) return;
     const int L = R.rev[0];
-    const int tY = line % R.rev[1], tZ = line / R.rev[1];
+    const int line = tZ * R.rev[1] + tY;
     int i0, n;
     line_segment(P, G, R, tY, tZ, L, i0, n);
     if (n <= 0) return;
     const EeBeamSpec& S = specs[b];
     const LineFrame F = line_frame(R, tY, tZ);
-    const long long nl = R.nlines;  // REV arena layout [i][tZ][tY]
+    const long long nl = R.nlines;  // line-major scratch [i][line]
     const long long row = G.arena_off + R.offset + line;
-    const float* gin = rev_grad + row;
+    const Brick Bv = rev_brick(R.rev[0], R.rev[1], R.rev[2]);  // bricked REV gradient
+    const float* gin = rev_grad + G.arena_off + R.offset + bk_x(tY) + bk_y(Bv, tZ);
     float2* sA = scratch + row;  // (pass-A contribution to Tbar[i], rho of sample i)
     const EeRayConst& RC = P.rays[ray];
     const float delr = P.lng, inv_nphi = 1.f / (float)P.nphi;
@@ -732,7 +748,7 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_T_lane(EeParams P, const Ee
                 const int i = ib - j;
                 gl[j] = 0.f;
                 rl[j] = -1.f;
-                if (i >= i0) gl[j] = gin[i * nl];
+                if (i >= i0) gl[j] = gin[bk_z(Bv, i)];
                 if (i > i0) rl[j] = sample_rho(P, S, G, F, i - 1, nullptr, dummy);
             }
 #pragma unroll
@@ -771,7 +787,7 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_T_lane(EeParams P, const Ee
                 const int i = ib + j;
                 gl[j] = 0.f;
                 al[j] = make_float2(0.f, -1.f);
-                if (i <= i1) gl[j] = gin[i * nl];
+                if (i <= i1) gl[j] = gin[bk_z(Bv, i)];
                 if (i < i1) al[j] = sA[(i + 1) * nl];
             }
 #pragma unroll
@@ -837,11 +853,12 @@ __global__ void __launch_bounds__(CONE_WARPS * 32) k_cone_T(EeParams P, const Ee
     line_segment(P, G, R, tY, tZ, L, i0, n);
     if (n == 0) return;
     gather_line(P, S, G, R, nullptr, tY, tZ, i0, n, lane, rho, nullptr);
-    const float* gin = rev_grad + G.arena_off + R.offset + line + (long long)i0 * R.nlines;
+    const Brick Bv = rev_brick(R.rev[0], R.rev[1], R.rev[2]);  // bricked REV gradient
+    const float* gin = rev_grad + G.arena_off + R.offset + bk_x(tY) + bk_y(Bv, tZ);
     const float inv_nphi = 1.f / (float)P.nphi;
     __syncwarp();
     for (int k = lane; k < n; k += 32) {
-        g[k] = rho[k] >= 0.f ? gin[(long long)k * R.nlines] * inv_nphi : 0.f;
+        g[k] = rho[k] >= 0.f ? gin[bk_z(Bv, i0 + k)] * inv_nphi : 0.f;
         Tb[k] = 0.f;
     }
     __syncwarp();
@@ -954,8 +971,8 @@ __global__ void __launch_bounds__(ROW_WARPS * 32) k_gather(EeParams P, const EeB
                 // q.y along the line (rev[0]), q.z -> rev[1], q.x -> rev[2]
                 if (qy >= (float)n0 || qz >= (float)n1 || qx >= (float)n2 || qx < 0.f || qy < 0.f || qz < 0.f)
                     continue;
-                // REV arena layout [i][tZ][tY]: x = tY (q.z), y = tZ (q.x), z = i (q.y)
-                acc += tri_border(base + __float_as_int(rv.w), n1, n2, n0, qz, qx, qy);
+                // bricked REV arrays over (tY, tZ, i): x = tY (q.z), y = tZ (q.x), z = i (q.y)
+                acc += tri_brick(base + __float_as_int(rv.w), rev_brick(n0, n1, n2), qz, qx, qy);
             }
         }
         if (mode == 2) out[rbase + x] = acc;
@@ -1069,6 +1086,7 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
             }
             __syncthreads();
             float* rb = base + R.offset;
+            const Brick Bv = rev_brick(R.rev[0], R.rev[1], R.rev[2]);
             // (k + 0.5) / n is at least 1/(2n) away from an integer, far above
             // the FP32 error for these sizes: the float quotient is exact
             const float inv1 = 1.f / (float)n1, inv0 = 1.f / (float)n0;
@@ -1081,7 +1099,7 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
                     const int k1 = k - q1 * n1;
                     const int k2 = __float2int_rd(((float)q1 + 0.5f) * inv0);
                     const int k0 = q1 - k2 * n0;
-                    atomicAdd(rb + (l1 + k1) + (long long)R.rev[1] * ((l2 + k2) + (long long)R.rev[2] * (l0 + k0)), v);
+                    atomicAdd(rb + bk_x(l1 + k1) + bk_y(Bv, l2 + k2) + bk_z(Bv, l0 + k0), v);
                 }
             }
         } else if (nbox > GT_SMEM && gd != 0.f) {
@@ -1093,7 +1111,7 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
                             fmaf(a2.x, dx, fmaf(a2.y, dy, fmaf(a2.z, dz, a2.w))));
             if (!(q.y >= (float)R.rev[0] || q.z >= (float)R.rev[1] || q.x >= (float)R.rev[2] || q.x < 0.f ||
                   q.y < 0.f || q.z < 0.f))
-                tri_border_scatter(base + R.offset, R.rev[1], R.rev[2], R.rev[0], q.z, q.x, q.y, gd);
+                tri_brick_scatter(base + R.offset, rev_brick(R.rev[0], R.rev[1], R.rev[2]), q.z, q.x, q.y, gd);
         }
         __syncthreads();
     }
