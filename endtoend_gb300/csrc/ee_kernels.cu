@@ -1038,9 +1038,18 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
             // REV axes: q.y -> rev[0] (along the line), q.z -> rev[1], q.x -> rev[2]
             const int dim = a == 1 ? R.rev[0] : (a == 2 ? R.rev[1] : R.rev[2]);
             const int slot = a == 1 ? 0 : (a == 2 ? 2 : 4);
-            const int l = max(0, (int)floorf(lo - 1e-3f)), h = min(dim - 1, (int)floorf(hi + 1e-3f) + 1);
+            int l = max(0, (int)floorf(lo - 1e-3f));
+            const int h = min(dim - 1, (int)floorf(hi + 1e-3f) + 1);
+            int w = h - l + 1;
+            if (a == 2 && w > 0) {
+                // tY range on whole quads: a box row of 4 tY cells is one
+                // 16-byte brick row of the REV gradient (flushed as one vector
+                // reduction); the cells past rev[1] are brick padding
+                w = ((h | 3) + 1) - (l & ~3);
+                l &= ~3;
+            }
             s_box[slot] = l;
-            s_box[slot + 1] = h - l + 1;
+            s_box[slot + 1] = w;
             // this cone's map for the voxels: the row [A | -q0] of REV axis a
             // (the forward gather forms q in the same order)
             s_A[a] = make_float4(Ar[0], Ar[1], Ar[2], -R.q0[a]);
@@ -1051,7 +1060,9 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
         const bool empty = n0 <= 0 || n1 <= 0 || n2 <= 0;
         const int nbox = empty ? 0 : n0 * n1 * n2;
         if (nbox > 0 && nbox <= GT_SMEM) {
-            for (int k = t; k < nbox; k += blockDim.x) acc[k] = 0.f;
+            float4* acc4 = reinterpret_cast<float4*>(acc);  // n1 (tY) is a multiple of 4
+            const int nquad = nbox >> 2;
+            for (int k = t; k < nquad; k += blockDim.x) acc4[k] = make_float4(0.f, 0.f, 0.f, 0.f);
             __syncthreads();
             if (gd != 0.f) {
                 const float4 a0 = s_A[0], a1 = s_A[1], a2 = s_A[2];
@@ -1087,19 +1098,23 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
             __syncthreads();
             float* rb = base + R.offset;
             const Brick Bv = rev_brick(R.rev[0], R.rev[1], R.rev[2]);
-            // (k + 0.5) / n is at least 1/(2n) away from an integer, far above
-            // the FP32 error for these sizes: the float quotient is exact
-            const float inv1 = 1.f / (float)n1, inv0 = 1.f / (float)n0;
-            for (int k = t; k < nbox; k += blockDim.x) {
-                float v = acc[k];
-                if (v != 0.f) {
-                    // tile order k1 (tY) fastest: consecutive threads add to
-                    // consecutive arena addresses
-                    const int q1 = __float2int_rd(((float)k + 0.5f) * inv1);
-                    const int k1 = k - q1 * n1;
+            // one box quad (4 tY cells) per iteration, quad index = kq + nq1 *
+            // (k0 + n0 * k2); (k + 0.5) / n is at least 1/(2n) away from an
+            // integer, far above the FP32 error for these sizes, so the float
+            // quotients are exact.  A non-zero quad is one 16-byte vector
+            // reduction into the bricked REV gradient (brick rows are 16-byte
+            // aligned: arena and cone offsets are multiples of 64 floats).
+            const int nq1 = n1 >> 2;
+            const float invq = 1.f / (float)nq1, inv0 = 1.f / (float)n0;
+            for (int k = t; k < nquad; k += blockDim.x) {
+                const float4 v = acc4[k];
+                if (v.x != 0.f || v.y != 0.f || v.z != 0.f || v.w != 0.f) {
+                    const int q1 = __float2int_rd(((float)k + 0.5f) * invq);
+                    const int kq = k - q1 * nq1;
                     const int k2 = __float2int_rd(((float)q1 + 0.5f) * inv0);
                     const int k0 = q1 - k2 * n0;
-                    atomicAdd(rb + bk_x(l1 + k1) + bk_y(Bv, l2 + k2) + bk_z(Bv, l0 + k0), v);
+                    atomicAdd(reinterpret_cast<float4*>(rb + bk_x(l1 + 4 * kq) + bk_y(Bv, l2 + k2) + bk_z(Bv, l0 + k0)),
+                              v);
                 }
             }
         } else if (nbox > GT_SMEM && gd != 0.f) {
