@@ -984,18 +984,25 @@ __global__ void __launch_bounds__(ROW_WARPS * 32) k_gather(EeParams P, const EeB
 // 8x8x4 tile of patient voxels.  For each cone the tile's trilinear
 // footprint in the REV grid (an AABB computed from the tile's corners under
 // the affine patient -> REV map) is accumulated in shared memory first, then
-// flushed with one global reduction per non-zero REV sample: about 4x fewer
-// L2 atomics than scattering each voxel's 8 weights directly.
+// flushed with one global reduction per non-zero quad of REV samples.  The
+// footprints of all cones are computed up front; consecutive cones alternate
+// between two shared buffers, so a cone's zeroing need not wait for the
+// previous cone's flush.
 constexpr int GT_TX = 8, GT_TY = 8, GT_TZ = 4;
-constexpr int GT_SMEM = 22 * 22 * 22;  // max footprint AABB (extent <= 8+8+4+2 per axis)
+// floats per footprint buffer: an 8x8x4 tile spans at most |(7,7,3)| + 2 = 13
+// REV cells per axis when the REV spacing equals the voxel size (16 in tY
+// after the quad alignment), 2704 < 4096; larger footprints (finer REV
+// spacing) take the direct-scatter path
+constexpr int GT_BUF = 4096;
+constexpr int GT_SMEM = 2 * GT_BUF;
 
 __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, const EeBeamSpec* __restrict__ specs,
                                                                    const EeBeamGeom* __restrict__ geoms,
                                                                    const float* __restrict__ dose_grad,
                                                                    float* __restrict__ rev_grad) {
-    extern __shared__ float acc[];
-    __shared__ int s_box[9];
-    __shared__ float4 s_A[3];
+    extern __shared__ float acc_all[];
+    __shared__ int s_box[EE_MAX_RAYS][9];
+    __shared__ float4 s_A[EE_MAX_RAYS][3];
     const int b = blockIdx.z;
     const EeBeamGeom& G = geoms[b];
     if (G.status != 0 || (int)blockIdx.x >= G.tiles) return;
@@ -1018,58 +1025,66 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
     if (!__syncthreads_or(gd != 0.f)) return;
     // tile origin relative to the crop box, in patient index units
     const float o0 = (float)ox - G.lim_off[0], o1 = (float)oy - G.lim_off[1], o2 = (float)oz - G.lim_off[2];
+    // REV footprint of the tile for every cone: q(v) = A (v - lim_off) - q0,
+    // one (cone, REV axis) per thread; bounds widened by 1e-3 so that the
+    // per-voxel q (formed in another order) never falls outside
+    for (int k = t; k < 3 * P.nrays; k += blockDim.x) {
+        const int r = k / 3, a = k - 3 * r;
+        const EeRayGeom& R = G.ray[r];
+        const float ext[3] = {(float)(GT_TX - 1), (float)(GT_TY - 1), (float)(GT_TZ - 1)};
+        const float* Ar = R.A + 3 * a;
+        float lo = Ar[0] * o0 + Ar[1] * o1 + Ar[2] * o2 - R.q0[a], hi = lo;
+#pragma unroll
+        for (int e = 0; e < 3; e++) {
+            const float d = Ar[e] * ext[e];
+            lo += fminf(d, 0.f);
+            hi += fmaxf(d, 0.f);
+        }
+        // REV axes: q.y -> rev[0] (along the line), q.z -> rev[1], q.x -> rev[2]
+        const int dim = a == 1 ? R.rev[0] : (a == 2 ? R.rev[1] : R.rev[2]);
+        const int slot = a == 1 ? 0 : (a == 2 ? 2 : 4);
+        int l = max(0, (int)floorf(lo - 1e-3f));
+        const int h = min(dim - 1, (int)floorf(hi + 1e-3f) + 1);
+        int w = h - l + 1;
+        if (a == 2 && w > 0) {
+            // tY range on whole quads: a box row of 4 tY cells is one
+            // 16-byte brick row of the REV gradient (flushed as one vector
+            // reduction); the cells past rev[1] are brick padding
+            w = ((h | 3) + 1) - (l & ~3);
+            l &= ~3;
+        }
+        s_box[r][slot] = l;
+        s_box[r][slot + 1] = w;
+        // this cone's map for the voxels: the row [A | -q0] of REV axis a
+        // (the forward gather forms q in the same order)
+        s_A[r][a] = make_float4(Ar[0], Ar[1], Ar[2], -R.q0[a]);
+        s_box[r][6 + a] = R.rev[a];
+    }
+    __syncthreads();
     float* base = rev_grad + G.arena_off;
+    int parity = 0;  // buffer of the next shared-memory cone
     for (int r = 0; r < P.nrays; r++) {
         const EeRayGeom& R = G.ray[r];
-        // REV footprint of the tile: q(v) = A (v - lim_off) - q0, one REV
-        // axis per thread; bounds widened by 1e-3 so that the per-voxel q
-        // (formed in another order) never falls outside
-        if (t < 3) {
-            const int a = t;
-            const float ext[3] = {(float)(GT_TX - 1), (float)(GT_TY - 1), (float)(GT_TZ - 1)};
-            const float* Ar = R.A + 3 * a;
-            float lo = Ar[0] * o0 + Ar[1] * o1 + Ar[2] * o2 - R.q0[a], hi = lo;
-#pragma unroll
-            for (int k = 0; k < 3; k++) {
-                const float d = Ar[k] * ext[k];
-                lo += fminf(d, 0.f);
-                hi += fmaxf(d, 0.f);
-            }
-            // REV axes: q.y -> rev[0] (along the line), q.z -> rev[1], q.x -> rev[2]
-            const int dim = a == 1 ? R.rev[0] : (a == 2 ? R.rev[1] : R.rev[2]);
-            const int slot = a == 1 ? 0 : (a == 2 ? 2 : 4);
-            int l = max(0, (int)floorf(lo - 1e-3f));
-            const int h = min(dim - 1, (int)floorf(hi + 1e-3f) + 1);
-            int w = h - l + 1;
-            if (a == 2 && w > 0) {
-                // tY range on whole quads: a box row of 4 tY cells is one
-                // 16-byte brick row of the REV gradient (flushed as one vector
-                // reduction); the cells past rev[1] are brick padding
-                w = ((h | 3) + 1) - (l & ~3);
-                l &= ~3;
-            }
-            s_box[slot] = l;
-            s_box[slot + 1] = w;
-            // this cone's map for the voxels: the row [A | -q0] of REV axis a
-            // (the forward gather forms q in the same order)
-            s_A[a] = make_float4(Ar[0], Ar[1], Ar[2], -R.q0[a]);
-            s_box[6 + a] = R.rev[a];
-        }
-        __syncthreads();
-        const int l0 = s_box[0], n0 = s_box[1], l1 = s_box[2], n1 = s_box[3], l2 = s_box[4], n2 = s_box[5];
+        const int l0 = s_box[r][0], n0 = s_box[r][1], l1 = s_box[r][2], n1 = s_box[r][3], l2 = s_box[r][4],
+                  n2 = s_box[r][5];
         const bool empty = n0 <= 0 || n1 <= 0 || n2 <= 0;
         const int nbox = empty ? 0 : n0 * n1 * n2;
-        if (nbox > 0 && nbox <= GT_SMEM) {
+        if (nbox > 0 && nbox <= GT_BUF) {
+            // buffers alternate over the shared-memory cones: the last reader
+            // of this buffer (the flush two such cones back) finished before
+            // the barrier after the previous cone's zeroing
+            float* acc = acc_all + parity * GT_BUF;
+            parity ^= 1;
             float4* acc4 = reinterpret_cast<float4*>(acc);  // n1 (tY) is a multiple of 4
             const int nquad = nbox >> 2;
             for (int k = t; k < nquad; k += blockDim.x) acc4[k] = make_float4(0.f, 0.f, 0.f, 0.f);
             __syncthreads();
             if (gd != 0.f) {
-                const float4 a0 = s_A[0], a1 = s_A[1], a2 = s_A[2];
+                const float4 a0 = s_A[r][0], a1 = s_A[r][1], a2 = s_A[r][2];
                 const f3 q = mk(fmaf(a0.x, dx, fmaf(a0.y, dy, fmaf(a0.z, dz, a0.w))),
                                 fmaf(a1.x, dx, fmaf(a1.y, dy, fmaf(a1.z, dz, a1.w))),
                                 fmaf(a2.x, dx, fmaf(a2.y, dy, fmaf(a2.z, dz, a2.w))));
-                const int rv0 = s_box[6], rv1 = s_box[7], rv2 = s_box[8];
+                const int rv0 = s_box[r][6], rv1 = s_box[r][7], rv2 = s_box[r][8];
                 if (!(q.y >= (float)rv0 || q.z >= (float)rv1 || q.x >= (float)rv2 || q.x < 0.f || q.y < 0.f ||
                       q.z < 0.f)) {
                     float f0 = floorf(q.y), f1 = floorf(q.z), f2 = floorf(q.x);
@@ -1117,10 +1132,10 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
                               v);
                 }
             }
-        } else if (nbox > GT_SMEM && gd != 0.f) {
-            // footprint too large for shared memory (not expected for 8x8x4
-            // tiles): scatter directly
-            const float4 a0 = s_A[0], a1 = s_A[1], a2 = s_A[2];
+        } else if (nbox > GT_BUF && gd != 0.f) {
+            // footprint too large for a shared buffer (a REV spacing finer
+            // than the voxels): scatter directly
+            const float4 a0 = s_A[r][0], a1 = s_A[r][1], a2 = s_A[r][2];
             const f3 q = mk(fmaf(a0.x, dx, fmaf(a0.y, dy, fmaf(a0.z, dz, a0.w))),
                             fmaf(a1.x, dx, fmaf(a1.y, dy, fmaf(a1.z, dz, a1.w))),
                             fmaf(a2.x, dx, fmaf(a2.y, dy, fmaf(a2.z, dz, a2.w))));
@@ -1128,7 +1143,6 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
                   q.y < 0.f || q.z < 0.f))
                 tri_brick_scatter(base + R.offset, rev_brick(R.rev[0], R.rev[1], R.rev[2]), q.z, q.x, q.y, gd);
         }
-        __syncthreads();
     }
 }
 
