@@ -384,8 +384,8 @@ def run_reference(args, ws, rank):
 # capture of all six chain kernels on eight beams of this workload (dram__bytes
 # of one call's launches / sum of V_beam = 12.37 M); roofline.traffic scales
 # the dominant stage's figure to the profiled step.
-DRAM_BYTES_PER_VBEAM = {"terma": 1.1, "cone": 359.4, "gather": 67.5, "gather_T": 99.0, "cone_T": 243.0,
-                        "terma_T": 3.8, "geometry": 0.0}
+DRAM_BYTES_PER_VBEAM = {"terma": 1.0, "cone": 328.2, "gather": 50.1, "gather_T": 84.8, "cone_T": 232.7,
+                        "terma_T": 3.5, "geometry": 0.0}
 
 
 def algorithmic_bytes(infos):
