@@ -1,10 +1,12 @@
 """In-tree build of the CUDA engine library ``endtoend_gb300/_lib/libee_cccs.so``
-and of the ``dosecalc-beam`` command-line program on top of it.
+and of the ``dosecalc-beam`` / ``dosecalc-beamlet`` command-line programs on
+top of it.
 
 nvcc, one ``-gencode`` for sm_103a, the translation units compiled in
 parallel, then linked as a shared library with the C ABI of include/ee_cccs.h.
 No torch, no cmake: the result loads with ctypes (or any C FFI).  The
-program (csrc/ee_dosecalc_beam.cpp) is host C++ that uses only that ABI.
+programs (csrc/ee_dosecalc_beam.cpp, csrc/ee_dosecalc_beamlet.cpp) are host
+C++ that uses only that ABI.
 """
 import os
 import shutil
@@ -21,6 +23,7 @@ HEADERS = ["ee_internal.h", "ee_device.cuh", os.path.join("..", "..", "include",
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CLI_SRC = os.path.join(CSRC, "ee_dosecalc_beam.cpp")
 CLI = os.path.join(OUT_DIR, "dosecalc-beam")
+CLIS = {"dosecalc-beam": CLI_SRC, "dosecalc-beamlet": os.path.join(CSRC, "ee_dosecalc_beamlet.cpp")}
 
 
 def nvcc_path():
@@ -43,22 +46,25 @@ def _stale():
 
 
 def build_cli(verbose=False, force=False):
-    """The dosecalc-beam program (host C++ over the C ABI; rpath $ORIGIN)."""
+    """The dosecalc-beam and dosecalc-beamlet programs (host C++ over the C
+    ABI; rpath $ORIGIN).  Returns the dosecalc-beam path."""
     build(verbose=verbose, force=force)
-    if not force and os.path.exists(CLI) and os.path.getmtime(CLI) >= max(
-            os.path.getmtime(p) for p in (CLI_SRC, LIB, os.path.join(ROOT, "include", "ee_cccs.h"))):
-        return CLI
     cxx = shutil.which("g++") or shutil.which("c++")
-    if not cxx:
-        raise RuntimeError("a host C++ compiler is required to build dosecalc-beam")
-    tmp = CLI + ".tmp"
-    cmd = [cxx, "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"), CLI_SRC, "-o", tmp, "-L", OUT_DIR,
-           "-lee_cccs", "-Wl,-rpath,$ORIGIN"]
-    if verbose:
-        print(" ".join(cmd), flush=True)
-    if subprocess.call(cmd) != 0:
-        raise RuntimeError("building dosecalc-beam failed")
-    os.replace(tmp, CLI)
+    for name, src in CLIS.items():
+        out = os.path.join(OUT_DIR, name)
+        deps = (src, LIB, os.path.join(ROOT, "include", "ee_cccs.h"), os.path.join(CSRC, "ee_contract.h"))
+        if not force and os.path.exists(out) and os.path.getmtime(out) >= max(os.path.getmtime(p) for p in deps):
+            continue
+        if not cxx:
+            raise RuntimeError("a host C++ compiler is required to build " + name)
+        tmp = out + ".tmp"
+        cmd = [cxx, "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"), src, "-o", tmp, "-L", OUT_DIR,
+               "-lee_cccs", "-Wl,-rpath,$ORIGIN"]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        if subprocess.call(cmd) != 0:
+            raise RuntimeError("building " + name + " failed")
+        os.replace(tmp, out)
     return CLI
 
 

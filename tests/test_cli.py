@@ -81,3 +81,18 @@ def test_errors(cli, tmp_path):
     os.remove(os.path.join(data, "dsa", "synth2"))
     r = run(cli, f"--temp={temp}", f"--data={data}", "--dry-run")
     assert r.returncode != 0 and "point kernel" in r.stderr
+
+
+def test_beamlet_program_dry_run_and_errors(cli, tmp_path):
+    bl = os.path.join(os.path.dirname(cli), "dosecalc-beamlet")
+    r = run(bl, "--help")
+    assert r.returncode == 0 and "--sparsify-threshold" in r.stdout
+    vol, beams = dc.slab_case()
+    beams[0]["fluence"][:2] = 0.0  # 16 beamlets without fluence: no column
+    temp, data = dc.write_contract(str(tmp_path), vol, beams)
+    r = run(bl, f"--temp={temp}", f"--data={data}", "--dry-run", "--thresh=1e-4")
+    assert r.returncode == 0, r.stderr
+    assert "3 beams, 176 beamlets with fluence, threshold 0.0001" in r.stdout
+    assert "kernel_extent 2 cm" in r.stdout
+    r = run(bl, f"--temp={temp}", f"--data={data}", "--dry-run", "--sparsify-threshold=abc")
+    assert r.returncode != 0 and "threshold" in r.stderr

@@ -54,3 +54,46 @@ def test_cli_dose(ss, mode, tmp_path):
         err = float(np.abs(dose - od).max() / od.max())
         print(f"ss_factor {ss}: dosecalc-beam vs FP64 oracle {err:.2e} of Dmax")
         assert err <= (1e-3 if ss == 1 else 5e-3)
+
+
+def test_beamlet_program_columns(tmp_path):
+    """dosecalc-beamlet's raw CSR files equal the library's beamlet columns
+    for the same inputs (kernel extent and REV limits from the header)."""
+    cli = _build.build_cli()
+    bl = os.path.join(os.path.dirname(cli), "dosecalc-beamlet")
+    vol, beams = dc.slab_case()
+    for d in beams:
+        d["fmap"], d["fluence"] = (4, 4), d["fluence"][:4, :4].copy()
+        d["beamlet"] = (1.0, 1.0)
+    beams[1]["fluence"][0, :] = 0.0
+    temp, data = dc.write_contract(str(tmp_path), vol, beams)
+    out = tmp_path / "res" / "Dose_Coefficients.h5"
+    r = subprocess.run([bl, f"--temp={temp}", f"--data={data}", f"--out={out}", "--thresh=1e-4", "--timing"],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    print(r.stdout)
+    odir = tmp_path / "res" / "Dose_Coefficients"
+    specs = dict(l.split(" ", 1) for l in (odir / "calc_specs.txt").read_text().splitlines())
+    assert specs["N_beams"] == "3" and float(specs["sparsity_thresh"]) == np.float32(1e-4)
+    phys = engine.physics_from_kernel_files(os.path.join(data, "spectra", golden_cases.SYNTH_SPECTRUM + ".spec"),
+                                            os.path.join(data, "dsa"), 8, 6, spacing_cm=0.25, penumbra_cm=1.0)
+    n = vol.nvoxels
+    with engine.Engine(0) as e:
+        e.set_volume(vol)
+        e.set_physics(phys, mode="table")
+        e.set_beamlet_options(2.0, (400, 400, 400))
+        for b, d in enumerate(beams):
+            bidx, cp, rows, vals = e.beamlet_columns(dc.as_engine_beam(d), 1e-4)
+            got_idx = np.fromfile(odir / f"beam_{b:05d}_beamlet_index.raw", np.int32)
+            got_cp = np.fromfile(odir / f"beam_{b:05d}_col_ptr.raw", np.int64)
+            got_rows = np.fromfile(odir / f"beam_{b:05d}_lindex.raw", np.uint32)
+            got_vals = np.fromfile(odir / f"beam_{b:05d}_coeffs.raw", np.float32)
+            np.testing.assert_array_equal(got_idx, bidx)
+            assert len(got_idx) == int((d["fluence"] > 0).sum())
+            assert got_cp[0] == 0 and got_cp[-1] == len(got_rows) == len(got_vals)
+            for c in range(len(bidx)):
+                g = np.zeros(n, np.float32)
+                g[got_rows[got_cp[c]:got_cp[c + 1]]] = got_vals[got_cp[c]:got_cp[c + 1]]
+                ref = np.zeros(n, np.float32)
+                ref[rows[cp[c]:cp[c + 1]]] = vals[cp[c]:cp[c + 1]]
+                assert np.abs(g - ref).max() <= 1e-6 * ref.max(), (b, c)
