@@ -13,6 +13,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <mutex>
@@ -372,6 +373,14 @@ struct ChunkDims {
 
 // Device buffer growth: a freed buffer may still be read by queued kernels,
 // so drain the stream first when a buffer has to grow.
+bool ee_debug_poison() {
+    static const bool on = [] {
+        const char* v = std::getenv("EE_DEBUG_POISON");
+        return v && *v && *v != '0';
+    }();
+    return on;
+}
+
 template <class T>
 cudaError_t grow(ee_context* c, DevBuf<T>& b, size_t n) {
     if (n <= b.n && b.p) return cudaSuccess;
@@ -471,7 +480,8 @@ int pipeline(ee_context* c, const PipeArgs& A) {
         c->last_geoms.insert(c->last_geoms.end(), hg, hg + nb);
         if (!fwd) continue;
         EE_CUDA(grow(c, c->rev, D.rev_total));
-        EE_CUDA(cudaMemsetAsync(c->rev.p, 0, sizeof(float) * D.rev_total, s));
+        // no clear: the cone kernels write every sample k_gather reads
+        if (ee_debug_poison()) EE_CUDA(cudaMemsetAsync(c->rev.p, 0xFF, sizeof(float) * D.rev_total, s));
         if (c->P.mode == EE_KERNEL_EXP) EE_CUDA(grow(c, c->samples, D.rev_total));
         EE_CUDA(staged(c, EE_STAGE_CONE, 1, [&] {
             return ee_launch_cone(c->P, dsp, dge, c->terma.p, c->rev.p,
@@ -506,7 +516,8 @@ int pipeline(ee_context* c, const PipeArgs& A) {
         const ChunkDims& D = dims[k];
         EE_CUDA(grow(c, c->rev_grad, D.rev_total + 4));  // +4: vector-reduction padding
         if (c->P.mode == EE_KERNEL_EXP) EE_CUDA(grow(c, c->samples, D.rev_total));  // adjoint cone scratch
-        EE_CUDA(cudaMemsetAsync(c->rev_grad.p, 0, sizeof(float) * D.rev_total, s));
+        if (ee_debug_poison()) EE_CUDA(cudaMemsetAsync(c->rev_grad.p, 0xFF, sizeof(float) * D.rev_total, s));
+        EE_CUDA(ee_launch_rev_zero(c->P, dge, c->rev_grad.p, nb, D.max_lines, s));
         EE_CUDA(staged(c, EE_STAGE_GATHER_T, 1, [&] {
             return ee_launch_gather_T(c->P, dsp, dge, dgrad, c->rev_grad.p, nb, D.max_tiles, s);
         }));
@@ -705,7 +716,7 @@ cudaError_t plan_enqueue(ee_plan* pl, cudaStream_t s) {
         PL(ee_launch_terma(P, dsp, dge, pl->d_fluence, pl->terma.p, pl->adjoint ? pl->unit.p : nullptr,
                            pl->adjoint ? pl->bl_idx.p : nullptr, nb, D.max_tvol, s));
         PL(ee_launch_geometry(P, dsp, dge, nb, s));
-        PL(cudaMemsetAsync(pl->rev.p, 0, sizeof(float) * D.rev_total, s));
+        if (ee_debug_poison()) PL(cudaMemsetAsync(pl->rev.p, 0xFF, sizeof(float) * D.rev_total, s));
         PL(ee_launch_cone(P, dsp, dge, pl->terma.p, pl->rev.p, P.mode == EE_KERNEL_EXP ? pl->samples.p : nullptr, nb,
                           D.max_lines, D.max_line, s, pl->lane_block));
         PL(ee_launch_gather(P, dsp, dge, pl->rev.p, pl->d_dose, nb, 1, D.max_rows, s));
@@ -718,7 +729,8 @@ cudaError_t plan_enqueue(ee_plan* pl, cudaStream_t s) {
         const EeBeamSpec* dsp = pl->d_specs.p + b0;
         const EeBeamGeom* dge = pl->d_geoms.p + b0;
         const ChunkDims& D = pl->dims[k];
-        PL(cudaMemsetAsync(pl->rev_grad.p, 0, sizeof(float) * D.rev_total, s));
+        if (ee_debug_poison()) PL(cudaMemsetAsync(pl->rev_grad.p, 0xFF, sizeof(float) * D.rev_total, s));
+        PL(ee_launch_rev_zero(P, dge, pl->rev_grad.p, nb, D.max_lines, s));
         PL(ee_launch_gather_T(P, dsp, dge, pl->d_grad, pl->rev_grad.p, nb, D.max_tiles, s));
         PL(ee_launch_cone_T(P, dsp, dge, pl->rev_grad.p, P.mode == EE_KERNEL_EXP ? pl->samples.p : nullptr,
                             pl->terma_grad.p, nb, D.max_lines, D.max_line, s, pl->lane_block));

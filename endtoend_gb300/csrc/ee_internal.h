@@ -154,6 +154,13 @@ cudaError_t ee_launch_gather_T(const EeParams& P, const EeBeamSpec* specs, const
 cudaError_t ee_launch_cone_T(const EeParams& P, const EeBeamSpec* specs, const EeBeamGeom* geoms, const float* rev_grad,
                              float2* scratch, float* terma_grad, int nbeams, int max_lines, int max_line,
                              cudaStream_t s, int lane_block = 128);
+// zeros on every line's read span of a chunk's REV gradient arena (before
+// ee_launch_gather_T; the forward cone kernels zero their own arena)
+cudaError_t ee_launch_rev_zero(const EeParams& P, const EeBeamGeom* geoms, float* rev_grad, int nbeams, int max_lines,
+                               cudaStream_t s);
+// test option: EE_DEBUG_POISON=1 fills scratch with NaN where the engine
+// relies on its kernels, not on a clear, to write every sample it reads
+bool ee_debug_poison();
 // per-beam status words of a geometry array (strided copy), for plans
 cudaError_t ee_copy_status(const EeBeamGeom* geoms, int* status_host, int nbeams, cudaStream_t s);
 cudaError_t ee_launch_terma_T(const EeParams& P, const EeBeamSpec* specs, const EeBeamGeom* geoms,

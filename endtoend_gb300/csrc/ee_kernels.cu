@@ -291,6 +291,47 @@ __device__ __forceinline__ void line_segment(const EeParams& P, const EeBeamGeom
     n = max(0, i1 - i0 + 1);
 }
 
+// Samples of a REV line that k_gather can read (and k_gather_T can add to):
+// k_gather visits voxels within 2 BEV voxels of the crop box and reads the
+// REV cells within one REV step (per axis) of each voxel's REV point, i.e.
+// within sum_k |B[a][k]| BEV units per axis a.  So the line's intersection
+// with the crop box dilated by 2 + sum_k |B[a][k]| (+0.05, +1 sample each
+// side) holds every sample either kernel touches; samples outside it are
+// never read and need no zero.  z1 < z0: none.
+__device__ __forceinline__ void line_read_span(const EeBeamGeom& G, const EeRayGeom& R, int tY, int tZ, int L,
+                                               int& z0, int& z1) {
+    const f3 bl = ld3(R.B0) + ld3(R.By) * (float)tY + ld3(R.Bz) * (float)tZ;
+    const float c[3] = {bl.x, bl.y, bl.z};
+    float a = 0.f, b = (float)(L - 1);
+    z0 = 0;
+    z1 = -1;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const float D = 2.05f + fabsf(R.Bx[k]) + fabsf(R.By[k]) + fabsf(R.Bz[k]);
+        const float lo = -D, hi = (float)G.bev[k] + D, m = R.Bx[k];
+        if (fabsf(m) < 1e-6f) {
+            if (c[k] < lo || c[k] > hi) return;
+        } else {
+            const float t0 = (lo - c[k]) / m, t1 = (hi - c[k]) / m;
+            a = fmaxf(a, fminf(t0, t1));
+            b = fminf(b, fmaxf(t0, t1));
+        }
+    }
+    if (!(a <= b + 2.f)) return;
+    z0 = max(0, (int)floorf(a) - 1);
+    z1 = min(L - 1, (int)ceilf(b) + 1);
+}
+
+// Zero the samples of a line's read span outside [i0, i0 + n) (the cone
+// writes those): the REV dose arena needs no separate clear.
+__device__ __forceinline__ void zero_outside_segment(float* out, const Brick& Bv, int z0, int z1, int i0, int n,
+                                                     int first, int stride) {
+    const int e0 = n > 0 ? min(z1 + 1, i0) : z1 + 1;  // [z0, e0) before the segment
+    const int s1 = n > 0 ? max(z0, i0 + n) : z1 + 1;  // [s1, z1] after it
+    for (int i = z0 + first; i < e0; i += stride) out[bk_z(Bv, i)] = 0.f;
+    for (int i = s1 + first; i <= z1; i += stride) out[bk_z(Bv, i)] = 0.f;
+}
+
 // REV resample of samples i0..i0+n-1 of one line into shared memory
 // (device.cu:47-79): density sentinel -3 outside the BEV crop box, -2 outside
 // the calc bbox; TERMA is zero at sentinel samples (never written by the
@@ -522,8 +563,10 @@ __global__ void __launch_bounds__(CONE_WARPS * 32) k_cone(EeParams P, const EeBe
     // bricked REV arena (rev_brick)
     const Brick Bv = rev_brick(R.rev[0], R.rev[1], R.rev[2]);
     float* out = rev + G.arena_off + R.offset + bk_x(tY) + bk_y(Bv, tZ);
-    int i0, n;
+    int i0, n, z0, z1;
     line_segment(P, G, R, tY, tZ, L, i0, n);
+    line_read_span(G, R, tY, tZ, L, z0, z1);
+    zero_outside_segment(out, Bv, z0, z1, i0, n, lane, 32);
     if (n > 0) {
         gather_line(P, specs[b], G, R, terma + specs[b].t_off, tY, tZ, i0, n, lane, rho, T);
         __syncwarp();
@@ -616,15 +659,17 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_lane(EeParams P, const EeBe
     if (!lane_line(R, blockIdx.x * LANE_BLOCK + threadIdx.x, tY, tZ)) return;
     const int L = R.rev[0];
     const int line = tZ * R.rev[1] + tY;
-    int i0, n;
+    // bricked REV arena: this line's sample i sits at out + bk_z(i)
+    const Brick Bv = rev_brick(R.rev[0], R.rev[1], R.rev[2]);
+    float* out = rev + G.arena_off + R.offset + bk_x(tY) + bk_y(Bv, tZ);
+    int i0, n, z0, z1;
     line_segment(P, G, R, tY, tZ, L, i0, n);
+    line_read_span(G, R, tY, tZ, L, z0, z1);
+    zero_outside_segment(out, Bv, z0, z1, i0, n, 0, 1);
     if (n <= 0) return;
     const EeBeamSpec& S = specs[b];
     const float* tb = terma + S.t_off;
     const LineFrame F = line_frame(R, tY, tZ);
-    // bricked REV arena: this line's sample i sits at out + bk_z(i)
-    const Brick Bv = rev_brick(R.rev[0], R.rev[1], R.rev[2]);
-    float* out = rev + G.arena_off + R.offset + bk_x(tY) + bk_y(Bv, tZ);
     // (rho, T) of each sample, kept from the forward pass for the reverse
     // one, line-major ([i][line]) in this cone's slot of the scratch
     const long long nl = R.nlines;
@@ -697,6 +742,25 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_lane(EeParams P, const EeBe
             }
         }
     }
+}
+
+// Zero the read spans (line_read_span) of every line of a chunk's REV
+// gradient arena before k_gather_T adds into it: the samples the adjoint
+// gather and cone can touch, instead of a clear of the whole arena.
+template <int LANE_BLOCK>
+__global__ void __launch_bounds__(LANE_BLOCK) k_rev_zero(const EeBeamGeom* __restrict__ geoms,
+                                                         float* __restrict__ rev_grad) {
+    const int ray = blockIdx.y, b = blockIdx.z;
+    const EeBeamGeom& G = geoms[b];
+    if (G.status != 0) return;
+    const EeRayGeom& R = G.ray[ray];
+    int tY, tZ;
+    if (!lane_line(R, blockIdx.x * LANE_BLOCK + threadIdx.x, tY, tZ)) return;
+    const Brick Bv = rev_brick(R.rev[0], R.rev[1], R.rev[2]);
+    float* out = rev_grad + G.arena_off + R.offset + bk_x(tY) + bk_y(Bv, tZ);
+    int z0, z1;
+    line_read_span(G, R, tY, tZ, R.rev[0], z0, z1);
+    for (int i = z0; i <= z1; i++) out[bk_z(Bv, i)] = 0.f;
 }
 
 // Adjoint of k_cone_lane followed by the transpose of the REV TERMA resample.
@@ -1237,6 +1301,12 @@ cudaError_t ee_launch_cone(const EeParams& P, const EeBeamSpec* specs, const EeB
     if (e != cudaSuccess) return e;
     dim3 grid(grid1(max_lines, CONE_WARPS), P.nrays, nbeams);
     k_cone<<<grid, CONE_WARPS * 32, smem, s>>>(P, specs, geoms, terma, rev, max_line);
+    return cudaGetLastError();
+}
+
+cudaError_t ee_launch_rev_zero(const EeParams& P, const EeBeamGeom* geoms, float* rev_grad, int nbeams, int max_lines,
+                               cudaStream_t s) {
+    k_rev_zero<128><<<dim3(grid1(max_lines, 128), P.nrays, nbeams), 128, 0, s>>>(geoms, rev_grad);
     return cudaGetLastError();
 }
 
