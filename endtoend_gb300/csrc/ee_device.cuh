@@ -82,17 +82,25 @@ __device__ __forceinline__ float tri_border(const float* __restrict__ v, int nx,
     return acc;
 }
 
+// Vector reduction of four floats into a 16-byte aligned quad of global
+// memory (red.global.add.v4.f32, sm_90+): no value comes back, unlike an
+// atomicAdd whose result the caller ignores.
+__device__ __forceinline__ void red_v4(float* q, float a, float b, float c, float d) {
+    asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(q), "f"(a), "f"(b), "f"(c), "f"(d)
+                 : "memory");
+}
+
 // Add (a, b) to p[0], p[1] with vector reductions: both land in one 16-byte
 // aligned quad unless p sits in its last slot.  The other slots of the quad
 // receive +0, so the buffer must hold 3 floats of padding past its last
 // element and its base must be 16-byte aligned (cudaMalloc'd).
 __device__ __forceinline__ void red_pair(float* p, float a, float b) {
     const uintptr_t u = (uintptr_t)p;
-    float4* q = (float4*)(u & ~(uintptr_t)15);
+    float* q = (float*)(u & ~(uintptr_t)15);
     const int o = (int)((u >> 2) & 3);
-    if (o == 0) atomicAdd(q, make_float4(a, b, 0.f, 0.f));
-    else if (o == 1) atomicAdd(q, make_float4(0.f, a, b, 0.f));
-    else if (o == 2) atomicAdd(q, make_float4(0.f, 0.f, a, b));
+    if (o == 0) red_v4(q, a, b, 0.f, 0.f);
+    else if (o == 1) red_v4(q, 0.f, a, b, 0.f);
+    else if (o == 2) red_v4(q, 0.f, 0.f, a, b);
     else {
         atomicAdd(p, a);
         atomicAdd(p + 1, b);

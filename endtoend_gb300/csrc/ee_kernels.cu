@@ -1192,8 +1192,7 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
                     const int kq = k - q1 * nq1;
                     const int k2 = __float2int_rd(((float)q1 + 0.5f) * inv0);
                     const int k0 = q1 - k2 * n0;
-                    atomicAdd(reinterpret_cast<float4*>(rb + bk_x(l1 + 4 * kq) + bk_y(Bv, l2 + k2) + bk_z(Bv, l0 + k0)),
-                              v);
+                    red_v4(rb + bk_x(l1 + 4 * kq) + bk_y(Bv, l2 + k2) + bk_z(Bv, l0 + k0), v.x, v.y, v.z, v.w);
                 }
             }
         } else if (nbox > GT_BUF && gd != 0.f) {
