@@ -1209,31 +1209,62 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
     }
 }
 
-// TERMA adjoint: fluence_grad[beamlet(v)] += G_v * terma_grad[v], warp-
-// aggregated per beamlet index before the atomic.
+// TERMA adjoint: fluence_grad[beamlet(v)] += G_v * terma_grad[v].  A block
+// takes TT_VPT * 256 consecutive bricked voxels (a run of bricks along x) and
+// sums them per beamlet in a shared histogram of the beam's fluence map, then
+// adds the non-zero bins to the fluence gradient: one global atomic per
+// beamlet the run touches.  Maps above TT_HIST beamlets aggregate per warp
+// (lanes of equal beamlet index summed before one atomic) instead.
+constexpr int TT_HIST = 4096, TT_VPT = 4;
+
 __global__ void __launch_bounds__(256) k_terma_T(EeParams P, const EeBeamSpec* __restrict__ specs,
                                                  const float* __restrict__ unit, const int* __restrict__ bl_idx,
                                                  const float* __restrict__ terma_grad, float* __restrict__ fluence_grad) {
+    __shared__ float hist[TT_HIST];
     const int b = blockIdx.z;
     const EeBeamSpec& S = specs[b];
     const long long tvol = ee_brick_vol(S.tn);  // padding: bl_idx -1
-    long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    int bl = -1;
-    float val = 0.f;
-    if (v < tvol) {
-        long long o = S.t_off + v;
-        bl = bl_idx[o];
-        if (bl >= 0) val = unit[o] * terma_grad[o];
+    const long long v0 = (long long)blockIdx.x * (256 * TT_VPT);
+    if (v0 >= tvol) return;
+    const int t = threadIdx.x, nfl = S.fmap[0] * S.fmap[1];
+    float* fg = fluence_grad + S.fl_off;
+    if (nfl > TT_HIST) {
+        for (int j = 0; j < TT_VPT; j++) {
+            const long long v = v0 + j * 256 + t;
+            int bl = -1;
+            float val = 0.f;
+            if (v < tvol) {
+                const long long o = S.t_off + v;
+                bl = bl_idx[o];
+                if (bl >= 0) val = unit[o] * terma_grad[o];
+            }
+            const unsigned peers = __match_any_sync(FULL, bl);
+            const int leader = __ffs(peers) - 1;
+            float sum = 0.f;
+            for (unsigned m = peers; m; m &= m - 1) sum += __shfl_sync(peers, val, __ffs(m) - 1);
+            if ((t & 31) == leader && bl >= 0 && sum != 0.f) atomicAdd(fg + bl, sum);
+        }
+        return;
     }
-    unsigned peers = __match_any_sync(FULL, bl);
-    int leader = __ffs(peers) - 1;
-    // sum val over lanes sharing bl (segmented by match mask)
-    float sum = 0.f;
-    for (unsigned m = peers; m; m &= m - 1) {
-        int src = __ffs(m) - 1;
-        sum += __shfl_sync(peers, val, src);
+    for (int k = t; k < nfl; k += 256) hist[k] = 0.f;
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < TT_VPT; j++) {
+        const long long v = v0 + j * 256 + t;
+        if (v < tvol) {
+            const long long o = S.t_off + v;
+            const int bl = bl_idx[o];
+            if (bl >= 0) {
+                const float val = unit[o] * terma_grad[o];
+                if (val != 0.f) atomicAdd(hist + bl, val);
+            }
+        }
     }
-    if ((int)(threadIdx.x & 31) == leader && bl >= 0 && sum != 0.f) atomicAdd(fluence_grad + specs[b].fl_off + bl, sum);
+    __syncthreads();
+    for (int k = t; k < nfl; k += 256) {
+        const float h = hist[k];
+        if (h != 0.f) atomicAdd(fg + k, h);
+    }
 }
 
 }  // namespace
@@ -1356,7 +1387,7 @@ cudaError_t ee_launch_terma_T(const EeParams& P, const EeBeamSpec* specs, const 
                               const float* unit_terma, const int* beamlet_idx, const float* terma_grad,
                               float* fluence_grad, int nbeams, long long max_tvol, cudaStream_t s) {
     (void)geoms;
-    dim3 grid(grid1(max_tvol, 256), 1, nbeams);
+    dim3 grid(grid1(max_tvol, 256 * TT_VPT), 1, nbeams);
     k_terma_T<<<grid, 256, 0, s>>>(P, specs, unit_terma, beamlet_idx, terma_grad, fluence_grad);
     return cudaGetLastError();
 }
