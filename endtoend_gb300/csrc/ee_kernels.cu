@@ -1065,7 +1065,7 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
                                                                    const float* __restrict__ dose_grad,
                                                                    float* __restrict__ rev_grad) {
     extern __shared__ float acc_all[];
-    __shared__ int s_box[EE_MAX_RAYS][9];
+    __shared__ int s_box[EE_MAX_RAYS][10];
     __shared__ float4 s_A[EE_MAX_RAYS][3];
     const int b = blockIdx.z;
     const EeBeamGeom& G = geoms[b];
@@ -1116,6 +1116,10 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
             // reduction); the cells past rev[1] are brick padding
             w = ((h | 3) + 1) - (l & ~3);
             l &= ~3;
+            // row stride 4 (mod 8) floats: the rows of x-adjacent voxels
+            // spread over the shared banks; the extra quad of a row is never
+            // scattered to (k1 < w), stays zero and is not flushed
+            s_box[r][9] = (w & 7) == 0 ? w + 4 : w;
         }
         s_box[r][slot] = l;
         s_box[r][slot + 1] = w;
@@ -1132,7 +1136,12 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
         const int l0 = s_box[r][0], n0 = s_box[r][1], l1 = s_box[r][2], n1 = s_box[r][3], l2 = s_box[r][4],
                   n2 = s_box[r][5];
         const bool empty = n0 <= 0 || n1 <= 0 || n2 <= 0;
-        const int nbox = empty ? 0 : n0 * n1 * n2;
+        const int s1 = empty ? 0 : s_box[r][9];  // row stride of the box (>= n1, a multiple of 4)
+        // rows per slab: odd, so that the slab stride s1 * n0p is 4 x odd
+        // (mod 32) and the slabs of y-adjacent voxels spread over the banks
+        // too; the padding rows (k0 >= n0) are never scattered to
+        const int n0p = n0 | 1;
+        const int nbox = empty ? 0 : n0p * s1 * n2;
         if (nbox > 0 && nbox <= GT_BUF) {
             // buffers alternate over the shared-memory cones: the last reader
             // of this buffer (the flush two such cones back) finished before
@@ -1168,7 +1177,7 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
                             for (int d0 = 0; d0 < 2; d0++) {
                                 int k0 = i0 + d0 - l0;
                                 if (i0 + d0 >= rv0 || k0 < 0 || k0 >= n0) continue;
-                                atomicAdd(acc + k1 + n1 * (k0 + n0 * k2), (d0 ? a0 : 1.f - a0) * w1);
+                                atomicAdd(acc + k1 + s1 * (k0 + n0p * k2), (d0 ? a0 : 1.f - a0) * w1);
                             }
                         }
                     }
@@ -1178,20 +1187,20 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
             float* rb = base + R.offset;
             const Brick Bv = rev_brick(R.rev[0], R.rev[1], R.rev[2]);
             // one box quad (4 tY cells) per iteration, quad index = kq + nq1 *
-            // (k0 + n0 * k2); (k + 0.5) / n is at least 1/(2n) away from an
+            // (k0 + n0p * k2); (k + 0.5) / n is at least 1/(2n) away from an
             // integer, far above the FP32 error for these sizes, so the float
             // quotients are exact.  A non-zero quad is one 16-byte vector
             // reduction into the bricked REV gradient (brick rows are 16-byte
             // aligned: arena and cone offsets are multiples of 64 floats).
-            const int nq1 = n1 >> 2;
-            const float invq = 1.f / (float)nq1, inv0 = 1.f / (float)n0;
+            const int nq1 = s1 >> 2;
+            const float invq = 1.f / (float)nq1, inv0 = 1.f / (float)n0p;
             for (int k = t; k < nquad; k += blockDim.x) {
                 const float4 v = acc4[k];
                 if (v.x != 0.f || v.y != 0.f || v.z != 0.f || v.w != 0.f) {
                     const int q1 = __float2int_rd(((float)k + 0.5f) * invq);
                     const int kq = k - q1 * nq1;
                     const int k2 = __float2int_rd(((float)q1 + 0.5f) * inv0);
-                    const int k0 = q1 - k2 * n0;
+                    const int k0 = q1 - k2 * n0p;
                     red_v4(rb + bk_x(l1 + 4 * kq) + bk_y(Bv, l2 + k2) + bk_z(Bv, l0 + k0), v.x, v.y, v.z, v.w);
                 }
             }
