@@ -634,6 +634,50 @@ __device__ __forceinline__ float sample_rho(const EeParams& P, const EeBeamSpec&
 
 constexpr int CONE_U = 4;
 
+// Sample indices [s0, s1] of a REV line whose TERMA trilinear corners can lie
+// inside the beam's field frustum.  A voxel has a beamlet only where its
+// iso-plane projection falls inside the fluence-map rectangle (beamlet_of,
+// cudaSiddon.cu:143-165): with diff = p - src, proj = dir.diff and
+// u = MB_row.(diff - proj dir), the fluence coordinate is inside iff
+// u + k proj >= 0 and k proj - u > 0, k = half the map's width / isodist,
+// per BEV axis x and z.  Outside, TERMA is exactly zero (k_terma writes 0
+// where there is no beamlet) and the TERMA adjoint drops the voxel, so the
+// cone kernels skip the TERMA reads and the TERMA-gradient scatter of the
+// samples outside [s0, s1].  The four sides are linear in the sample index;
+// a sample is outside when one side's form is below minus its change over
+// two voxels per axis (the trilinear corners, and supersampled centres half
+// a voxel beyond them).
+__device__ __forceinline__ void field_span(const EeParams& P, const EeBeamSpec& S, const LineFrame& F, int& s0,
+                                           int& s1) {
+    const f3 vox = mk(P.voxel[0], P.voxel[1], P.voxel[2]);
+    const f3 d0 = mk(P.start[0] + vox.x * F.gl.x - S.src[0], P.start[1] + vox.y * F.gl.y - S.src[1],
+                     P.start[2] + vox.z * F.gl.z - S.src[2]);  // diff at sample 0
+    const f3 d1 = mk(vox.x * F.gx.x, vox.y * F.gx.y, vox.z * F.gx.z);  // diff step per sample
+    const f3 dir = ld3(S.dir);
+    float lo = -1e9f, hi = 1e9f;
+#pragma unroll
+    for (int a = 0; a < 2; a++) {
+        const f3 m = ld3(S.MB + (a ? 6 : 0));
+        const f3 g = m - dir * dot(m, dir);  // u = g . diff
+        const float k = 0.5f * (float)S.fmap[a] * S.beamlet[a] / S.isodist;
+#pragma unroll
+        for (int sg = -1; sg <= 1; sg += 2) {
+            const f3 gl = g * (float)sg + dir * k;  // the side's form: gl . diff >= 0 inside
+            const float M = 2.f * (fabsf(gl.x) * vox.x + fabsf(gl.y) * vox.y + fabsf(gl.z) * vox.z) + 1e-3f;
+            const float al = dot(gl, d1), be = dot(gl, d0) + M;  // maybe inside where al i + be >= 0
+            if (fabsf(al) < 1e-20f) {
+                if (be < 0.f) { lo = 1e9f; hi = -1e9f; }
+            } else {
+                const float t = fminf(fmaxf(-be / al, -1e9f), 1e9f);
+                if (al > 0.f) lo = fmaxf(lo, t);
+                else hi = fminf(hi, t);
+            }
+        }
+    }
+    s0 = (int)floorf(lo) - 1;
+    s1 = (int)ceilf(hi) + 1;
+}
+
 // Lane slot -> REV line for the one-lane-per-line kernels: the lanes of a
 // warp own an 8 (tY) x 4 (tZ) tile of lines, so at every sample index the
 // warp's reads and writes of the bricked REV arrays fall in two 64-byte brick
@@ -670,6 +714,8 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_lane(EeParams P, const EeBe
     const EeBeamSpec& S = specs[b];
     const float* tb = terma + S.t_off;
     const LineFrame F = line_frame(R, tY, tZ);
+    int f0, f1;  // samples that can see TERMA
+    field_span(P, S, F, f0, f1);
     // (rho, T) of each sample, kept from the forward pass for the reverse
     // one, line-major ([i][line]) in this cone's slot of the scratch
     const long long nl = R.nlines;
@@ -690,7 +736,8 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_lane(EeParams P, const EeBe
             for (int j = 0; j < CONE_U; j++) {
                 rr[j] = -1.f;
                 tt[j] = 0.f;
-                if (ib + j < iend) rr[j] = sample_rho(P, S, G, F, ib + j, tb, tt[j]);
+                if (ib + j < iend)
+                    rr[j] = sample_rho(P, S, G, F, ib + j, (ib + j >= f0 && ib + j <= f1) ? tb : nullptr, tt[j]);
             }
 #pragma unroll
             for (int j = 0; j < CONE_U; j++) {
@@ -786,6 +833,8 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_T_lane(EeParams P, const Ee
     if (n <= 0) return;
     const EeBeamSpec& S = specs[b];
     const LineFrame F = line_frame(R, tY, tZ);
+    int f0, f1;  // samples whose TERMA corners can lie in the field (field_span)
+    field_span(P, S, F, f0, f1);
     const long long nl = R.nlines;  // line-major scratch [i][line]
     const long long row = G.arena_off + R.offset + line;
     const Brick Bv = rev_brick(R.rev[0], R.rev[1], R.rev[2]);  // bricked REV gradient
@@ -860,7 +909,7 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_T_lane(EeParams P, const Ee
                 if (i > i1) break;
                 const float gi = v ? gl[j] * inv_nphi : 0.f;
                 const float tot = a.x + cprev;
-                if (v && tot != 0.f) {
+                if (v && tot != 0.f && i >= f0 && i <= f1) {
                     f3 gp = F.gl + F.gx * (float)i;
                     tri_brick_scatter(tg, brick_of(S.tn), gp.x - (float)S.t0[0], gp.y - (float)S.t0[1],
                                        gp.z - (float)S.t0[2], tot);
