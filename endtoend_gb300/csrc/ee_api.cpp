@@ -235,7 +235,14 @@ void terma_box(const EeParams& P, const EeBeamSpec& S, int t0[3], int tn[3]) {
     }
     for (int a = 0; a < 3; a++) { t0[a] = P.bb0[a]; tn[a] = 0; }
     if (dmax <= 0) return;  // the bbox lies behind the source
-    dmin = std::max(dmin, 1e-6);
+    if (dmin <= 1e-3 * S.isodist) {
+        // the source sits inside (or close to) the calc bbox: the beamlet
+        // lookup takes |depth| (cudaSiddon.cu:148-152), so voxels behind the
+        // source see a mirrored field; TERMA over the whole bbox, as the
+        // reference computes it
+        for (int a = 0; a < 3; a++) tn[a] = P.bbs[a];
+        return;
+    }
     const double hu = 0.5 * S.fmap[0] * S.beamlet[0], hw = 0.5 * S.fmap[1] * S.beamlet[1];
     double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
     for (int c = 0; c < 8; c++) {

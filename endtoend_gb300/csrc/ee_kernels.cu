@@ -647,13 +647,22 @@ constexpr int CONE_U = 4;
 // a sample is outside when one side's form is below minus its change over
 // two voxels per axis (the trilinear corners, and supersampled centres half
 // a voxel beyond them).
-__device__ __forceinline__ void field_span(const EeParams& P, const EeBeamSpec& S, const LineFrame& F, int& s0,
-                                           int& s1) {
+__device__ __forceinline__ void field_span(const EeParams& P, const EeBeamSpec& S, const LineFrame& F, int i0, int n,
+                                           int& s0, int& s1) {
     const f3 vox = mk(P.voxel[0], P.voxel[1], P.voxel[2]);
     const f3 d0 = mk(P.start[0] + vox.x * F.gl.x - S.src[0], P.start[1] + vox.y * F.gl.y - S.src[1],
                      P.start[2] + vox.z * F.gl.z - S.src[2]);  // diff at sample 0
     const f3 d1 = mk(vox.x * F.gx.x, vox.y * F.gx.y, vox.z * F.gx.z);  // diff step per sample
     const f3 dir = ld3(S.dir);
+    // the forms hold in front of the source (proj > 0); beamlet_of mirrors
+    // points behind it, so a segment that does not stay well in front of
+    // the source (proj linear in i: its ends decide) is not restricted
+    const float pa = dot(dir, d0) + dot(dir, d1) * (float)i0, pb = dot(dir, d0) + dot(dir, d1) * (float)(i0 + n - 1);
+    if (!(fminf(pa, pb) > 1e-2f * S.isodist)) {
+        s0 = -0x3fffffff;
+        s1 = 0x3fffffff;
+        return;
+    }
     float lo = -1e9f, hi = 1e9f;
 #pragma unroll
     for (int a = 0; a < 2; a++) {
@@ -715,7 +724,7 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_lane(EeParams P, const EeBe
     const float* tb = terma + S.t_off;
     const LineFrame F = line_frame(R, tY, tZ);
     int f0, f1;  // samples that can see TERMA
-    field_span(P, S, F, f0, f1);
+    field_span(P, S, F, i0, n, f0, f1);
     // (rho, T) of each sample, kept from the forward pass for the reverse
     // one, line-major ([i][line]) in this cone's slot of the scratch
     const long long nl = R.nlines;
@@ -834,7 +843,7 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_T_lane(EeParams P, const Ee
     const EeBeamSpec& S = specs[b];
     const LineFrame F = line_frame(R, tY, tZ);
     int f0, f1;  // samples whose TERMA corners can lie in the field (field_span)
-    field_span(P, S, F, f0, f1);
+    field_span(P, S, F, i0, n, f0, f1);
     const long long nl = R.nlines;  // line-major scratch [i][line]
     const long long row = G.arena_off + R.offset + line;
     const Brick Bv = rev_brick(R.rev[0], R.rev[1], R.rev[2]);  // bricked REV gradient
