@@ -154,7 +154,7 @@ cudaError_t ee_launch_gather_T(const EeParams& P, const EeBeamSpec* specs, const
 cudaError_t ee_launch_cone_T(const EeParams& P, const EeBeamSpec* specs, const EeBeamGeom* geoms, const float* rev_grad,
                              float2* scratch, float* terma_grad, int nbeams, int max_lines, int max_line,
                              cudaStream_t s, int lane_block = 128);
-// zeros on every line's read span of a chunk's REV gradient arena (before
+// zeros on every line's segment of a chunk's REV gradient arena (before
 // ee_launch_gather_T; the forward cone kernels zero their own arena)
 cudaError_t ee_launch_rev_zero(const EeParams& P, const EeBeamGeom* geoms, float* rev_grad, int nbeams, int max_lines,
                                cudaStream_t s);

@@ -800,11 +800,12 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_lane(EeParams P, const EeBe
     }
 }
 
-// Zero the read spans (line_read_span) of every line of a chunk's REV
-// gradient arena before k_gather_T adds into it: the samples the adjoint
-// gather and cone can touch, instead of a clear of the whole arena.
+// Zero the segment (line_segment) of every line of a chunk's REV gradient
+// arena before k_gather_T adds into it: the samples the adjoint cone reads.
+// k_gather_T also adds into the rest of the line's read span; those cells are
+// never read, so they need no zero.
 template <int LANE_BLOCK>
-__global__ void __launch_bounds__(LANE_BLOCK) k_rev_zero(const EeBeamGeom* __restrict__ geoms,
+__global__ void __launch_bounds__(LANE_BLOCK) k_rev_zero(EeParams P, const EeBeamGeom* __restrict__ geoms,
                                                          float* __restrict__ rev_grad) {
     const int ray = blockIdx.y, b = blockIdx.z;
     const EeBeamGeom& G = geoms[b];
@@ -814,9 +815,9 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_rev_zero(const EeBeamGeom* __res
     if (!lane_line(R, blockIdx.x * LANE_BLOCK + threadIdx.x, tY, tZ)) return;
     const Brick Bv = rev_brick(R.rev[0], R.rev[1], R.rev[2]);
     float* out = rev_grad + G.arena_off + R.offset + bk_x(tY) + bk_y(Bv, tZ);
-    int z0, z1;
-    line_read_span(G, R, tY, tZ, R.rev[0], z0, z1);
-    for (int i = z0; i <= z1; i++) out[bk_z(Bv, i)] = 0.f;
+    int i0, n;
+    line_segment(P, G, R, tY, tZ, R.rev[0], i0, n);
+    for (int i = i0; i < i0 + n; i++) out[bk_z(Bv, i)] = 0.f;
 }
 
 // Adjoint of k_cone_lane followed by the transpose of the REV TERMA resample.
@@ -1403,7 +1404,7 @@ cudaError_t ee_launch_cone(const EeParams& P, const EeBeamSpec* specs, const EeB
 
 cudaError_t ee_launch_rev_zero(const EeParams& P, const EeBeamGeom* geoms, float* rev_grad, int nbeams, int max_lines,
                                cudaStream_t s) {
-    k_rev_zero<128><<<dim3(grid1(max_lines, 128), P.nrays, nbeams), 128, 0, s>>>(geoms, rev_grad);
+    k_rev_zero<128><<<dim3(grid1(max_lines, 128), P.nrays, nbeams), 128, 0, s>>>(P, geoms, rev_grad);
     return cudaGetLastError();
 }
 
