@@ -118,7 +118,7 @@ struct EeBeamGeom {
     // patient rows (y,z) whose voxels can see this beam's REV dose: the AABB
     // of the crop box dilated by 2 voxels, clipped to the calc bbox
     int gy0, gz0, gny, gnz;
-    int rows;
+    int rows;              // row groups of the forward gather: ceil(gny / 4) * gnz
     int gx0, gnx;          // x range of the same AABB
     int tiles;             // 8x8x4 patient tiles covering the AABB (adjoint gather)
     long long arena_off;   // element offset of this beam's REV arena

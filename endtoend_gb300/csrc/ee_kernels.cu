@@ -237,7 +237,7 @@ __global__ void k_geometry(EeParams P, const EeBeamSpec* __restrict__ specs, EeB
         int z0 = max(P.bb0[2], (int)floorf(lo[2]) - 1), z1 = min(P.bb0[2] + P.bbs[2] - 1, (int)ceilf(hi[2]) + 1);
         G.gx0 = x0; G.gy0 = y0; G.gz0 = z0;
         G.gnx = max(0, x1 - x0 + 1); G.gny = max(0, y1 - y0 + 1); G.gnz = max(0, z1 - z0 + 1);
-        G.rows = G.gny * G.gnz;
+        G.rows = ((G.gny + 3) >> 2) * G.gnz;
         G.tiles = ((G.gnx + 7) / 8) * ((G.gny + 7) / 8) * ((G.gnz + 3) / 4);
         long long off = 0;
         int ml = 0, mls = 0;
@@ -1041,10 +1041,13 @@ __device__ __forceinline__ bool row_span(const EeParams& P, const EeBeamSpec& S,
 
 constexpr int ROW_WARPS = 8;
 
-// REV2XYZdose (device.cu:222-261) for all cones at once: one warp per
-// patient row of one beam's AABB, lanes sweeping the row's span; a voxel
-// sums the trilinear REV dose of every cone.  mode 0/1: atomic accumulation
-// into dose; mode 2: dose[b] written directly.
+// REV2XYZdose (device.cu:222-261) for all cones at once.  A warp takes a
+// group of four patient rows (y .. y+3, one z) of one beam's AABB and sweeps
+// the union of their spans in 8 x 4 patches (lane = x % 8 + 8 * (y % 4)): a
+// compact patch of voxels maps to a compact patch of REV cells, so a corner
+// load of the warp touches fewer cache lines than a run of 32 voxels along x
+// would.  A voxel sums the trilinear REV dose of every cone.  mode 0/1:
+// atomic accumulation into dose; mode 2: dose[b] written directly.
 __global__ void __launch_bounds__(ROW_WARPS * 32) k_gather(EeParams P, const EeBeamSpec* __restrict__ specs,
                                                            const EeBeamGeom* __restrict__ geoms,
                                                            const float* __restrict__ rev, float* __restrict__ dose,
@@ -1068,17 +1071,27 @@ __global__ void __launch_bounds__(ROW_WARPS * 32) k_gather(EeParams P, const EeB
         s_ray[r][c] = v;
     }
     __syncthreads();
-    const int row = blockIdx.x * ROW_WARPS + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-    if (row >= G.rows) return;
-    const int y = G.gy0 + row % G.gny, z = G.gz0 + row / G.gny;
+    const int grp = blockIdx.x * ROW_WARPS + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (grp >= G.rows) return;
+    const int ngy = (G.gny + 3) >> 2;
+    const int lx = lane & 7, yy = (grp % ngy) * 4 + (lane >> 3);
+    const int y = G.gy0 + yy, z = G.gz0 + grp / ngy;
     const EeBeamSpec& S = specs[b];
-    int x0, x1;
-    if (!row_span(P, S, G, y, z, x0, x1)) return;
+    int x0 = 0, x1 = -1;
+    if (yy >= G.gny || !row_span(P, S, G, y, z, x0, x1)) {
+        x0 = 0;
+        x1 = -1;
+    }
+    const int wx0 = __reduce_min_sync(FULL, x0 <= x1 ? x0 : INT_MAX);
+    const int wx1 = __reduce_max_sync(FULL, x0 <= x1 ? x1 : INT_MIN);
+    if (wx0 > wx1) return;
     float* out = dose + S.out_off + (mode == 2 ? (long long)b * nfull : 0ll);
     const long long rbase = (long long)P.size[0] * (y + (long long)P.size[1] * z);
     const float* base = rev + G.arena_off;
     const float dy = (float)y - G.lim_off[1], dz = (float)z - G.lim_off[2];
-    for (int x = x0 + lane; x <= x1; x += 32) {
+    for (int xs = wx0; xs <= wx1; xs += 8) {
+        const int x = xs + lx;
+        if (x < x0 || x > x1) continue;
         const float dx = (float)x - G.lim_off[0];
         // voxels more than 2 BEV voxels outside the crop box see no REV dose
         const f3 bi = mv(S.MB, mk(dx, dy, dz));
@@ -1109,8 +1122,9 @@ __global__ void __launch_bounds__(ROW_WARPS * 32) k_gather(EeParams P, const EeB
 // the affine patient -> REV map) is accumulated in shared memory first, then
 // flushed with one global reduction per non-zero quad of REV samples.  The
 // footprints of all cones are computed up front; consecutive cones alternate
-// between two shared buffers, so a cone's zeroing need not wait for the
-// previous cone's flush.
+// between two shared buffers.  The flush clears the quads it sends, so every
+// buffer is all zero again when its next cone scatters into it, and one
+// barrier per cone (between its scatter and its flush) suffices.
 constexpr int GT_TX = 8, GT_TY = 8, GT_TZ = 4;
 // floats per footprint buffer: an 8x8x4 tile spans at most |(7,7,3)| + 2 = 13
 // REV cells per axis when the REV spacing equals the voxel size (16 in tY
@@ -1124,7 +1138,10 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
                                                                    const float* __restrict__ dose_grad,
                                                                    float* __restrict__ rev_grad) {
     extern __shared__ float acc_all[];
-    __shared__ int s_box[EE_MAX_RAYS][10];
+    // per cone: {l0, n0, l1, n1}, {l2, n2, s1, rev0}, {rev1, rev2, offset lo, offset hi}
+    // (box origin and extent per REV axis, the box's tY row stride, the REV
+    // sizes and the cone's arena offset), read with three vector loads
+    __shared__ int4 s_p[EE_MAX_RAYS][3];
     __shared__ float4 s_A[EE_MAX_RAYS][3];
     const int b = blockIdx.z;
     const EeBeamGeom& G = geoms[b];
@@ -1165,58 +1182,64 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
         }
         // REV axes: q.y -> rev[0] (along the line), q.z -> rev[1], q.x -> rev[2]
         const int dim = a == 1 ? R.rev[0] : (a == 2 ? R.rev[1] : R.rev[2]);
-        const int slot = a == 1 ? 0 : (a == 2 ? 2 : 4);
         int l = max(0, (int)floorf(lo - 1e-3f));
         const int h = min(dim - 1, (int)floorf(hi + 1e-3f) + 1);
         int w = h - l + 1;
-        if (a == 2 && w > 0) {
-            // tY range on whole quads: a box row of 4 tY cells is one
-            // 16-byte brick row of the REV gradient (flushed as one vector
-            // reduction); the cells past rev[1] are brick padding
-            w = ((h | 3) + 1) - (l & ~3);
-            l &= ~3;
-            // row stride 4 (mod 8) floats: the rows of x-adjacent voxels
-            // spread over the shared banks; the extra quad of a row is never
-            // scattered to (k1 < w), stays zero and is not flushed
-            s_box[r][9] = (w & 7) == 0 ? w + 4 : w;
+        int* sp = reinterpret_cast<int*>(s_p[r]);
+        if (a == 2) {
+            int s1 = 0;
+            if (w > 0) {
+                // tY range on whole quads: a box row of 4 tY cells is one
+                // 16-byte brick row of the REV gradient (flushed as one
+                // vector reduction); the cells past rev[1] are brick padding
+                w = ((h | 3) + 1) - (l & ~3);
+                l &= ~3;
+                // row stride 4 (mod 8) floats: the rows of x-adjacent voxels
+                // spread over the shared banks; the extra quad of a row is
+                // never scattered to (k1 < w), stays zero and is not sent
+                s1 = (w & 7) == 0 ? w + 4 : w;
+            }
+            sp[6] = s1;
         }
-        s_box[r][slot] = l;
-        s_box[r][slot + 1] = w;
+        const int slot = a == 1 ? 0 : (a == 2 ? 2 : 4);
+        sp[slot] = l;
+        sp[slot + 1] = w;
+        sp[7 + a] = R.rev[a];
+        if (a == 0) {
+            sp[10] = (int)(unsigned)(R.offset & 0xffffffffll);
+            sp[11] = (int)(R.offset >> 32);
+        }
         // this cone's map for the voxels: the row [A | -q0] of REV axis a
         // (the forward gather forms q in the same order)
         s_A[r][a] = make_float4(Ar[0], Ar[1], Ar[2], -R.q0[a]);
-        s_box[r][6 + a] = R.rev[a];
     }
+    float4* const all4 = reinterpret_cast<float4*>(acc_all);
+    for (int k = t; k < GT_SMEM / 4; k += blockDim.x) all4[k] = make_float4(0.f, 0.f, 0.f, 0.f);
     __syncthreads();
     float* base = rev_grad + G.arena_off;
     int parity = 0;  // buffer of the next shared-memory cone
     for (int r = 0; r < P.nrays; r++) {
-        const EeRayGeom& R = G.ray[r];
-        const int l0 = s_box[r][0], n0 = s_box[r][1], l1 = s_box[r][2], n1 = s_box[r][3], l2 = s_box[r][4],
-                  n2 = s_box[r][5];
+        const int4 p0 = s_p[r][0], p1 = s_p[r][1], p2 = s_p[r][2];
+        const int l0 = p0.x, n0 = p0.y, l1 = p0.z, n1 = p0.w, l2 = p1.x, n2 = p1.y;
+        const int rv0 = p1.w, rv1 = p2.x, rv2 = p2.y;
         const bool empty = n0 <= 0 || n1 <= 0 || n2 <= 0;
-        const int s1 = empty ? 0 : s_box[r][9];  // row stride of the box (>= n1, a multiple of 4)
+        const int s1 = empty ? 0 : p1.z;  // row stride of the box (>= n1, a multiple of 4)
         // rows per slab: odd, so that the slab stride s1 * n0p is 4 x odd
         // (mod 32) and the slabs of y-adjacent voxels spread over the banks
         // too; the padding rows (k0 >= n0) are never scattered to
         const int n0p = n0 | 1;
         const int nbox = empty ? 0 : n0p * s1 * n2;
         if (nbox > 0 && nbox <= GT_BUF) {
-            // buffers alternate over the shared-memory cones: the last reader
-            // of this buffer (the flush two such cones back) finished before
-            // the barrier after the previous cone's zeroing
+            // buffers alternate over the shared-memory cones: the last flush
+            // of this buffer (two such cones back) was cleared by every
+            // thread before the barrier of the previous cone
             float* acc = acc_all + parity * GT_BUF;
             parity ^= 1;
-            float4* acc4 = reinterpret_cast<float4*>(acc);  // n1 (tY) is a multiple of 4
-            const int nquad = nbox >> 2;
-            for (int k = t; k < nquad; k += blockDim.x) acc4[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-            __syncthreads();
             if (gd != 0.f) {
                 const float4 a0 = s_A[r][0], a1 = s_A[r][1], a2 = s_A[r][2];
                 const f3 q = mk(fmaf(a0.x, dx, fmaf(a0.y, dy, fmaf(a0.z, dz, a0.w))),
                                 fmaf(a1.x, dx, fmaf(a1.y, dy, fmaf(a1.z, dz, a1.w))),
                                 fmaf(a2.x, dx, fmaf(a2.y, dy, fmaf(a2.z, dz, a2.w))));
-                const int rv0 = s_box[r][6], rv1 = s_box[r][7], rv2 = s_box[r][8];
                 if (!(q.y >= (float)rv0 || q.z >= (float)rv1 || q.x >= (float)rv2 || q.x < 0.f || q.y < 0.f ||
                       q.z < 0.f)) {
                     float f0 = floorf(q.y), f1 = floorf(q.z), f2 = floorf(q.x);
@@ -1243,19 +1266,23 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
                 }
             }
             __syncthreads();
-            float* rb = base + R.offset;
-            const Brick Bv = rev_brick(R.rev[0], R.rev[1], R.rev[2]);
+            float* rb = base + (long long)(((unsigned long long)(unsigned)p2.w << 32) | (unsigned)p2.z);
+            const Brick Bv = rev_brick(rv0, rv1, rv2);
             // one box quad (4 tY cells) per iteration, quad index = kq + nq1 *
             // (k0 + n0p * k2); (k + 0.5) / n is at least 1/(2n) away from an
             // integer, far above the FP32 error for these sizes, so the float
             // quotients are exact.  A non-zero quad is one 16-byte vector
             // reduction into the bricked REV gradient (brick rows are 16-byte
-            // aligned: arena and cone offsets are multiples of 64 floats).
+            // aligned: arena and cone offsets are multiples of 64 floats),
+            // and is cleared for the buffer's next cone.
+            float4* acc4 = reinterpret_cast<float4*>(acc);  // s1 is a multiple of 4
+            const int nquad = nbox >> 2;
             const int nq1 = s1 >> 2;
             const float invq = 1.f / (float)nq1, inv0 = 1.f / (float)n0p;
             for (int k = t; k < nquad; k += blockDim.x) {
                 const float4 v = acc4[k];
                 if (v.x != 0.f || v.y != 0.f || v.z != 0.f || v.w != 0.f) {
+                    acc4[k] = make_float4(0.f, 0.f, 0.f, 0.f);
                     const int q1 = __float2int_rd(((float)k + 0.5f) * invq);
                     const int kq = k - q1 * nq1;
                     const int k2 = __float2int_rd(((float)q1 + 0.5f) * inv0);
@@ -1266,6 +1293,7 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
         } else if (nbox > GT_BUF && gd != 0.f) {
             // footprint too large for a shared buffer (a REV spacing finer
             // than the voxels): scatter directly
+            const EeRayGeom& R = G.ray[r];
             const float4 a0 = s_A[r][0], a1 = s_A[r][1], a2 = s_A[r][2];
             const f3 q = mk(fmaf(a0.x, dx, fmaf(a0.y, dy, fmaf(a0.z, dz, a0.w))),
                             fmaf(a1.x, dx, fmaf(a1.y, dy, fmaf(a1.z, dz, a1.w))),
