@@ -669,7 +669,7 @@ PlanBound plan_bound(const ee_context* c, const EeBeamSpec& S) {
         long long h = std::min<long long>(P.bb0[a] + P.bbs[a] - 1, (long long)std::ceil(hi[a]) + 2);
         n[a] = std::max<long long>(1, h - l + 1);
     }
-    B.rows = (int)(((n[1] + 3) / 4) * n[2]);
+    B.rows = (int)ee_gather_groups(n[1], n[2]);
     B.tiles = (int)(((n[0] + 7) / 8) * ((n[1] + 7) / 8) * ((n[2] + 3) / 4));
     return B;
 }

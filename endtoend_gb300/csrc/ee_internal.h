@@ -57,6 +57,13 @@ inline __host__ __device__ long long ee_brick_vol(const int tn[3]) {
     return 64ll * ((tn[0] + 3) >> 2) * ((tn[1] + 3) >> 2) * ((tn[2] + 3) >> 2);
 }
 
+// The forward gather's warp patch: EE_GATHER_PX x EE_GATHER_PY x EE_GATHER_PZ
+// patient voxels (32 lanes); a warp owns a group of PY x PZ patient rows.
+constexpr int EE_GATHER_PX = 8, EE_GATHER_PY = 2, EE_GATHER_PZ = 2;
+inline __host__ __device__ long long ee_gather_groups(long long ny, long long nz) {
+    return ((ny + EE_GATHER_PY - 1) / EE_GATHER_PY) * ((nz + EE_GATHER_PZ - 1) / EE_GATHER_PZ);
+}
+
 // Per-beam constants built on the host.
 struct EeBeamSpec {
     float src[3];
@@ -118,7 +125,7 @@ struct EeBeamGeom {
     // patient rows (y,z) whose voxels can see this beam's REV dose: the AABB
     // of the crop box dilated by 2 voxels, clipped to the calc bbox
     int gy0, gz0, gny, gnz;
-    int rows;              // row groups of the forward gather: ceil(gny / 4) * gnz
+    int rows;              // row groups of the forward gather (ee_gather_groups)
     int gx0, gnx;          // x range of the same AABB
     int tiles;             // 8x8x4 patient tiles covering the AABB (adjoint gather)
     long long arena_off;   // element offset of this beam's REV arena

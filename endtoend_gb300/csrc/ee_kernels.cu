@@ -237,7 +237,7 @@ __global__ void k_geometry(EeParams P, const EeBeamSpec* __restrict__ specs, EeB
         int z0 = max(P.bb0[2], (int)floorf(lo[2]) - 1), z1 = min(P.bb0[2] + P.bbs[2] - 1, (int)ceilf(hi[2]) + 1);
         G.gx0 = x0; G.gy0 = y0; G.gz0 = z0;
         G.gnx = max(0, x1 - x0 + 1); G.gny = max(0, y1 - y0 + 1); G.gnz = max(0, z1 - z0 + 1);
-        G.rows = ((G.gny + 3) >> 2) * G.gnz;
+        G.rows = (int)ee_gather_groups(G.gny, G.gnz);
         G.tiles = ((G.gnx + 7) / 8) * ((G.gny + 7) / 8) * ((G.gnz + 3) / 4);
         long long off = 0;
         int ml = 0, mls = 0;
@@ -1042,11 +1042,10 @@ __device__ __forceinline__ bool row_span(const EeParams& P, const EeBeamSpec& S,
 constexpr int ROW_WARPS = 8;
 
 // REV2XYZdose (device.cu:222-261) for all cones at once.  A warp takes a
-// group of four patient rows (y .. y+3, one z) of one beam's AABB and sweeps
-// the union of their spans in 8 x 4 patches (lane = x % 8 + 8 * (y % 4)): a
-// compact patch of voxels maps to a compact patch of REV cells, so a corner
-// load of the warp touches fewer cache lines than a run of 32 voxels along x
-// would.  A voxel sums the trilinear REV dose of every cone.  mode 0/1:
+// group of PY x PZ patient rows (EE_GATHER_*) of one beam's AABB and sweeps
+// the union of their spans in PX x PY x PZ patches: a compact patch of voxels
+// maps to a compact patch of REV cells, so a corner load of the warp touches
+// fewer cache lines than a run of 32 voxels along x would.  A voxel sums the trilinear REV dose of every cone.  mode 0/1:
 // atomic accumulation into dose; mode 2: dose[b] written directly.
 __global__ void __launch_bounds__(ROW_WARPS * 32) k_gather(EeParams P, const EeBeamSpec* __restrict__ specs,
                                                            const EeBeamGeom* __restrict__ geoms,
@@ -1073,12 +1072,14 @@ __global__ void __launch_bounds__(ROW_WARPS * 32) k_gather(EeParams P, const EeB
     __syncthreads();
     const int grp = blockIdx.x * ROW_WARPS + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (grp >= G.rows) return;
-    const int ngy = (G.gny + 3) >> 2;
-    const int lx = lane & 7, yy = (grp % ngy) * 4 + (lane >> 3);
-    const int y = G.gy0 + yy, z = G.gz0 + grp / ngy;
+    constexpr int PX = EE_GATHER_PX, PY = EE_GATHER_PY;
+    const int ngy = (G.gny + PY - 1) / PY;
+    const int lx = lane % PX, yy = (grp % ngy) * PY + (lane / PX) % PY;
+    const int zz = (grp / ngy) * EE_GATHER_PZ + lane / (PX * PY);
+    const int y = G.gy0 + yy, z = G.gz0 + zz;
     const EeBeamSpec& S = specs[b];
     int x0 = 0, x1 = -1;
-    if (yy >= G.gny || !row_span(P, S, G, y, z, x0, x1)) {
+    if (yy >= G.gny || zz >= G.gnz || !row_span(P, S, G, y, z, x0, x1)) {
         x0 = 0;
         x1 = -1;
     }
@@ -1089,7 +1090,7 @@ __global__ void __launch_bounds__(ROW_WARPS * 32) k_gather(EeParams P, const EeB
     const long long rbase = (long long)P.size[0] * (y + (long long)P.size[1] * z);
     const float* base = rev + G.arena_off;
     const float dy = (float)y - G.lim_off[1], dz = (float)z - G.lim_off[2];
-    for (int xs = wx0; xs <= wx1; xs += 8) {
+    for (int xs = wx0; xs <= wx1; xs += PX) {
         const int x = xs + lx;
         if (x < x0 || x > x1) continue;
         const float dx = (float)x - G.lim_off[0];
