@@ -1271,15 +1271,15 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
             const Brick Bv = rev_brick(rv0, rv1, rv2);
             // one box quad (4 tY cells) per iteration, quad index = kq + nq1 *
             // (k0 + n0p * k2); (k + 0.5) / n is at least 1/(2n) away from an
-            // integer, far above the FP32 error for these sizes, so the float
-            // quotients are exact.  A non-zero quad is one 16-byte vector
+            // integer, far above the FP32 error of (k + 0.5) * rcp(n) for
+            // these sizes, so the floored quotients are exact.  A non-zero quad is one 16-byte vector
             // reduction into the bricked REV gradient (brick rows are 16-byte
             // aligned: arena and cone offsets are multiples of 64 floats),
             // and is cleared for the buffer's next cone.
             float4* acc4 = reinterpret_cast<float4*>(acc);  // s1 is a multiple of 4
             const int nquad = nbox >> 2;
             const int nq1 = s1 >> 2;
-            const float invq = 1.f / (float)nq1, inv0 = 1.f / (float)n0p;
+            const float invq = __frcp_rn((float)nq1), inv0 = __frcp_rn((float)n0p);
             for (int k = t; k < nquad; k += blockDim.x) {
                 const float4 v = acc4[k];
                 if (v.x != 0.f || v.y != 0.f || v.z != 0.f || v.w != 0.f) {
