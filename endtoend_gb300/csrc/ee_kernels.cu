@@ -1047,10 +1047,10 @@ constexpr int ROW_WARPS = 8;
 // group of PY x PZ patient rows (EE_GATHER_*) of one beam's AABB and sweeps
 // the union of their spans in PX x PY x PZ patches: a compact patch of voxels
 // maps to a compact patch of REV cells, so a corner load of the warp touches
-// fewer cache lines than a run of 32 voxels along x would.  A voxel sums the trilinear REV dose of every cone.  mode 0/1:
-// atomic accumulation into dose; mode 2: dose[b] written directly.
-// six resident blocks per SM: 40 registers without spills, measured faster
-// than 48
+// fewer cache lines than a run of 32 voxels along x would.  A voxel sums the
+// trilinear REV dose of every cone.  mode 0/1: atomic accumulation into dose;
+// mode 2: dose[b] written directly.  Six resident blocks per SM: 40
+// registers without spills, measured faster than 48.
 __global__ void __launch_bounds__(ROW_WARPS * 32, 6) k_gather(EeParams P, const EeBeamSpec* __restrict__ specs,
                                                            const EeBeamGeom* __restrict__ geoms,
                                                            const float* __restrict__ rev, float* __restrict__ dose,
