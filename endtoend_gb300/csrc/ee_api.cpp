@@ -698,6 +698,13 @@ struct ee_plan {
     std::vector<int> status;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
+    // releases everything, also when ee_plan_create fails half-way
+    ~ee_plan() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        d_specs.release(); d_geoms.release(); terma.release(); unit.release(); terma_grad.release();
+        rev.release(); rev_grad.release(); bl_idx.release(); samples.release();
+    }
 };
 
 namespace {
@@ -1242,10 +1249,6 @@ int ee_plan_destroy(ee_plan* pl) {
     if (!pl) return EE_OK;
     cudaSetDevice(pl->c->device);
     cudaStreamSynchronize(pl->c->stream);
-    if (pl->exec) cudaGraphExecDestroy(pl->exec);
-    if (pl->graph) cudaGraphDestroy(pl->graph);
-    pl->d_specs.release(); pl->d_geoms.release(); pl->terma.release(); pl->unit.release();
-    pl->terma_grad.release(); pl->rev.release(); pl->rev_grad.release(); pl->bl_idx.release(); pl->samples.release();
     delete pl;
     return EE_OK;
 }
