@@ -1247,25 +1247,30 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
                                 fmaf(a2.x, dx, fmaf(a2.y, dy, fmaf(a2.z, dz, a2.w))));
                 if (!(q.y >= (float)rv0 || q.z >= (float)rv1 || q.x >= (float)rv2 || q.x < 0.f || q.y < 0.f ||
                       q.z < 0.f)) {
-                    float f0 = floorf(q.y), f1 = floorf(q.z), f2 = floorf(q.x);
-                    int i0 = (int)f0, i1 = (int)f1, i2 = (int)f2;
-                    float a0 = q.y - f0, a1 = q.z - f1, a2 = q.x - f2;
+                    const float f0 = floorf(q.y), f1 = floorf(q.z), f2 = floorf(q.x);
+                    const int j0 = (int)f0 - l0, j1 = (int)f1 - l1, j2 = (int)f2 - l2;
+                    const float a0 = q.y - f0, a1 = q.z - f1, a2 = q.x - f2;
+                    // Corners outside the box get weight 0 and a clamped
+                    // index inside it, so the eight adds need no tests.  The
+                    // box ends at the last REV cell in i and tZ, so that is
+                    // the array edge there (tri_brick's border); in tY it can
+                    // reach the brick padding past rev[1], cells no line
+                    // owns, which the flush sends but nothing reads.
+                    const float w0[2] = {j0 >= 0 && j0 < n0 ? 1.f - a0 : 0.f, j0 + 1 >= 0 && j0 + 1 < n0 ? a0 : 0.f};
+                    const float w1[2] = {j1 >= 0 && j1 < n1 ? 1.f - a1 : 0.f, j1 + 1 >= 0 && j1 + 1 < n1 ? a1 : 0.f};
+                    const float w2[2] = {j2 >= 0 && j2 < n2 ? 1.f - a2 : 0.f, j2 + 1 >= 0 && j2 + 1 < n2 ? a2 : 0.f};
+                    const int c0[2] = {min(max(j0, 0), n0 - 1), min(max(j0 + 1, 0), n0 - 1)};
+                    const int c1[2] = {min(max(j1, 0), n1 - 1), min(max(j1 + 1, 0), n1 - 1)};
+                    const int c2[2] = {min(max(j2, 0), n2 - 1), min(max(j2 + 1, 0), n2 - 1)};
 #pragma unroll
                     for (int d2 = 0; d2 < 2; d2++) {
-                        int k2 = i2 + d2 - l2;
-                        if (i2 + d2 >= rv2 || k2 < 0 || k2 >= n2) continue;
-                        float w2 = (d2 ? a2 : 1.f - a2) * gd;
+                        const float t2 = w2[d2] * gd;
 #pragma unroll
                         for (int d1 = 0; d1 < 2; d1++) {
-                            int k1 = i1 + d1 - l1;
-                            if (i1 + d1 >= rv1 || k1 < 0 || k1 >= n1) continue;
-                            float w1 = (d1 ? a1 : 1.f - a1) * w2;
+                            const float t1 = w1[d1] * t2;
 #pragma unroll
-                            for (int d0 = 0; d0 < 2; d0++) {
-                                int k0 = i0 + d0 - l0;
-                                if (i0 + d0 >= rv0 || k0 < 0 || k0 >= n0) continue;
-                                atomicAdd(acc + k1 + s1 * (k0 + n0p * k2), (d0 ? a0 : 1.f - a0) * w1);
-                            }
+                            for (int d0 = 0; d0 < 2; d0++)
+                                atomicAdd(acc + c1[d1] + s1 * (c0[d0] + n0p * c2[d2]), w0[d0] * t1);
                         }
                     }
                 }
