@@ -713,7 +713,6 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_lane(EeParams P, const EeBe
     int tY, tZ;
     if (!lane_line(R, blockIdx.x * LANE_BLOCK + threadIdx.x, tY, tZ)) return;
     const int L = R.rev[0];
-    const int line = tZ * R.rev[1] + tY;
     // bricked REV arena: this line's sample i sits at out + bk_z(i)
     const Brick Bv = rev_brick(R.rev[0], R.rev[1], R.rev[2]);
     float* out = rev + G.arena_off + R.offset + bk_x(tY) + bk_y(Bv, tZ);
@@ -728,9 +727,10 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_lane(EeParams P, const EeBe
     int f0, f1;  // samples that can see TERMA
     field_span(P, S, F, i0, n, f0, f1);
     // (rho, T) of each sample, kept from the forward pass for the reverse
-    // one, line-major ([i][line]) in this cone's slot of the scratch
-    const long long nl = R.nlines;
-    float2* smp = samples + G.arena_off + R.offset + line;
+    // one, in this cone's slot of the scratch bricked like the REV arena:
+    // sample i of the line at smp[bk_z(i)], so a warp's 8 x 4 lines write two
+    // whole 128-byte lines per sample
+    float2* smp = samples + G.arena_off + R.offset + bk_x(tY) + bk_y(Bv, tZ);
     const EeRayConst& RC = P.rays[ray];
     const float delr = P.lng;
     // samples are gathered CONE_U at a time before the recurrence consumes
@@ -758,7 +758,7 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_lane(EeParams P, const EeBe
                 const bool v = r >= 0.f;
                 const float h1 = v ? __expf(e1 * r) : 1.f, h2 = v ? __expf(e2 * r) : 1.f;
                 const float t = v ? tt[j] : 0.f;
-                smp[i * nl] = make_float2(r, t);
+                smp[bk_z(Bv, i)] = make_float2(r, t);
                 out[bk_z(Bv, i)] = v ? c1 * (Y1 + tm * (1.f - hm1)) + c2 * (Y2 + tm * (1.f - hm2)) : 0.f;
                 Y1 = fmaf(h1 * h1, Y1, tm * h1 * (1.f - hm1 * h1));
                 Y2 = fmaf(h2 * h2, Y2, tm * h2 * (1.f - hm2 * h2));
@@ -780,7 +780,7 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_lane(EeParams P, const EeBe
                 rt[j] = make_float2(-1.f, 0.f);
                 ov[j] = 0.f;
                 if (ib - j >= i0) {
-                    rt[j] = smp[(ib - j) * nl];
+                    rt[j] = smp[bk_z(Bv, ib - j)];
                     ov[j] = out[bk_z(Bv, ib - j)];
                 }
             }
@@ -839,7 +839,6 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_T_lane(EeParams P, const Ee
     int tY, tZ;
     if (!lane_line(R, blockIdx.x * LANE_BLOCK + threadIdx.x, tY, tZ)) return;
     const int L = R.rev[0];
-    const int line = tZ * R.rev[1] + tY;
     int i0, n;
     line_segment(P, G, R, tY, tZ, L, i0, n);
     if (n <= 0) return;
@@ -847,11 +846,10 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_T_lane(EeParams P, const Ee
     const LineFrame F = line_frame(R, tY, tZ);
     int f0, f1;  // samples whose TERMA corners can lie in the field (field_span)
     field_span(P, S, F, i0, n, f0, f1);
-    const long long nl = R.nlines;  // line-major scratch [i][line]
-    const long long row = G.arena_off + R.offset + line;
+    // scratch bricked like the REV arena (k_cone_lane): sample i at sA[bk_z(i)]
     const Brick Bv = rev_brick(R.rev[0], R.rev[1], R.rev[2]);  // bricked REV gradient
     const float* gin = rev_grad + G.arena_off + R.offset + bk_x(tY) + bk_y(Bv, tZ);
-    float2* sA = scratch + row;  // (pass-A contribution to Tbar[i], rho of sample i)
+    float2* sA = scratch + G.arena_off + R.offset + bk_x(tY) + bk_y(Bv, tZ);  // (pass-A part of Tbar[i], rho[i])
     const EeRayConst& RC = P.rays[ray];
     const float delr = P.lng, inv_nphi = 1.f / (float)P.nphi;
     const int i1 = i0 + n - 1;
@@ -864,7 +862,7 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_T_lane(EeParams P, const Ee
         bool v = r >= 0.f;
         float h1 = v ? __expf(e1 * r) : 1.f, h2 = v ? __expf(e2 * r) : 1.f;
         float Z1 = 0.f, Z2 = 0.f;
-        sA[i1 * nl] = make_float2(0.f, r);
+        sA[bk_z(Bv, i1)] = make_float2(0.f, r);
         // inputs gathered CONE_U samples ahead of the recurrence
         for (int ib = i1; ib >= i0; ib -= CONE_U) {
             float gl[CONE_U], rl[CONE_U];
@@ -884,7 +882,7 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_T_lane(EeParams P, const Ee
                 const float rm = rl[j];
                 const bool vm = rm >= 0.f;
                 const float hm1 = vm ? __expf(e1 * rm) : 1.f, hm2 = vm ? __expf(e2 * rm) : 1.f;
-                sA[(i - 1) * nl] = make_float2(vm ? c1 * gi * (1.f - hm1) + Z1 * h1 * (1.f - hm1 * h1) +
+                sA[bk_z(Bv, i - 1)] = make_float2(vm ? c1 * gi * (1.f - hm1) + Z1 * h1 * (1.f - hm1 * h1) +
                                                         c2 * gi * (1.f - hm2) + Z2 * h2 * (1.f - hm2 * h2)
                                                   : 0.f,
                                                rm);
@@ -899,7 +897,7 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_T_lane(EeParams P, const Ee
         const float c1 = prm[0] / prm[1], c2 = prm[2] / prm[3];
         const float e1 = -0.5f * prm[1] * delr, e2 = -0.5f * prm[3] * delr;
         float* tg = terma_grad + S.t_off;
-        float2 a = sA[i0 * nl];
+        float2 a = sA[bk_z(Bv, i0)];
         float r = a.y;
         bool v = r >= 0.f;
         float h1 = v ? __expf(e1 * r) : 1.f, h2 = v ? __expf(e2 * r) : 1.f;
@@ -913,7 +911,7 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_T_lane(EeParams P, const Ee
                 gl[j] = 0.f;
                 al[j] = make_float2(0.f, -1.f);
                 if (i <= i1) gl[j] = gin[bk_z(Bv, i)];
-                if (i < i1) al[j] = sA[(i + 1) * nl];
+                if (i < i1) al[j] = sA[bk_z(Bv, i + 1)];
             }
 #pragma unroll
             for (int j = 0; j < CONE_U; j++) {
