@@ -180,17 +180,22 @@ __device__ __forceinline__ float tri_brick(const float* __restrict__ v, const Br
     return acc;
 }
 
-// Transpose of tri_brick (same weights as tri_border_scatter): an x-pair
-// inside a brick row is one 16-byte-quad vector reduction, a pair across a
-// brick edge two scalar atomics.
+// Transpose of tri_brick (same weights as tri_border_scatter).  Each (y, z)
+// corner row takes one vector reduction on the 16-byte brick row of corner
+// i, holding both x corners unless the pair straddles a brick edge (i % 4 ==
+// 3), and a second one on slot 0 of the next brick row only then (or when
+// corner i is outside the box).  The other slots of a quad receive +0.  No
+// branch on the slot, so the lanes of a warp issue the same two reductions.
 __device__ __forceinline__ void tri_brick_scatter(float* v, const Brick& B, float x, float y, float z, float g) {
     if (!(x > -1.f && x < (float)B.n0 && y > -1.f && y < (float)B.n1 && z > -1.f && z < (float)B.n2)) return;
     float fx = floorf(x), fy = floorf(y), fz = floorf(z);
     int i = (int)fx, j = (int)fy, k = (int)fz;
     float ax = x - fx, ay = y - fy, az = z - fz;
     const bool in0 = i >= 0, in1 = i + 1 < B.n0;
-    const int x0 = in0 ? bk_x(i) : 0, x1 = in1 ? bk_x(i + 1) : 0;
-    const bool quad = in0 && in1 && (i & 3) != 3;
+    const int o = i & 3;                        // slot of corner i in its brick row
+    const bool both = in0 && in1 && o != 3;     // corner i + 1 in the same row
+    const int xa = in0 ? (i >> 2) << 6 : 0;     // brick row of corner i
+    const int xb = in1 ? ((i + 1) >> 2) << 6 : 0;  // brick row of corner i + 1 (slot 0 unless both)
 #pragma unroll
     for (int dk = 0; dk < 2; dk++) {
         int kk = k + dk;
@@ -202,11 +207,13 @@ __device__ __forceinline__ void tri_brick_scatter(float* v, const Brick& B, floa
             if (jj < 0 || jj >= B.n1) continue;
             float w = (dj ? ay : 1.f - ay) * wz * g;
             float* row = v + bk_y(B, jj) + bk_z(B, kk);
-            if (quad) red_pair(row + x0, (1.f - ax) * w, ax * w);
-            else {
-                if (in0) atomicAdd(row + x0, (1.f - ax) * w);
-                if (in1) atomicAdd(row + x1, ax * w);
+            const float wa = (1.f - ax) * w, wb = ax * w;
+            if (in0) {
+                const float pb = both ? wb : 0.f;
+                red_v4(row + xa, o == 0 ? wa : 0.f, o == 1 ? wa : (o == 0 ? pb : 0.f),
+                       o == 2 ? wa : (o == 1 ? pb : 0.f), o == 3 ? wa : (o == 2 ? pb : 0.f));
             }
+            if (in1 && !both) red_v4(row + xb, wb, 0.f, 0.f, 0.f);
         }
     }
 }

@@ -183,3 +183,46 @@ def test_fused_dose_and_adjoint_matches_separate_calls():
         e._check(st)
     assert np.allclose(d, d_sep, rtol=1e-5, atol=1e-6 * d_sep.max())
     assert np.allclose(f, f_sep, rtol=1e-4, atol=1e-5 * np.abs(f_sep).max())
+
+
+def test_rev_array_over_the_limit_is_an_array_size_error(cfg0):
+    """A cone's REV array larger than max_rev_size fails the beam with
+    EE_ERR_REV_SIZE, the reference's ArraySizeError (host.cu:71-74,148-154);
+    the context stays usable once the limit is lifted."""
+    vol, phys, beams = cfg0
+    with engine.Engine(0) as e:
+        e.set_volume(vol)
+        e.set_physics(phys, mode="exp", max_rev_size=(16, 16, 16))
+        with pytest.raises(engine.ArraySizeError) as ei:
+            e.beam_dose(beams)
+        assert ei.value.code == engine.EE_ERR_REV_SIZE
+        e.set_physics(phys, mode="exp")
+        ref, _ = Oracle(vol, phys, kernel_mode=2).beam_dose(beams[0])
+        assert _rel(e.beam_dose(beams), ref) <= 1e-3
+
+
+def test_all_zero_fluence_is_a_crop_box_error(cfg0, eng):
+    """No voxel with TERMA leaves the crop-box scan (host.cu:442-459) empty:
+    the beam fails (the oracle refuses it too), and the next call works."""
+    vol, phys, beams = cfg0
+    z = inputs.Beam(**{**beams[0].__dict__, "fluence": np.zeros_like(beams[0].fluence)})
+    with pytest.raises(RuntimeError):
+        Oracle(vol, phys, kernel_mode=2).beam_dose(z)
+    with pytest.raises(engine.CropBoxError):
+        eng.beam_dose([z])
+    assert eng.beam_dose(beams).max() > 0
+
+
+def test_single_beamlet_map(cfg0, eng):
+    """A 1 x 1 fluence map: forward against the FP64 oracle, adjoint by the
+    dot-product identity <A x, g> = <x, A^T g>."""
+    vol, phys, _ = cfg0
+    b = inputs.single_beam(fmap=(1, 1), beamlet_cm=1.0)
+    d = eng.beam_dose([b])
+    ref, _ = Oracle(vol, phys, kernel_mode=2).beam_dose(b)
+    assert _rel(d, ref) <= 1e-3
+    g = np.random.default_rng(5).standard_normal(d.shape).astype(np.float32)
+    fg = eng.beam_dose_adjoint([b], g)
+    lhs = float(np.dot(d.ravel().astype(np.float64), g.ravel()))
+    rhs = float(np.dot(b.fluence.ravel().astype(np.float64), np.asarray(fg, np.float64).ravel()))
+    assert abs(lhs - rhs) <= 1e-4 * abs(lhs)
