@@ -805,7 +805,11 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_lane(EeParams P, const EeBe
 // Zero the segment (line_segment) of every line of a chunk's REV gradient
 // arena before k_gather_T adds into it: the samples the adjoint cone reads.
 // k_gather_T also adds into the rest of the line's read span; those cells are
-// never read, so they need no zero.
+// never read, so they need no zero.  The four lanes of a brick row (a tY quad
+// at one tZ) zero the union of their lines' segments with 16-byte stores,
+// lane q of the four taking samples i = q (mod 4): a warp's store covers two
+// whole bricks.  Cells of a line outside its own segment that this zeroes are
+// never read either.
 template <int LANE_BLOCK>
 __global__ void __launch_bounds__(LANE_BLOCK) k_rev_zero(EeParams P, const EeBeamGeom* __restrict__ geoms,
                                                          float* __restrict__ rev_grad) {
@@ -814,12 +818,26 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_rev_zero(EeParams P, const EeBea
     if (G.status != 0) return;
     const EeRayGeom& R = G.ray[ray];
     int tY, tZ;
-    if (!lane_line(R, blockIdx.x * LANE_BLOCK + threadIdx.x, tY, tZ)) return;
+    const bool ok = lane_line(R, blockIdx.x * LANE_BLOCK + threadIdx.x, tY, tZ);
+    int lo = 0x7fffffff, hi = -1;
+    if (ok) {
+        int i0, n;
+        line_segment(P, G, R, tY, tZ, R.rev[0], i0, n);
+        if (n > 0) {
+            lo = i0;
+            hi = i0 + n - 1;
+        }
+    }
+    // lanes 4k .. 4k+3 own one brick row (lane_line: tY = lane % 8, tZ = lane / 8)
+    lo = min(lo, __shfl_xor_sync(FULL, lo, 1));
+    hi = max(hi, __shfl_xor_sync(FULL, hi, 1));
+    lo = min(lo, __shfl_xor_sync(FULL, lo, 2));
+    hi = max(hi, __shfl_xor_sync(FULL, hi, 2));
+    if (lo > hi) return;
     const Brick Bv = rev_brick(R.rev[0], R.rev[1], R.rev[2]);
-    float* out = rev_grad + G.arena_off + R.offset + bk_x(tY) + bk_y(Bv, tZ);
-    int i0, n;
-    line_segment(P, G, R, tY, tZ, R.rev[0], i0, n);
-    for (int i = i0; i < i0 + n; i++) out[bk_z(Bv, i)] = 0.f;
+    float* row = rev_grad + G.arena_off + R.offset + bk_x(tY & ~3) + bk_y(Bv, tZ);
+    for (int i = lo + (threadIdx.x & 3); i <= hi; i += 4)
+        *reinterpret_cast<float4*>(row + bk_z(Bv, i)) = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
 // Adjoint of k_cone_lane followed by the transpose of the REV TERMA resample.
