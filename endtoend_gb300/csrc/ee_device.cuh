@@ -126,15 +126,21 @@ __device__ __forceinline__ int bk_x(int x) { return ((x >> 2) << 6) + (x & 3); }
 __device__ __forceinline__ int bk_y(const Brick& B, int y) { return (y >> 2) * B.sy + ((y & 3) << 2); }
 __device__ __forceinline__ int bk_z(const Brick& B, int z) { return (z >> 2) * B.sz + ((z & 3) << 4); }
 
-// A cone's REV arrays (dose, dose gradient) are bricked over (tY, tZ, i),
-// tY fastest: dimensions (rev[1], rev[2], rev[0]); ee_brick_vol(rev) floats.
+// A cone's REV arrays (dose, dose gradient, cone scratch) are bricked over
+// (i, tY, tZ), the sample index along the line fastest: dimensions (rev[0],
+// rev[1], rev[2]); ee_brick_vol(rev) cells.  Four consecutive samples of a
+// line are one 16-byte brick row, and the 8 x 4 lines of a warp cover two
+// whole bricks per quad of samples.
 __device__ __forceinline__ Brick rev_brick(int n0, int n1, int n2) {  // n0 = rev[0] (along the line)
     Brick B;
-    B.n0 = n1; B.n1 = n2; B.n2 = n0;
-    B.sy = 64 * ((n1 + 3) >> 2);
-    B.sz = B.sy * ((n2 + 3) >> 2);
+    B.n0 = n0; B.n1 = n1; B.n2 = n2;
+    B.sy = 64 * ((n0 + 3) >> 2);
+    B.sz = B.sy * ((n1 + 3) >> 2);
     return B;
 }
+// Offset of line (tY, tZ) in a bricked REV array: its sample i sits at
+// rev_line(B, tY, tZ) + bk_x(i).
+__device__ __forceinline__ int rev_line(const Brick& B, int tY, int tZ) { return bk_y(B, tY) + bk_z(B, tZ); }
 
 // tri_border on a bricked box: the same weights, products and order, so the
 // value is bit-identical to tri_border on the x-fastest box.

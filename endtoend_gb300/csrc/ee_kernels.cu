@@ -330,8 +330,8 @@ __device__ __forceinline__ void zero_outside_segment(float* out, const Brick& Bv
                                                      int first, int stride) {
     const int e0 = n > 0 ? min(z1 + 1, i0) : z1 + 1;  // [z0, e0) before the segment
     const int s1 = n > 0 ? max(z0, i0 + n) : z1 + 1;  // [s1, z1] after it
-    for (int i = z0 + first; i < e0; i += stride) out[bk_z(Bv, i)] = 0.f;
-    for (int i = s1 + first; i <= z1; i += stride) out[bk_z(Bv, i)] = 0.f;
+    for (int i = z0 + first; i < e0; i += stride) out[bk_x(i)] = 0.f;
+    for (int i = s1 + first; i <= z1; i += stride) out[bk_x(i)] = 0.f;
 }
 
 // REV resample of samples i0..i0+n-1 of one line into shared memory
@@ -562,9 +562,9 @@ __global__ void __launch_bounds__(CONE_WARPS * 32) k_cone(EeParams P, const EeBe
     float* rho = sm + (size_t)warp * 3 * maxL;
     float* T = rho + maxL;
     float* D = T + maxL;
-    // bricked REV arena (rev_brick)
+    // bricked REV arena (rev_brick): sample i at out + bk_x(i)
     const Brick Bv = rev_brick(R.rev[0], R.rev[1], R.rev[2]);
-    float* out = rev + G.arena_off + R.offset + bk_x(tY) + bk_y(Bv, tZ);
+    float* out = rev + G.arena_off + R.offset + rev_line(Bv, tY, tZ);
     int i0, n, z0, z1;
     line_segment(P, G, R, tY, tZ, L, i0, n);
     line_read_span(G, R, tY, tZ, L, z0, z1);
@@ -591,7 +591,7 @@ __global__ void __launch_bounds__(CONE_WARPS * 32) k_cone(EeParams P, const EeBe
         }
         __syncwarp();
     }
-    for (int k = lane; k < n; k += 32) out[bk_z(Bv, i0 + k)] = D[k];
+    for (int k = lane; k < n; k += 32) out[bk_x(i0 + k)] = D[k];
 }
 
 // ------------------------------------------- cone: one lane per line ----
@@ -633,8 +633,6 @@ __device__ __forceinline__ float sample_rho(const EeParams& P, const EeBeamSpec&
                        g.z - (float)S.t0[2]);
     return tex3D<float>(P.dens_tex, g.x + 0.5f, g.y + 0.5f, g.z + 0.5f);
 }
-
-constexpr int CONE_U = 4;
 
 // Sample indices [s0, s1] of a REV line whose TERMA trilinear corners can lie
 // inside the beam's field frustum.  A voxel has a beamlet only where its
@@ -713,9 +711,9 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_lane(EeParams P, const EeBe
     int tY, tZ;
     if (!lane_line(R, blockIdx.x * LANE_BLOCK + threadIdx.x, tY, tZ)) return;
     const int L = R.rev[0];
-    // bricked REV arena: this line's sample i sits at out + bk_z(i)
+    // bricked REV arena (rev_brick): this line's sample i sits at out + bk_x(i)
     const Brick Bv = rev_brick(R.rev[0], R.rev[1], R.rev[2]);
-    float* out = rev + G.arena_off + R.offset + bk_x(tY) + bk_y(Bv, tZ);
+    float* out = rev + G.arena_off + R.offset + rev_line(Bv, tY, tZ);
     int i0, n, z0, z1;
     line_segment(P, G, R, tY, tZ, L, i0, n);
     line_read_span(G, R, tY, tZ, L, z0, z1);
@@ -727,43 +725,53 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_lane(EeParams P, const EeBe
     int f0, f1;  // samples that can see TERMA
     field_span(P, S, F, i0, n, f0, f1);
     // (rho, T) of each sample, kept from the forward pass for the reverse
-    // one, in this cone's slot of the scratch bricked like the REV arena:
-    // sample i of the line at smp[bk_z(i)], so a warp's 8 x 4 lines write two
-    // whole 128-byte lines per sample
-    float2* smp = samples + G.arena_off + R.offset + bk_x(tY) + bk_y(Bv, tZ);
+    // one, in this cone's slot of the scratch bricked like the REV arena.
+    // Both passes walk whole quads of samples (4q .. 4q+3): a lane reads and
+    // writes a quad's dose and (rho, T) with 16-byte accesses, and the warp's
+    // 8 x 4 lines cover two whole bricks.  Samples of an end quad outside the
+    // segment get dose 0 (they are inside the read span or never read) and
+    // scratch (-1, 0).
+    float2* smp = samples + G.arena_off + R.offset + rev_line(Bv, tY, tZ);
     const EeRayConst& RC = P.rays[ray];
     const float delr = P.lng;
-    // samples are gathered CONE_U at a time before the recurrence consumes
-    // them, so each lane keeps several independent loads in flight
     const int iend = i0 + n;
     {   // forward direction: contributions from k < i, kernel row P
         const float* prm = P.expp + 4 * RC.row_fwd;
         const float c1 = prm[0] / prm[1], c2 = prm[2] / prm[3];
         const float e1 = -0.5f * prm[1] * delr, e2 = -0.5f * prm[3] * delr;
         float Y1 = 0.f, Y2 = 0.f, tm = 0.f, hm1 = 1.f, hm2 = 1.f;
-        for (int ib = i0; ib < iend; ib += CONE_U) {
-            float rr[CONE_U], tt[CONE_U];
+        for (int ib = i0 & ~3; ib < iend; ib += 4) {
+            // the quad's samples gathered before the recurrence consumes
+            // them, so each lane keeps several independent loads in flight
+            float rr[4], tt[4];
 #pragma unroll
-            for (int j = 0; j < CONE_U; j++) {
+            for (int j = 0; j < 4; j++) {
+                const int i = ib + j;
                 rr[j] = -1.f;
                 tt[j] = 0.f;
-                if (ib + j < iend)
-                    rr[j] = sample_rho(P, S, G, F, ib + j, (ib + j >= f0 && ib + j <= f1) ? tb : nullptr, tt[j]);
+                if (i >= i0 && i < iend) rr[j] = sample_rho(P, S, G, F, i, (i >= f0 && i <= f1) ? tb : nullptr, tt[j]);
             }
+            float dq[4];
 #pragma unroll
-            for (int j = 0; j < CONE_U; j++) {
+            for (int j = 0; j < 4; j++) {
                 const int i = ib + j;
-                if (i >= iend) break;
+                dq[j] = 0.f;
+                if (i < i0 || i >= iend) continue;
                 const float r = rr[j];
                 const bool v = r >= 0.f;
                 const float h1 = v ? __expf(e1 * r) : 1.f, h2 = v ? __expf(e2 * r) : 1.f;
                 const float t = v ? tt[j] : 0.f;
-                smp[bk_z(Bv, i)] = make_float2(r, t);
-                out[bk_z(Bv, i)] = v ? c1 * (Y1 + tm * (1.f - hm1)) + c2 * (Y2 + tm * (1.f - hm2)) : 0.f;
+                rr[j] = r;
+                tt[j] = t;
+                dq[j] = v ? c1 * (Y1 + tm * (1.f - hm1)) + c2 * (Y2 + tm * (1.f - hm2)) : 0.f;
                 Y1 = fmaf(h1 * h1, Y1, tm * h1 * (1.f - hm1 * h1));
                 Y2 = fmaf(h2 * h2, Y2, tm * h2 * (1.f - hm2 * h2));
                 tm = t; hm1 = h1; hm2 = h2;
             }
+            float4* sq = reinterpret_cast<float4*>(smp + bk_x(ib));
+            sq[0] = make_float4(rr[0], tt[0], rr[1], tt[1]);
+            sq[1] = make_float4(rr[2], tt[2], rr[3], tt[3]);
+            *reinterpret_cast<float4*>(out + bk_x(ib)) = make_float4(dq[0], dq[1], dq[2], dq[3]);
         }
     }
     {   // reverse direction: contributions from k > i, kernel row ntheta-1-P
@@ -772,32 +780,29 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_lane(EeParams P, const EeBe
         const float e1 = -0.5f * prm[1] * delr, e2 = -0.5f * prm[3] * delr;
         const float inv_nphi = 1.f / (float)P.nphi;
         float Y1 = 0.f, Y2 = 0.f, tm = 0.f, hm1 = 1.f, hm2 = 1.f;
-        for (int ib = iend - 1; ib >= i0; ib -= CONE_U) {
-            float2 rt[CONE_U];
-            float ov[CONE_U];
+        for (int ib = (iend - 1) & ~3; ib >= (i0 & ~3); ib -= 4) {
+            const float4* sq = reinterpret_cast<const float4*>(smp + bk_x(ib));
+            const float4 s01 = sq[0], s23 = sq[1];
+            const float4 o4 = *reinterpret_cast<const float4*>(out + bk_x(ib));
+            const float rs[4] = {s01.x, s01.z, s23.x, s23.z}, ts[4] = {s01.y, s01.w, s23.y, s23.w};
+            const float ov[4] = {o4.x, o4.y, o4.z, o4.w};
+            float dq[4];
 #pragma unroll
-            for (int j = 0; j < CONE_U; j++) {
-                rt[j] = make_float2(-1.f, 0.f);
-                ov[j] = 0.f;
-                if (ib - j >= i0) {
-                    rt[j] = smp[bk_z(Bv, ib - j)];
-                    ov[j] = out[bk_z(Bv, ib - j)];
-                }
-            }
-#pragma unroll
-            for (int j = 0; j < CONE_U; j++) {
-                const int i = ib - j;
-                if (i < i0) break;
-                const float r = rt[j].x;
+            for (int j = 3; j >= 0; j--) {
+                const int i = ib + j;
+                dq[j] = 0.f;
+                if (i < i0 || i >= iend) continue;
+                const float r = rs[j];
                 const bool v = r >= 0.f;
-                const float t = v ? rt[j].y : 0.f;
+                const float t = v ? ts[j] : 0.f;
                 const float h1 = v ? __expf(e1 * r) : 1.f, h2 = v ? __expf(e2 * r) : 1.f;
                 const float d = c1 * (Y1 + tm * (1.f - hm1)) + c2 * (Y2 + tm * (1.f - hm2));
-                out[bk_z(Bv, i)] = v ? (ov[j] + d) * inv_nphi : 0.f;
+                dq[j] = v ? (ov[j] + d) * inv_nphi : 0.f;
                 Y1 = fmaf(h1 * h1, Y1, tm * h1 * (1.f - hm1 * h1));
                 Y2 = fmaf(h2 * h2, Y2, tm * h2 * (1.f - hm2 * h2));
                 tm = t; hm1 = h1; hm2 = h2;
             }
+            *reinterpret_cast<float4*>(out + bk_x(ib)) = make_float4(dq[0], dq[1], dq[2], dq[3]);
         }
     }
 }
@@ -805,11 +810,9 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_lane(EeParams P, const EeBe
 // Zero the segment (line_segment) of every line of a chunk's REV gradient
 // arena before k_gather_T adds into it: the samples the adjoint cone reads.
 // k_gather_T also adds into the rest of the line's read span; those cells are
-// never read, so they need no zero.  The four lanes of a brick row (a tY quad
-// at one tZ) zero the union of their lines' segments with 16-byte stores,
-// lane q of the four taking samples i = q (mod 4): a warp's store covers two
-// whole bricks.  Cells of a line outside its own segment that this zeroes are
-// never read either.
+// never read, so they need no zero.  A lane zeroes the quads of samples that
+// hold its segment with 16-byte stores (the end quads' other samples are
+// never read either); a warp's store covers two whole bricks.
 template <int LANE_BLOCK>
 __global__ void __launch_bounds__(LANE_BLOCK) k_rev_zero(EeParams P, const EeBeamGeom* __restrict__ geoms,
                                                          float* __restrict__ rev_grad) {
@@ -818,26 +821,13 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_rev_zero(EeParams P, const EeBea
     if (G.status != 0) return;
     const EeRayGeom& R = G.ray[ray];
     int tY, tZ;
-    const bool ok = lane_line(R, blockIdx.x * LANE_BLOCK + threadIdx.x, tY, tZ);
-    int lo = 0x7fffffff, hi = -1;
-    if (ok) {
-        int i0, n;
-        line_segment(P, G, R, tY, tZ, R.rev[0], i0, n);
-        if (n > 0) {
-            lo = i0;
-            hi = i0 + n - 1;
-        }
-    }
-    // lanes 4k .. 4k+3 own one brick row (lane_line: tY = lane % 8, tZ = lane / 8)
-    lo = min(lo, __shfl_xor_sync(FULL, lo, 1));
-    hi = max(hi, __shfl_xor_sync(FULL, hi, 1));
-    lo = min(lo, __shfl_xor_sync(FULL, lo, 2));
-    hi = max(hi, __shfl_xor_sync(FULL, hi, 2));
-    if (lo > hi) return;
+    if (!lane_line(R, blockIdx.x * LANE_BLOCK + threadIdx.x, tY, tZ)) return;
+    int i0, n;
+    line_segment(P, G, R, tY, tZ, R.rev[0], i0, n);
     const Brick Bv = rev_brick(R.rev[0], R.rev[1], R.rev[2]);
-    float* row = rev_grad + G.arena_off + R.offset + bk_x(tY & ~3) + bk_y(Bv, tZ);
-    for (int i = lo + (threadIdx.x & 3); i <= hi; i += 4)
-        *reinterpret_cast<float4*>(row + bk_z(Bv, i)) = make_float4(0.f, 0.f, 0.f, 0.f);
+    float* row = rev_grad + G.arena_off + R.offset + rev_line(Bv, tY, tZ);
+    for (int ib = i0 & ~3; ib < i0 + n; ib += 4)
+        *reinterpret_cast<float4*>(row + bk_x(ib)) = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
 // Adjoint of k_cone_lane followed by the transpose of the REV TERMA resample.
@@ -864,15 +854,19 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_T_lane(EeParams P, const Ee
     const LineFrame F = line_frame(R, tY, tZ);
     int f0, f1;  // samples whose TERMA corners can lie in the field (field_span)
     field_span(P, S, F, i0, n, f0, f1);
-    // scratch bricked like the REV arena (k_cone_lane): sample i at sA[bk_z(i)]
-    const Brick Bv = rev_brick(R.rev[0], R.rev[1], R.rev[2]);  // bricked REV gradient
-    const float* gin = rev_grad + G.arena_off + R.offset + bk_x(tY) + bk_y(Bv, tZ);
-    float2* sA = scratch + G.arena_off + R.offset + bk_x(tY) + bk_y(Bv, tZ);  // (pass-A part of Tbar[i], rho[i])
+    // REV gradient and scratch bricked like the REV arena (rev_brick): sample
+    // i at gin + bk_x(i) and sA + bk_x(i).  Both passes walk whole quads of
+    // samples with 16-byte loads and stores, as k_cone_lane does.
+    const Brick Bv = rev_brick(R.rev[0], R.rev[1], R.rev[2]);
+    const float* gin = rev_grad + G.arena_off + R.offset + rev_line(Bv, tY, tZ);
+    float2* sA = scratch + G.arena_off + R.offset + rev_line(Bv, tY, tZ);  // (pass-A part of Tbar[i], rho[i])
     const EeRayConst& RC = P.rays[ray];
     const float delr = P.lng, inv_nphi = 1.f / (float)P.nphi;
     const int i1 = i0 + n - 1;
     float dummy;
-    {   // pass A: transpose of the forward recurrence, walking down
+    {   // pass A: transpose of the forward recurrence, walking down; step i
+        // writes the entry of sample i - 1, so a quad's top entry comes from
+        // the quad above (carry) and the top sample's entry is (0, rho[i1])
         const float* prm = P.expp + 4 * RC.row_fwd;
         const float c1 = prm[0] / prm[1], c2 = prm[2] / prm[3];
         const float e1 = -0.5f * prm[1] * delr, e2 = -0.5f * prm[3] * delr;
@@ -880,34 +874,42 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_T_lane(EeParams P, const Ee
         bool v = r >= 0.f;
         float h1 = v ? __expf(e1 * r) : 1.f, h2 = v ? __expf(e2 * r) : 1.f;
         float Z1 = 0.f, Z2 = 0.f;
-        sA[bk_z(Bv, i1)] = make_float2(0.f, r);
-        // inputs gathered CONE_U samples ahead of the recurrence
-        for (int ib = i1; ib >= i0; ib -= CONE_U) {
-            float gl[CONE_U], rl[CONE_U];
+        float2 carry = make_float2(0.f, r);
+        for (int qb = i1 & ~3; qb >= (i0 & ~3); qb -= 4) {
+            const float4 g4 = *reinterpret_cast<const float4*>(gin + bk_x(qb));
+            const float gl[4] = {g4.x, g4.y, g4.z, g4.w};
+            float rl[4];
 #pragma unroll
-            for (int j = 0; j < CONE_U; j++) {
-                const int i = ib - j;
-                gl[j] = 0.f;
+            for (int j = 0; j < 4; j++) {
+                const int i = qb + j;
                 rl[j] = -1.f;
-                if (i >= i0) gl[j] = gin[bk_z(Bv, i)];
-                if (i > i0) rl[j] = sample_rho(P, S, G, F, i - 1, nullptr, dummy);
+                if (i > i0 && i <= i1) rl[j] = sample_rho(P, S, G, F, i - 1, nullptr, dummy);
             }
+            float2 o[4];
+            const int cs = min(3, i1 - qb);  // slot of the carried entry
 #pragma unroll
-            for (int j = 0; j < CONE_U; j++) {
-                const int i = ib - j;
-                if (i <= i0) break;
+            for (int j = 0; j < 4; j++) o[j] = j == cs ? carry : make_float2(0.f, -1.f);
+#pragma unroll
+            for (int j = 3; j >= 0; j--) {
+                const int i = qb + j;
+                if (i > i1 || i <= i0) continue;
                 const float gi = v ? gl[j] * inv_nphi : 0.f;
                 const float rm = rl[j];
                 const bool vm = rm >= 0.f;
                 const float hm1 = vm ? __expf(e1 * rm) : 1.f, hm2 = vm ? __expf(e2 * rm) : 1.f;
-                sA[bk_z(Bv, i - 1)] = make_float2(vm ? c1 * gi * (1.f - hm1) + Z1 * h1 * (1.f - hm1 * h1) +
-                                                        c2 * gi * (1.f - hm2) + Z2 * h2 * (1.f - hm2 * h2)
-                                                  : 0.f,
-                                               rm);
+                const float2 e = make_float2(vm ? c1 * gi * (1.f - hm1) + Z1 * h1 * (1.f - hm1 * h1) +
+                                                      c2 * gi * (1.f - hm2) + Z2 * h2 * (1.f - hm2 * h2)
+                                                : 0.f,
+                                             rm);
+                if (j > 0) o[j - 1] = e;
+                else carry = e;
                 Z1 = fmaf(h1 * h1, Z1, c1 * gi);
                 Z2 = fmaf(h2 * h2, Z2, c2 * gi);
                 v = vm; h1 = hm1; h2 = hm2;
             }
+            float4* sq = reinterpret_cast<float4*>(sA + bk_x(qb));
+            sq[0] = make_float4(o[0].x, o[0].y, o[1].x, o[1].y);
+            sq[1] = make_float4(o[2].x, o[2].y, o[3].x, o[3].y);
         }
     }
     {   // pass B: transpose of the reverse recurrence, walking up; scatter
@@ -915,36 +917,33 @@ __global__ void __launch_bounds__(LANE_BLOCK) k_cone_T_lane(EeParams P, const Ee
         const float c1 = prm[0] / prm[1], c2 = prm[2] / prm[3];
         const float e1 = -0.5f * prm[1] * delr, e2 = -0.5f * prm[3] * delr;
         float* tg = terma_grad + S.t_off;
-        float2 a = sA[bk_z(Bv, i0)];
-        float r = a.y;
+        const float r = sA[bk_x(i0)].y;
         bool v = r >= 0.f;
         float h1 = v ? __expf(e1 * r) : 1.f, h2 = v ? __expf(e2 * r) : 1.f;
         float Z1 = 0.f, Z2 = 0.f, cprev = 0.f;
-        for (int ib = i0; ib <= i1; ib += CONE_U) {
-            float gl[CONE_U];
-            float2 al[CONE_U];
+        for (int qb = i0 & ~3; qb <= i1; qb += 4) {
+            const float4* sq = reinterpret_cast<const float4*>(sA + bk_x(qb));
+            const float4 s01 = sq[0], s23 = sq[1];
+            // the first entry of the next quad, for the step at qb + 3
+            const float4 nx = qb + 4 <= i1 ? *reinterpret_cast<const float4*>(sA + bk_x(qb + 4))
+                                            : make_float4(0.f, -1.f, 0.f, -1.f);
+            const float4 g4 = *reinterpret_cast<const float4*>(gin + bk_x(qb));
+            const float2 al[5] = {make_float2(s01.x, s01.y), make_float2(s01.z, s01.w), make_float2(s23.x, s23.y),
+                                  make_float2(s23.z, s23.w), make_float2(nx.x, nx.y)};
+            const float gl[4] = {g4.x, g4.y, g4.z, g4.w};
 #pragma unroll
-            for (int j = 0; j < CONE_U; j++) {
-                const int i = ib + j;
-                gl[j] = 0.f;
-                al[j] = make_float2(0.f, -1.f);
-                if (i <= i1) gl[j] = gin[bk_z(Bv, i)];
-                if (i < i1) al[j] = sA[bk_z(Bv, i + 1)];
-            }
-#pragma unroll
-            for (int j = 0; j < CONE_U; j++) {
-                const int i = ib + j;
-                if (i > i1) break;
+            for (int j = 0; j < 4; j++) {
+                const int i = qb + j;
+                if (i < i0 || i > i1) continue;
                 const float gi = v ? gl[j] * inv_nphi : 0.f;
-                const float tot = a.x + cprev;
+                const float tot = al[j].x + cprev;
                 if (v && tot != 0.f && i >= f0 && i <= f1) {
                     f3 gp = F.gl + F.gx * (float)i;
                     tri_brick_scatter(tg, brick_of(S.tn), gp.x - (float)S.t0[0], gp.y - (float)S.t0[1],
                                        gp.z - (float)S.t0[2], tot);
                 }
                 if (i < i1) {
-                    a = al[j];
-                    const float rm = a.y;
+                    const float rm = al[j + 1].y;
                     const bool vm = rm >= 0.f;
                     const float hm1 = vm ? __expf(e1 * rm) : 1.f, hm2 = vm ? __expf(e2 * rm) : 1.f;
                     cprev = vm ? c1 * gi * (1.f - hm1) + Z1 * h1 * (1.f - hm1 * h1) + c2 * gi * (1.f - hm2) +
@@ -995,11 +994,11 @@ __global__ void __launch_bounds__(CONE_WARPS * 32) k_cone_T(EeParams P, const Ee
     if (n == 0) return;
     gather_line(P, S, G, R, nullptr, tY, tZ, i0, n, lane, rho, nullptr);
     const Brick Bv = rev_brick(R.rev[0], R.rev[1], R.rev[2]);  // bricked REV gradient
-    const float* gin = rev_grad + G.arena_off + R.offset + bk_x(tY) + bk_y(Bv, tZ);
+    const float* gin = rev_grad + G.arena_off + R.offset + rev_line(Bv, tY, tZ);
     const float inv_nphi = 1.f / (float)P.nphi;
     __syncwarp();
     for (int k = lane; k < n; k += 32) {
-        g[k] = rho[k] >= 0.f ? gin[bk_z(Bv, i0 + k)] * inv_nphi : 0.f;
+        g[k] = rho[k] >= 0.f ? gin[bk_x(i0 + k)] * inv_nphi : 0.f;
         Tb[k] = 0.f;
     }
     __syncwarp();
@@ -1128,8 +1127,8 @@ __global__ void __launch_bounds__(ROW_WARPS * 32, 6) k_gather(EeParams P, const 
                 // q.y along the line (rev[0]), q.z -> rev[1], q.x -> rev[2]
                 if (qy >= (float)n0 || qz >= (float)n1 || qx >= (float)n2 || qx < 0.f || qy < 0.f || qz < 0.f)
                     continue;
-                // bricked REV arrays over (tY, tZ, i): x = tY (q.z), y = tZ (q.x), z = i (q.y)
-                acc += tri_brick(base + __float_as_int(rv.w), rev_brick(n0, n1, n2), qz, qx, qy);
+                // bricked REV arrays over (i, tY, tZ): x = i (q.y), y = tY (q.z), z = tZ (q.x)
+                acc += tri_brick(base + __float_as_int(rv.w), rev_brick(n0, n1, n2), qy, qz, qx);
             }
         }
         if (mode == 2) out[rbase + x] = acc;
@@ -1148,7 +1147,7 @@ __global__ void __launch_bounds__(ROW_WARPS * 32, 6) k_gather(EeParams P, const 
 // barrier per cone (between its scatter and its flush) suffices.
 constexpr int GT_TX = 8, GT_TY = 8, GT_TZ = 4;
 // floats per footprint buffer: an 8x8x4 tile spans at most |(7,7,3)| + 2 = 13
-// REV cells per axis when the REV spacing equals the voxel size (16 in tY
+// REV cells per axis when the REV spacing equals the voxel size (16 along i
 // after the quad alignment), 2704 < 4096; larger footprints (finer REV
 // spacing) take the direct-scatter path
 constexpr int GT_BUF = 4096;
@@ -1159,9 +1158,10 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
                                                                    const float* __restrict__ dose_grad,
                                                                    float* __restrict__ rev_grad) {
     extern __shared__ float acc_all[];
-    // per cone: {l0, n0, l1, n1}, {l2, n2, s1, rev0}, {rev1, rev2, offset lo, offset hi}
-    // (box origin and extent per REV axis, the box's tY row stride, the REV
-    // sizes and the cone's arena offset), read with three vector loads
+    // per cone: {l0, n0, l1, n1}, {l2, n2, s0, rev0}, {rev1, rev2, offset lo, offset hi}
+    // (box origin and extent along i, tY and tZ, the box's row stride along
+    // i, the REV sizes and the cone's arena offset), read with three vector
+    // loads
     __shared__ int4 s_p[EE_MAX_RAYS][3];
     __shared__ float4 s_A[EE_MAX_RAYS][3];
     const int b = blockIdx.z;
@@ -1207,20 +1207,20 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
         const int h = min(dim - 1, (int)floorf(hi + 1e-3f) + 1);
         int w = h - l + 1;
         int* sp = reinterpret_cast<int*>(s_p[r]);
-        if (a == 2) {
-            int s1 = 0;
+        if (a == 1) {
+            int s0 = 0;
             if (w > 0) {
-                // tY range on whole quads: a box row of 4 tY cells is one
+                // i range on whole quads: a box row of 4 samples is one
                 // 16-byte brick row of the REV gradient (flushed as one
-                // vector reduction); the cells past rev[1] are brick padding
+                // vector reduction); the cells past rev[0] are brick padding
                 w = ((h | 3) + 1) - (l & ~3);
                 l &= ~3;
-                // row stride 4 (mod 8) floats: the rows of x-adjacent voxels
+                // row stride 4 (mod 8) floats: the rows of adjacent voxels
                 // spread over the shared banks; the extra quad of a row is
-                // never scattered to (k1 < w), stays zero and is not sent
-                s1 = (w & 7) == 0 ? w + 4 : w;
+                // never scattered to (k0 < w), stays zero and is not sent
+                s0 = (w & 7) == 0 ? w + 4 : w;
             }
-            sp[6] = s1;
+            sp[6] = s0;
         }
         const int slot = a == 1 ? 0 : (a == 2 ? 2 : 4);
         sp[slot] = l;
@@ -1244,12 +1244,13 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
         const int l0 = p0.x, n0 = p0.y, l1 = p0.z, n1 = p0.w, l2 = p1.x, n2 = p1.y;
         const int rv0 = p1.w, rv1 = p2.x, rv2 = p2.y;
         const bool empty = n0 <= 0 || n1 <= 0 || n2 <= 0;
-        const int s1 = empty ? 0 : p1.z;  // row stride of the box (>= n1, a multiple of 4)
-        // rows per slab: odd, so that the slab stride s1 * n0p is 4 x odd
-        // (mod 32) and the slabs of y-adjacent voxels spread over the banks
-        // too; the padding rows (k0 >= n0) are never scattered to
-        const int n0p = n0 | 1;
-        const int nbox = empty ? 0 : n0p * s1 * n2;
+        // box cell (k0, k1, k2) over (i, tY, tZ) at k0 + s0 * (k1 + n1p * k2)
+        const int s0 = empty ? 0 : p1.z;  // row stride of the box (>= n0, a multiple of 4)
+        // rows per slab: odd, so that the slab stride s0 * n1p is 4 x odd
+        // (mod 32) and the slabs of adjacent voxels spread over the banks
+        // too; the padding rows (k1 >= n1) are never scattered to
+        const int n1p = n1 | 1;
+        const int nbox = empty ? 0 : n1p * s0 * n2;
         if (nbox > 0 && nbox <= GT_BUF) {
             // buffers alternate over the shared-memory cones: the last flush
             // of this buffer (two such cones back) was cleared by every
@@ -1268,10 +1269,10 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
                     const float a0 = q.y - f0, a1 = q.z - f1, a2 = q.x - f2;
                     // Corners outside the box get weight 0 and a clamped
                     // index inside it, so the eight adds need no tests.  The
-                    // box ends at the last REV cell in i and tZ, so that is
-                    // the array edge there (tri_brick's border); in tY it can
-                    // reach the brick padding past rev[1], cells no line
-                    // owns, which the flush sends but nothing reads.
+                    // box ends at the last REV cell in tY and tZ, so that is
+                    // the array edge there (tri_brick's border); in i it can
+                    // reach the brick padding past rev[0], cells outside
+                    // every segment, which the flush sends but nothing reads.
                     const float w0[2] = {j0 >= 0 && j0 < n0 ? 1.f - a0 : 0.f, j0 + 1 >= 0 && j0 + 1 < n0 ? a0 : 0.f};
                     const float w1[2] = {j1 >= 0 && j1 < n1 ? 1.f - a1 : 0.f, j1 + 1 >= 0 && j1 + 1 < n1 ? a1 : 0.f};
                     const float w2[2] = {j2 >= 0 && j2 < n2 ? 1.f - a2 : 0.f, j2 + 1 >= 0 && j2 + 1 < n2 ? a2 : 0.f};
@@ -1286,7 +1287,7 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
                             const float t1 = w1[d1] * t2;
 #pragma unroll
                             for (int d0 = 0; d0 < 2; d0++)
-                                atomicAdd(acc + c1[d1] + s1 * (c0[d0] + n0p * c2[d2]), w0[d0] * t1);
+                                atomicAdd(acc + c0[d0] + s0 * (c1[d1] + n1p * c2[d2]), w0[d0] * t1);
                         }
                     }
                 }
@@ -1294,26 +1295,26 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
             __syncthreads();
             float* rb = base + (long long)(((unsigned long long)(unsigned)p2.w << 32) | (unsigned)p2.z);
             const Brick Bv = rev_brick(rv0, rv1, rv2);
-            // one box quad (4 tY cells) per iteration, quad index = kq + nq1 *
-            // (k0 + n0p * k2); (k + 0.5) / n is at least 1/(2n) away from an
+            // one box quad (4 samples) per iteration, quad index = kq + nq0 *
+            // (k1 + n1p * k2); (k + 0.5) / n is at least 1/(2n) away from an
             // integer, far above the FP32 error of (k + 0.5) * rcp(n) for
             // these sizes, so the floored quotients are exact.  A non-zero quad is one 16-byte vector
             // reduction into the bricked REV gradient (brick rows are 16-byte
             // aligned: arena and cone offsets are multiples of 64 floats),
             // and is cleared for the buffer's next cone.
-            float4* acc4 = reinterpret_cast<float4*>(acc);  // s1 is a multiple of 4
+            float4* acc4 = reinterpret_cast<float4*>(acc);  // s0 is a multiple of 4
             const int nquad = nbox >> 2;
-            const int nq1 = s1 >> 2;
-            const float invq = __frcp_rn((float)nq1), inv0 = __frcp_rn((float)n0p);
+            const int nq0 = s0 >> 2;
+            const float invq = __frcp_rn((float)nq0), inv1 = __frcp_rn((float)n1p);
             for (int k = t; k < nquad; k += blockDim.x) {
                 const float4 v = acc4[k];
                 if (v.x != 0.f || v.y != 0.f || v.z != 0.f || v.w != 0.f) {
                     acc4[k] = make_float4(0.f, 0.f, 0.f, 0.f);
                     const int q1 = __float2int_rd(((float)k + 0.5f) * invq);
-                    const int kq = k - q1 * nq1;
-                    const int k2 = __float2int_rd(((float)q1 + 0.5f) * inv0);
-                    const int k0 = q1 - k2 * n0p;
-                    red_v4(rb + bk_x(l1 + 4 * kq) + bk_y(Bv, l2 + k2) + bk_z(Bv, l0 + k0), v.x, v.y, v.z, v.w);
+                    const int kq = k - q1 * nq0;
+                    const int k2 = __float2int_rd(((float)q1 + 0.5f) * inv1);
+                    const int k1 = q1 - k2 * n1p;
+                    red_v4(rb + bk_x(l0 + 4 * kq) + bk_y(Bv, l1 + k1) + bk_z(Bv, l2 + k2), v.x, v.y, v.z, v.w);
                 }
             }
         } else if (nbox > GT_BUF && gd != 0.f) {
@@ -1326,7 +1327,7 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
                             fmaf(a2.x, dx, fmaf(a2.y, dy, fmaf(a2.z, dz, a2.w))));
             if (!(q.y >= (float)R.rev[0] || q.z >= (float)R.rev[1] || q.x >= (float)R.rev[2] || q.x < 0.f ||
                   q.y < 0.f || q.z < 0.f))
-                tri_brick_scatter(base + R.offset, rev_brick(R.rev[0], R.rev[1], R.rev[2]), q.z, q.x, q.y, gd);
+                tri_brick_scatter(base + R.offset, rev_brick(R.rev[0], R.rev[1], R.rev[2]), q.y, q.z, q.x, gd);
         }
     }
 }
