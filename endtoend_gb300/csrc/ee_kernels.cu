@@ -1158,11 +1158,12 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
                                                                    const float* __restrict__ dose_grad,
                                                                    float* __restrict__ rev_grad) {
     extern __shared__ float acc_all[];
-    // per cone: {l0, n0, l1, n1}, {l2, n2, s0, rev0}, {rev1, rev2, offset lo, offset hi}
-    // (box origin and extent along i, tY and tZ, the box's row stride along
-    // i, the REV sizes and the cone's arena offset), read with three vector
-    // loads
-    __shared__ int4 s_p[EE_MAX_RAYS][3];
+    // per cone: {l0 | n0 << 16, l1 | n1 << 16, l2 | n2 << 16, s0} (box origin
+    // and extent along i, tY and tZ, the box's row stride along i; all below
+    // 2^16), read with one vector load before the scatter, and {sy, sz,
+    // offset lo, offset hi} (the REV gradient's brick strides and the cone's
+    // arena offset), read with one before the flush
+    __shared__ int4 s_p[EE_MAX_RAYS][2];
     __shared__ float4 s_A[EE_MAX_RAYS][3];
     const int b = blockIdx.z;
     const EeBeamGeom& G = geoms[b];
@@ -1220,15 +1221,15 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
                 // never scattered to (k0 < w), stays zero and is not sent
                 s0 = (w & 7) == 0 ? w + 4 : w;
             }
-            sp[6] = s0;
+            sp[3] = s0;
         }
-        const int slot = a == 1 ? 0 : (a == 2 ? 2 : 4);
-        sp[slot] = l;
-        sp[slot + 1] = w;
-        sp[7 + a] = R.rev[a];
+        sp[a == 1 ? 0 : (a == 2 ? 1 : 2)] = l | (max(w, 0) << 16);
         if (a == 0) {
-            sp[10] = (int)(unsigned)(R.offset & 0xffffffffll);
-            sp[11] = (int)(R.offset >> 32);
+            const Brick Bv = rev_brick(R.rev[0], R.rev[1], R.rev[2]);
+            sp[4] = Bv.sy;
+            sp[5] = Bv.sz;
+            sp[6] = (int)(unsigned)(R.offset & 0xffffffffll);
+            sp[7] = (int)(R.offset >> 32);
         }
         // this cone's map for the voxels: the row [A | -q0] of REV axis a
         // (the forward gather forms q in the same order)
@@ -1240,12 +1241,12 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
     float* base = rev_grad + G.arena_off;
     int parity = 0;  // buffer of the next shared-memory cone
     for (int r = 0; r < P.nrays; r++) {
-        const int4 p0 = s_p[r][0], p1 = s_p[r][1], p2 = s_p[r][2];
-        const int l0 = p0.x, n0 = p0.y, l1 = p0.z, n1 = p0.w, l2 = p1.x, n2 = p1.y;
-        const int rv0 = p1.w, rv1 = p2.x, rv2 = p2.y;
+        const int4 p0 = s_p[r][0];
+        const int l0 = p0.x & 0xffff, n0 = p0.x >> 16, l1 = p0.y & 0xffff, n1 = p0.y >> 16, l2 = p0.z & 0xffff,
+                  n2 = p0.z >> 16;
         const bool empty = n0 <= 0 || n1 <= 0 || n2 <= 0;
         // box cell (k0, k1, k2) over (i, tY, tZ) at k0 + s0 * (k1 + n1p * k2)
-        const int s0 = empty ? 0 : p1.z;  // row stride of the box (>= n0, a multiple of 4)
+        const int s0 = empty ? 0 : p0.w;  // row stride of the box (>= n0, a multiple of 4)
         // rows per slab: odd, so that the slab stride s0 * n1p is 4 x odd
         // (mod 32) and the slabs of adjacent voxels spread over the banks
         // too; the padding rows (k1 >= n1) are never scattered to
@@ -1262,8 +1263,10 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
                 const f3 q = mk(fmaf(a0.x, dx, fmaf(a0.y, dy, fmaf(a0.z, dz, a0.w))),
                                 fmaf(a1.x, dx, fmaf(a1.y, dy, fmaf(a1.z, dz, a1.w))),
                                 fmaf(a2.x, dx, fmaf(a2.y, dy, fmaf(a2.z, dz, a2.w))));
-                if (!(q.y >= (float)rv0 || q.z >= (float)rv1 || q.x >= (float)rv2 || q.x < 0.f || q.y < 0.f ||
-                      q.z < 0.f)) {
+                // the forward gather skips a cone where q is outside [0, rev):
+                // below 0 here; above, every corner lies past the box's end
+                // in tY and tZ (weight 0) or in the brick padding past rev[0]
+                if (!(q.x < 0.f || q.y < 0.f || q.z < 0.f)) {
                     const float f0 = floorf(q.y), f1 = floorf(q.z), f2 = floorf(q.x);
                     const int j0 = (int)f0 - l0, j1 = (int)f1 - l1, j2 = (int)f2 - l2;
                     const float a0 = q.y - f0, a1 = q.z - f1, a2 = q.x - f2;
@@ -1293,8 +1296,11 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
                 }
             }
             __syncthreads();
-            float* rb = base + (long long)(((unsigned long long)(unsigned)p2.w << 32) | (unsigned)p2.z);
-            const Brick Bv = rev_brick(rv0, rv1, rv2);
+            const int4 p1 = s_p[r][1];
+            float* rb = base + (long long)(((unsigned long long)(unsigned)p1.w << 32) | (unsigned)p1.z);
+            Brick Bv;  // strides only (bk_y, bk_z)
+            Bv.sy = p1.x;
+            Bv.sz = p1.y;
             // one box quad (4 samples) per iteration, quad index = kq + nq0 *
             // (k1 + n1p * k2); (k + 0.5) / n is at least 1/(2n) away from an
             // integer, far above the FP32 error of (k + 0.5) * rcp(n) for
