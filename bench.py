@@ -384,7 +384,7 @@ def run_reference(args, ws, rank):
 # capture of all six chain kernels on eight beams of this workload (dram__bytes
 # of one call's launches / sum of V_beam = 12.37 M); roofline.traffic scales
 # the dominant stage's figure to the profiled step.
-DRAM_BYTES_PER_VBEAM = {"terma": 1.0, "cone": 251.8, "gather": 52.0, "gather_T": 84.6, "cone_T": 196.0,
+DRAM_BYTES_PER_VBEAM = {"terma": 1.0, "cone": 251.9, "gather": 51.7, "gather_T": 84.6, "cone_T": 196.1,
                         "terma_T": 3.5, "geometry": 0.0}
 
 
