@@ -51,6 +51,17 @@ def cases():
     b = inputs.single_beam(fmap=(12, 12), beamlet_cm=0.4, gantry_deg=130.0, couch_deg=25.0)
     b.fluence = rng.uniform(0.0, 1.0, b.fluence.shape).astype(np.float32)
     yield "headneck48", vol, phys, [b]
+    # a calc bbox inside the volume (dosecalc-preprocess crops it to the
+    # body): TERMA, the crop box and the dose stop at its faces; a
+    # non-square fluence map of non-square beamlets, larger than the bbox
+    vol = inputs.slab_phantom(32, 0.25)
+    vol.bbox_start = np.array([5, 3, 7], np.int64)
+    vol.bbox_size = np.array([22, 26, 18], np.int64)
+    phys = inputs.make_physics(seed=0, spacing_cm=0.25)
+    b = inputs.single_beam(fmap=(10, 6), beamlet_cm=0.4, gantry_deg=60.0, couch_deg=15.0, coll_deg=20.0)
+    b.beamlet_size = (0.4, 0.6)
+    b.fluence = rng.uniform(0.2, 1.0, b.fluence.shape).astype(np.float32)
+    yield "slab32_bbox", vol, phys, [b]
 
 
 def beamlet_cases():
