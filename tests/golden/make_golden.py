@@ -13,6 +13,7 @@ generators in endtoend_gb300/inputs.py staying unchanged.
     python tests/golden/make_golden.py          # every fixture
     python tests/golden/make_golden.py kernel   # the kernel-table fixtures only
     python tests/golden/make_golden.py beam [name ...]   # dosecalc-beam fixtures (all, or the named)
+    python tests/golden/make_golden.py beamlet [name ...]   # dosecalc-beamlet fixtures (all, or the named)
 
 The kernel-table fixtures in tests/golden/kernel come from the reference's
 spectrum and kernel-table build (spectra.cpp, kernel.cpp) run on the CPU by
@@ -80,6 +81,15 @@ def beamlet_cases():
     f[2, 1] = 0.0
     b.fluence = f
     yield "bl_headneck40", vol, phys, b, 1.5, (500, 500, 500), 1e-4
+    # a calc bbox inside the volume: pillars, columns and CSR rows clipped
+    # to it (rows keyed in the full volume)
+    vol = inputs.slab_phantom(32, 0.25)
+    vol.bbox_start = np.array([4, 2, 5], np.int64)
+    vol.bbox_size = np.array([24, 28, 22], np.int64)
+    phys = inputs.make_physics(seed=7, spacing_cm=0.25)
+    b = inputs.single_beam(fmap=(3, 3), beamlet_cm=0.5, gantry_deg=30.0, couch_deg=10.0)
+    b.fluence = np.array([[1, 0.5, 0], [1, 1, 1], [0.2, 1, 1]], np.float32)
+    yield "bl_slab32_bbox", vol, phys, b, 2.0, (500, 500, 500), 1e-4
 
 
 def physics_fields(vol, phys):
@@ -92,9 +102,11 @@ def physics_fields(vol, phys):
     }
 
 
-def main_beamlet():
+def main_beamlet(only=None):
     os.makedirs(os.path.join(HERE, "beamlet"), exist_ok=True)
     for name, vol, phys, b, ke, max_rev, thresh in beamlet_cases():
+        if only and name not in only:
+            continue
         h = BeamletHarness(vol, phys, tex_emulate=True)
         idx, cols, info = h.columns(b, kernel_extent=ke, max_rev_size=max_rev)
         out = physics_fields(vol, phys)
@@ -171,6 +183,9 @@ def main():
         return
     if sys.argv[1:2] == ["beam"]:
         main_beam(sys.argv[2:] or None)
+        return
+    if sys.argv[1:2] == ["beamlet"]:
+        main_beamlet(sys.argv[2:] or None)
         return
     main_kernel()
     main_beamlet()
