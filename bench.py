@@ -22,6 +22,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -51,6 +52,7 @@ def parse():
     ap.add_argument("--beamlet-beams", type=int, default=3)
     ap.add_argument("--no-beamlet", action="store_true")
     ap.add_argument("--no-anneal", action="store_true")
+    ap.add_argument("--clocks-csv", default=None, help="keep the nvidia-smi samples of the timed region here")
     return ap.parse_args()
 
 
@@ -88,14 +90,21 @@ class ClockSampler:
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, index):
+    def __init__(self, index, path=None):
+        """path: keep the raw samples there (CSV); by default a temporary file
+        that is removed once the summary is read."""
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{index}.csv")
+        self.keep = path is not None
+        self.path = path
 
     def start(self):
         try:
-            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            if self.keep:
+                os.makedirs(os.path.dirname(os.path.abspath(self.path)), exist_ok=True)
+            else:
+                fd, self.path = tempfile.mkstemp(prefix=f"ee_clocks_rank{self.index}_", suffix=".csv")
+                os.close(fd)
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
                                           "--format=csv,noheader,nounits", "-lms", "200"],
@@ -105,6 +114,11 @@ class ClockSampler:
 
     def stop(self):
         if self.proc is None:
+            if not self.keep and self.path:
+                try:
+                    os.remove(self.path)
+                except OSError:
+                    pass
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         time.sleep(0.3)
         self.proc.terminate()
@@ -127,6 +141,11 @@ class ClockSampler:
             for n, v in zip(names, p[5:9]):
                 if v.lower().startswith("active"):
                     reasons.add(n)
+        if not self.keep:
+            try:
+                os.remove(self.path)
+            except OSError:
+                pass
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
                 "samples": len(sm)}
 
@@ -460,7 +479,7 @@ def main():
             ms.append(a.elapsed_time(b))
         return ms
 
-    clocks = ClockSampler(local)
+    clocks = ClockSampler(local, args.clocks_csv)
     barrier(ws)
     torch.cuda.synchronize()
     clocks.start()
