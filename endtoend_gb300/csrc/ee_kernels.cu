@@ -21,6 +21,7 @@
 #include <algorithm>
 #include <cfloat>
 #include <cstddef>
+#include <mutex>
 
 #include "ee_device.cuh"
 
@@ -1428,21 +1429,37 @@ cudaError_t ee_launch_geometry(const EeParams& P, const EeBeamSpec* specs, EeBea
 
 static size_t cone_smem(int maxL) { return sizeof(float) * ((size_t)CONE_WARPS * 3 * maxL + 2 * EE_MAX_RADII + EE_MAX_RADII); }
 
-// Raise a kernel's dynamic shared-memory limit once per size class (set
-// before any graph capture by the first eager launch).
-static cudaError_t cone_attr(const void* fn, size_t smem) {
+// Raise a kernel's dynamic shared-memory limit on the current device.  The
+// attribute belongs to the (device, kernel) pair, so the cache of what was
+// set is keyed by both; the lock covers concurrent server threads.  The
+// first eager launch on a device sets it, before any graph capture.
+static cudaError_t smem_attr(const void* fn, size_t smem) {
     if (smem <= 48 * 1024) return cudaSuccess;
-    static const void* done_fn[4] = {nullptr, nullptr, nullptr, nullptr};
-    static size_t done_sz[4] = {0, 0, 0, 0};
-    for (int k = 0; k < 4; k++)
-        if (done_fn[k] == fn && done_sz[k] >= smem) return cudaSuccess;
-    const size_t cap = 200 * 1024;  // set once to the largest size any line needs
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max(smem, cap));
-    if (e != cudaSuccess) e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e == cudaSuccess)
-        for (int k = 0; k < 4; k++)
-            if (done_fn[k] == nullptr || done_fn[k] == fn) { done_fn[k] = fn; done_sz[k] = std::max(smem, cap); break; }
-    return e;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    struct Done {
+        int dev;
+        const void* fn;
+        size_t sz;
+    };
+    static std::mutex mu;
+    static Done done[64];
+    static int ndone = 0;
+    std::lock_guard<std::mutex> lock(mu);
+    for (int k = 0; k < ndone; k++)
+        if (done[k].dev == dev && done[k].fn == fn && done[k].sz >= smem) return cudaSuccess;
+    size_t got = std::max(smem, (size_t)200 * 1024);  // once, to the largest size any line needs
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)got);
+    if (e != cudaSuccess) {
+        got = smem;
+        e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)got);
+    }
+    if (e != cudaSuccess) return e;
+    for (int k = 0; k < ndone; k++)
+        if (done[k].dev == dev && done[k].fn == fn) { done[k].sz = got; return cudaSuccess; }
+    if (ndone < 64) done[ndone++] = Done{dev, fn, got};
+    return cudaSuccess;
 }
 
 cudaError_t ee_launch_cone(const EeParams& P, const EeBeamSpec* specs, const EeBeamGeom* geoms, const float* terma,
@@ -1456,7 +1473,7 @@ cudaError_t ee_launch_cone(const EeParams& P, const EeBeamSpec* specs, const EeB
         return cudaGetLastError();
     }
     size_t smem = cone_smem(max_line);
-    cudaError_t e = cone_attr((const void*)k_cone, smem);
+    cudaError_t e = smem_attr((const void*)k_cone, smem);
     if (e != cudaSuccess) return e;
     dim3 grid(grid1(max_lines, CONE_WARPS), P.nrays, nbeams);
     k_cone<<<grid, CONE_WARPS * 32, smem, s>>>(P, specs, geoms, terma, rev, max_line);
@@ -1480,13 +1497,8 @@ cudaError_t ee_launch_gather(const EeParams& P, const EeBeamSpec* specs, const E
 cudaError_t ee_launch_gather_T(const EeParams& P, const EeBeamSpec* specs, const EeBeamGeom* geoms,
                                const float* dose_grad, float* rev_grad, int nbeams, int max_tiles, cudaStream_t s) {
     const size_t smem = sizeof(float) * GT_SMEM;
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute((const void*)k_gather_T, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)smem);
-        if (e != cudaSuccess) return e;
-        attr_set = true;
-    }
+    cudaError_t e = smem_attr((const void*)k_gather_T, smem);
+    if (e != cudaSuccess) return e;
     dim3 grid(max(1, max_tiles), 1, nbeams);
     k_gather_T<<<grid, GT_TX * GT_TY * GT_TZ, smem, s>>>(P, specs, geoms, dose_grad, rev_grad);
     return cudaGetLastError();
@@ -1505,7 +1517,7 @@ cudaError_t ee_launch_cone_T(const EeParams& P, const EeBeamSpec* specs, const E
         return cudaGetLastError();
     }
     size_t smem = cone_smem(max_line);
-    cudaError_t e = cone_attr((const void*)k_cone_T, smem);
+    cudaError_t e = smem_attr((const void*)k_cone_T, smem);
     if (e != cudaSuccess) return e;
     dim3 grid(grid1(max_lines, CONE_WARPS), P.nrays, nbeams);
     k_cone_T<<<grid, CONE_WARPS * 32, smem, s>>>(P, specs, geoms, rev_grad, terma_grad, max_line);

@@ -25,6 +25,11 @@
 //  * The first call on a device looks the array's device address up with
 //    cudaGetSymbolAddress (that device current); make that first call before
 //    any stream capture.
+//  * Every call reads the beam's crop box back to the host and waits for the
+//    caller's stream before it returns.  The kernels run on that stream and
+//    read the context's density texture and kernel tables, which ee_set_* and
+//    ee_destroy release after synchronising only the context's own stream:
+//    the caller synchronises its stream before either.
 #include <cuda_runtime.h>
 
 #include <cstdio>

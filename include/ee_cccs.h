@@ -207,7 +207,11 @@ int ee_dose_and_adjoint(ee_context *ctx, const ee_beam *beams, int nbeams, const
  * cudaFree.  The context must be set up (ee_set_*, which allocate) first.
  * Calls share the array, so calls that overlap on the GPU race; the first
  * call on a device looks the array's address up and should come before any
- * stream capture.  `stream` is a cudaStream_t (NULL = legacy default). */
+ * stream capture.  Every call reads the beam's crop box back to the host and
+ * waits for `stream` before it returns.  The call reads the context's
+ * density texture and kernel tables on `stream`, so synchronise `stream`
+ * before an ee_set_* or ee_destroy of that context.  `stream` is a
+ * cudaStream_t (NULL = legacy default). */
 int ee_beam_dose_noalloc(ee_context *ctx, const ee_beam *beam, const float *d_fluence, float *d_dose, void *stream);
 
 /* ---- planned batches (CUDA graph) ----

@@ -19,16 +19,31 @@ LIB = os.path.join(OUT, "libccref.so")
 LIBS = {"beam": ("ref_harness.cpp", LIB),
         "beamlet": ("ref_beamlet_harness.cpp", os.path.join(OUT, "libccref_beamlet.so")),
         "kernel": ("ref_kernel_harness.cpp", os.path.join(OUT, "libccref_kernel.so"))}
-REF = os.environ.get("CCCS_REFERENCE", "/root/reference")
+HOW = ("set CCCS_REFERENCE to the reference checkout (the directory that holds CCCS/), "
+       "or place the checkout beside this repository as ../reference")
+
+
+def reference_root():
+    """The reference checkout: $CCCS_REFERENCE, else a `reference` directory
+    beside this repository; None when neither holds CCCS/dosecalc-beam."""
+    env = os.environ.get("CCCS_REFERENCE")
+    cands = [env] if env else [os.path.join(os.path.dirname(ORACLE), "..", "reference")]
+    for c in cands:
+        if c and os.path.isdir(os.path.join(c, "CCCS", "dosecalc-beam")):
+            return os.path.abspath(c)
+    return None
+
+
+REF = reference_root()
 
 
 def available():
-    return os.path.isdir(os.path.join(REF, "CCCS", "dosecalc-beam"))
+    return REF is not None
 
 
 def build(verbose=False, which="beam"):
     if not available():
-        raise RuntimeError(f"reference checkout not found at {REF}")
+        raise RuntimeError("reference checkout not found: " + HOW)
     os.makedirs(OUT, exist_ok=True)
     srcname, LIB = LIBS[which]
     src = os.path.join(HERE, srcname)

@@ -6,7 +6,8 @@ the beamlet-column fixtures in tests/golden/beamlet/ from the reference's
 dosecalc-beamlet kernel source (cudaBeamletRaytrace, PackRowConvolve,
 PackedREVtoBEVdose, UnpackBEVDosePillar) sparsified as sparse_io.cpp does.
 
-Needs the reference checkout (default /root/reference, or $CCCS_REFERENCE).
+Needs the reference checkout: $CCCS_REFERENCE, or a `reference` directory
+beside this repository (oracle/ref_harness/build.py, reference_root).
 Each fixture stores its complete inputs, so tests never depend on the
 generators in endtoend_gb300/inputs.py staying unchanged.
 
@@ -157,7 +158,10 @@ def main_kernel():
     point kernels (inputs stored) in every (ntheta, nphi) of KERNEL_CONFIGS,
     and the outputs only of the 6 MV spectrum with the measured dsa kernels."""
     os.makedirs(golden_cases.KERNEL, exist_ok=True)
-    ref = os.environ.get("CCCS_REFERENCE", "/root/reference")
+    from oracle.ref_harness import build as ref_build
+    ref = ref_build.reference_root()
+    if ref is None:
+        raise RuntimeError("reference checkout not found: " + ref_build.HOW)
     scratch = os.path.join(os.path.dirname(os.path.dirname(HERE)), "oracle", "_ref", "tmp")
     for seed in (11, 12):
         spec, mono = golden_cases.synthetic_dsa(seed)
