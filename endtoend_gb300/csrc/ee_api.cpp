@@ -941,7 +941,8 @@ int ee_set_kernel_exp(ee_context* c, const float* params) {
 
 int ee_set_kernel_mode(ee_context* c, int mode) {
     if (!c) return fail(EE_ERR_INVALID_ARG, "null context");
-    if (mode != EE_KERNEL_TABLE && mode != EE_KERNEL_EXP) return fail(EE_ERR_INVALID_ARG, "bad kernel mode %d", mode);
+    if (mode != EE_KERNEL_TABLE && mode != EE_KERNEL_EXP && mode != EE_KERNEL_TABLE_WALK)
+        return fail(EE_ERR_INVALID_ARG, "bad kernel mode %d", mode);
     if (mode == EE_KERNEL_EXP && !c->have_exp) return fail(EE_ERR_NOT_READY, "ee_set_kernel_exp has not been called");
     c->P.mode = mode;
     return EE_OK;

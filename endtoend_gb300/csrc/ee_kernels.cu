@@ -545,7 +545,7 @@ __global__ void __launch_bounds__(CONE_WARPS * 32) k_cone(EeParams P, const EeBe
     const EeBeamGeom& G = geoms[b];
     float* tabK = sm + (size_t)CONE_WARPS * 3 * maxL;  // [2][nradii] kernel rows + radii
     float* tabR = tabK + 2 * EE_MAX_RADII;
-    if (P.mode == 0) {
+    if (P.mode != EE_KERNEL_EXP) {
         const EeRayConst& RC = P.rays[ray];
         for (int k = threadIdx.x; k < P.nradii; k += blockDim.x) {
             tabK[k] = P.cumkern[RC.row_fwd * P.nradii + k];
@@ -575,7 +575,7 @@ __global__ void __launch_bounds__(CONE_WARPS * 32) k_cone(EeParams P, const EeBe
         __syncwarp();
         const float inv_nphi = 1.f / (float)P.nphi;
         const EeRayConst& RC = P.rays[ray];
-        if (P.mode == 1) {
+        if (P.mode == EE_KERNEL_EXP) {
             line_scan<true>(rho, T, n, lane, P.lng, P.expp + 4 * RC.row_fwd, D, inv_nphi);
             __syncwarp();
             line_scan<false>(rho, T, n, lane, P.lng, P.expp + 4 * RC.row_rev, D, inv_nphi);
@@ -593,6 +593,486 @@ __global__ void __launch_bounds__(CONE_WARPS * 32) k_cone(EeParams P, const EeBe
         __syncwarp();
     }
     for (int k = lane; k < n; k += 32) out[bk_x(i0 + k)] = D[k];
+}
+
+// ------------------------------------- cone: exact table scan, O(n nr) ----
+// The reference's RowConvolve walk (device.cu:126-211) with the cumulative
+// kernel interpolated linearly between its nr = 24 radial boundaries (the
+// reference's N_KERNEL_RADII), evaluated exactly in O(n * nr) per line
+// instead of O(n^2).
+//
+// One walk direction at a time, in walk order w = 0..n-1 (FWD: line order,
+// the sources of receiver w are k < w; reverse: the mirrored order).  With
+// d_w = delr * rho_w (0 at sentinels), P_w = sum_{m<w} d_m and
+// M_w = P_w + d_w / 2, the walk from receiver w gives source k the
+// radiological distance c_k = P_w - M_k (half the source voxel plus every
+// voxel in between, device.cu:144-164).  It includes every source with
+// c_k <= R_{nr-2} plus the first one beyond that, if its c_k <= R_{nr-1} (the
+// loop's two exits, device.cu:146-147,171).  With s the last included source
+// and V_k = T_k - T_{k-1}, summation by parts of sum T_k (K(c_k) - K(c_{k+1}))
+// gives
+//   D_w = T_s K(c_s) + sum_{k=s+1}^{w-1} V_k K(c_k).
+// K is linear on segment j, (Rm_j, R_j] with Rm_j = R_{j-1} (Rm_0 = 0):
+// K(c) = Km_j + beta_j (c - Rm_j), Km_j = K_{j-1} (Km_0 = 0).  The sources of
+// segment j form the index window [x_j, x_{j-1}) with x_j = the first k whose
+// M_k >= P_w - R_j (x_{-1} = w), so with the prefix sums SV_k = T_{k-1} and
+// SVM_k = sum_{m<k} V_m M_m a window costs two lookups, and regrouping the
+// windows at their shared ends leaves one per boundary:
+//   D_w = T_s K(c_s) + beta_0 (P_w SV_w - SVM_w)
+//       + sum_{j=0}^{nr-3} gamma_{j+1} ((P_w - R_j) SV_{x_j} - SVM_{x_j})
+//       - coef_{nr-2} SV_{x_{nr-2}} + beta_{nr-2} SVM_{x_{nr-2}},
+// gamma_j = beta_j - beta_{j-1}, coef_j = Km_j + beta_j (P_w - Rm_j), every
+// x_j clipped below at s + 1 (source s enters through its own term).  Each
+// lane walks a contiguous chunk of receivers; the x_j only move forward as w
+// grows, so after a binary search for the chunk's first receiver each is
+// advanced, not searched.  Plain FP32: the regrouped terms are bounded by
+// |gamma| * P * T, measured at <= 2e-5 of the line's maximum against the
+// FP64 walk on 1000-sample lines.
+//
+// Transpose (TERMA gradient from the REV-dose gradient g): with the last
+// receiver b_k whose walk reaches source k (P_i - M_{k+1} <= R_{nr-2} and
+// P_i - M_k <= R_{nr-1}, or i = k + 1), and
+//   Phi_b(m) = sum_{i <= b} g_i K(P_i - m)   (K = 0 for P_i <= m),
+// source k receives Tbar_k = Phi_{b_k}(M_k) - Phi_{b_k}(M_{k+1}).  Phi_b(m)
+// regroups the same way over the receiver windows y_j = the first i with
+// P_i > m + R_j, with prefix sums Sg_i = sum_{m<i} g_m and
+// SgP_i = sum_{m<i} g_m P_m; source k evaluates W_k = Phi_{b_k}(M_k) and
+// U_k = Phi_{b_{k-1}}(M_k) in one pass over its pointers, and
+// Tbar_k = W_k - U_{k+1}.
+constexpr int TAB_NR = 24;            // radial boundaries of the fast path
+constexpr int TAB_NB = TAB_NR - 1;    // receiver windows of the forward walk
+
+// Per-block kernel-row tables: R, Rm (shared by both rows), then Km, beta,
+// gamma of the forward row and of the reverse row (EE_MAX_RADII each).
+struct TabRow {
+    const float *R, *Rm, *Km, *B, *G;
+};
+constexpr int TAB_SMEM = 8 * EE_MAX_RADII;
+
+__device__ __forceinline__ void tab_tables(const EeParams& P, const EeRayConst& RC, float* t) {
+    for (int k = threadIdx.x; k < TAB_NR * 2; k += blockDim.x) {
+        const int row = k < TAB_NR ? RC.row_fwd : RC.row_rev, j = k % TAB_NR;
+        const float* Kr = P.cumkern + (size_t)row * P.nradii;
+        const float R = P.radii[j], Rm = j ? P.radii[j - 1] : 0.f;
+        const float K = Kr[j], Km = j ? Kr[j - 1] : 0.f;
+        const float b = (K - Km) / (R - Rm);
+        float bm = 0.f;
+        if (j) bm = (Km - (j > 1 ? Kr[j - 2] : 0.f)) / (Rm - (j > 1 ? P.radii[j - 2] : 0.f));
+        float* o = t + (k < TAB_NR ? 2 : 5) * EE_MAX_RADII;
+        o[j] = Km;
+        o[EE_MAX_RADII + j] = b;
+        o[2 * EE_MAX_RADII + j] = b - bm;
+        if (k < TAB_NR) {
+            t[j] = R;
+            t[EE_MAX_RADII + j] = Rm;
+        }
+    }
+}
+
+__device__ __forceinline__ TabRow tab_row(const float* t, bool fwd) {
+    const float* o = t + (fwd ? 2 : 5) * EE_MAX_RADII;
+    return TabRow{t, t + EE_MAX_RADII, o, o + EE_MAX_RADII, o + 2 * EE_MAX_RADII};
+}
+
+__device__ __forceinline__ float warp_excl_scan(float x, int lane) {
+    float s = x;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const float y = __shfl_up_sync(FULL, s, off);
+        if (lane >= off) s += y;
+    }
+    return s - x;
+}
+
+template <bool FWD>
+__device__ __forceinline__ int wmap(int w, int n) { return FWD ? w : n - 1 - w; }
+
+// lane chunks of a line: odd lengths keep the lanes' strided shared-memory
+// accesses spread over the banks
+__device__ __forceinline__ void tab_chunk(int n, int lane, int& w0, int& w1) {
+    const int cs = ((n + 31) >> 5) | 1;
+    w0 = min(n, lane * cs);
+    w1 = min(n, w0 + cs);
+}
+
+// A[w] = (M_w, SV_w = T_{w-1}, SVM_w, P_w) in walk order; T is 0 at sentinels.
+template <bool FWD>
+__device__ __forceinline__ void tab_build(const float* rho, const float* T, int n, int lane, float delr, float4* A) {
+    int w0, w1;
+    tab_chunk(n, lane, w0, w1);
+    const float tp0 = (w0 > 0 && w0 < w1) ? T[wmap<FWD>(w0 - 1, n)] : 0.f;
+    float sd = 0.f, svm = 0.f, tp = tp0;
+    for (int w = w0; w < w1; w++) {  // chunk sums, P local to the chunk
+        const int i = wmap<FWD>(w, n);
+        const float r = rho[i], t = T[i];
+        const float d = r >= 0.f ? delr * r : 0.f;
+        svm = fmaf(t - tp, fmaf(0.5f, d, sd), svm);
+        sd += d;
+        tp = t;
+    }
+    const float Pst = warp_excl_scan(sd, lane);
+    float S = warp_excl_scan(fmaf(Pst, tp - tp0, svm), lane);
+    float Pw = Pst;
+    tp = tp0;
+    for (int w = w0; w < w1; w++) {
+        const int i = wmap<FWD>(w, n);
+        const float r = rho[i], t = T[i];
+        const float d = r >= 0.f ? delr * r : 0.f;
+        const float M = fmaf(0.5f, d, Pw);
+        A[w] = make_float4(M, tp, S, Pw);
+        S = fmaf(t - tp, M, S);
+        Pw += d;
+        tp = t;
+    }
+}
+
+// Receivers of one walk direction.  FWD writes D[i]; the reverse direction
+// adds its part, divides by nphi and zeroes sentinel samples.  The window
+// ends are independent of one another, so each step issues its shared-memory
+// loads for every boundary before it uses any of them.
+template <bool FWD>
+__device__ __forceinline__ void tab_receivers(const float4* A, const float* rho, int n, int lane, const TabRow& K,
+                                              float* D, float nphi) {
+    int w0, w1;
+    tab_chunk(n, lane, w0, w1);
+    if (w0 >= w1) return;
+    const float* Am = reinterpret_cast<const float*>(A);  // Am[4 k] = M_k
+    const float Rl = K.R[TAB_NR - 1];
+    // boundaries at or beyond the line's radiological length minus M_0 keep
+    // x_j = 0 for every receiver: only the first `ja` move
+    int ja = 0;
+    {
+        const float span = (n > 1 ? A[n - 1].x : 0.f) - Am[0];
+#pragma unroll
+        for (int j = 0; j < TAB_NB; j++) ja += K.R[j] < span ? 1 : 0;
+    }
+    int x[TAB_NB];
+    {   // the chunk's first receiver: lockstep binary searches over [0, w0]
+        const float Pw = A[w0].w;
+#pragma unroll
+        for (int j = 0; j < TAB_NB; j++) x[j] = 0;
+        for (int len = w0 + 1; len > 1;) {
+            const int half = len >> 1;
+#pragma unroll
+            for (int j = 0; j < TAB_NB; j++)
+                if (j < ja) x[j] += Am[4 * (x[j] + half)] < Pw - K.R[j] ? half : 0;
+            len -= half;
+        }
+#pragma unroll
+        for (int j = 0; j < TAB_NB; j++)
+            if (j < ja) x[j] += Am[4 * x[j]] < Pw - K.R[j] ? 1 : 0;
+    }
+    for (int w = w0; w < w1; w++) {
+        const float4 aw = A[w];
+        const float Pw = aw.w;
+        {   // advance every window end to the first k with M_k >= P_w - R_j
+            float m[TAB_NB];
+#pragma unroll
+            for (int j = 0; j < TAB_NB; j++) m[j] = j < ja ? Am[4 * x[j]] : FLT_MAX;
+#pragma unroll
+            for (int j = 0; j < TAB_NB; j++) {
+                const bool adv = x[j] < w && m[j] < Pw - K.R[j];
+                x[j] += adv ? 1 : 0;
+                m[j] = adv ? Am[4 * x[j]] : FLT_MAX;
+            }
+#pragma unroll
+            for (int j = 0; j < TAB_NB; j++) {
+                const float t = Pw - K.R[j];
+                if (x[j] < w && m[j] < t) {
+                    int xx = x[j] + 1;
+                    while (xx < w && Am[4 * xx] < t) ++xx;
+                    x[j] = xx;
+                }
+            }
+        }
+        // the last boundary (radius R_{nr-2}) decides the last included source s
+        const int xs = x[TAB_NB - 1];
+        const bool back = xs >= 1 && Pw - Am[4 * (xs - 1)] <= Rl;
+        const int s = back ? xs - 1 : xs;
+        float tot = 0.f;
+        if (s < w) {
+            const int clip = s + 1;
+            const float4 a_s = A[s], a_s1 = A[clip];
+            float t0 = K.B[0] * fmaf(Pw, aw.y, -aw.z), t1 = 0.f;
+            int seg = 0;
+#pragma unroll
+            for (int j = 0; j < TAB_NB - 1; j++) {
+                const float4 v = A[max(x[j], clip)];
+                seg += x[j] > s ? 1 : 0;
+                const float term = K.G[j + 1] * fmaf(Pw - K.R[j], v.y, -v.z);
+                if (j & 1) t1 += term;
+                else t0 += term;
+            }
+            {   // the lowest window's lower end
+                seg += xs > s ? 1 : 0;
+                const float4 v = A[max(xs, clip)];
+                const float coef = fmaf(K.B[TAB_NB - 1], Pw - K.Rm[TAB_NB - 1], K.Km[TAB_NB - 1]);
+                t1 = fmaf(K.B[TAB_NB - 1], v.z, fmaf(-coef, v.y, t1));
+            }
+            const int sg = back ? TAB_NR - 1 : seg;  // segment of c_s
+            tot = fmaf(a_s1.y, fmaf(K.B[sg], (Pw - a_s.x) - K.Rm[sg], K.Km[sg]), t0 + t1);
+        }
+        const int i = wmap<FWD>(w, n);
+        if (FWD) D[i] = tot;
+        else D[i] = rho[i] >= 0.f ? __fdiv_rn(D[i] + tot, nphi) : 0.f;
+    }
+}
+
+// A[w] = (P_w, Sg_w, SgP_w, M_w), w = 0..n, A[n].x = +inf (pointer stop).
+template <bool FWD>
+__device__ __forceinline__ void tab_build_T(const float* rho, const float* g, int n, int lane, float delr, float4* A) {
+    int w0, w1;
+    tab_chunk(n, lane, w0, w1);
+    float sd = 0.f, sg = 0.f, sgp = 0.f;
+    for (int w = w0; w < w1; w++) {
+        const int i = wmap<FWD>(w, n);
+        const float r = rho[i], gi = g[i];
+        sgp = fmaf(gi, sd, sgp);
+        sg += gi;
+        sd += r >= 0.f ? delr * r : 0.f;
+    }
+    float Pw = warp_excl_scan(sd, lane);
+    float Sg = warp_excl_scan(sg, lane);
+    float SgP = warp_excl_scan(fmaf(Pw, sg, sgp), lane);
+    for (int w = w0; w < w1; w++) {
+        const int i = wmap<FWD>(w, n);
+        const float r = rho[i], gi = g[i];
+        const float d = r >= 0.f ? delr * r : 0.f;
+        A[w] = make_float4(Pw, Sg, SgP, fmaf(0.5f, d, Pw));
+        SgP = fmaf(gi, Pw, SgP);
+        Sg += gi;
+        Pw += d;
+    }
+    if (w1 == n && w0 < w1) A[n] = make_float4(__int_as_float(0x7f800000), Sg, SgP, Pw);
+}
+
+// Sources of one walk direction: W[k] = Phi_{b_k}(M_k), U[k] = Phi_{b_{k-1}}(M_k),
+// with the window ends y_j of source k clipped above at cap + 1 for each cap.
+template <bool FWD>
+__device__ __forceinline__ void tab_sources(const float4* A, int n, int lane, const TabRow& K, float* Wk, float* Uk) {
+    int w0, w1;
+    tab_chunk(n, lane, w0, w1);
+    if (w0 >= w1) return;
+    const float* Ap = reinterpret_cast<const float*>(A);  // Ap[4 i] = P_i, Ap[4 n] = +inf
+    const float Rl = K.R[TAB_NR - 1], Rl2 = K.R[TAB_NR - 2];
+    // the last receiver whose walk reaches source k is the last i with
+    // P_i <= lim_k (or k + 1)
+    auto lim_of = [&](int k, float mk) {
+        float l = mk + Rl;
+        if (k + 1 < n) l = fminf(l, A[k + 1].w + Rl2);
+        return l;
+    };
+    // window ends at or beyond the line's radiological length minus M_0
+    // stay at n for every source: only the first `ja` move
+    int ja = 0;
+    {
+        const float span = Ap[4 * (n - 1)] - A[0].w;
+#pragma unroll
+        for (int j = 0; j < TAB_NR; j++) ja += K.R[j] < span ? 1 : 0;
+    }
+    int y[TAB_NR];
+    int ylim, yu;
+    {   // lockstep searches over [w0 + 1, n]: the first i with P_i > v
+        const float m = A[w0].w;
+        const float vl = lim_of(w0, m), vu = w0 >= 1 ? lim_of(w0 - 1, A[w0 - 1].w) : -FLT_MAX;
+        const int lo = min(w0 + 1, n);
+#pragma unroll
+        for (int j = 0; j < TAB_NR; j++) y[j] = j < ja ? lo : n;
+        ylim = lo;
+        yu = lo;
+        for (int len = n - lo + 1; len > 1;) {
+            const int half = len >> 1;
+#pragma unroll
+            for (int j = 0; j < TAB_NR; j++)
+                if (j < ja) y[j] += Ap[4 * (y[j] + half)] <= m + K.R[j] ? half : 0;
+            ylim += Ap[4 * (ylim + half)] <= vl ? half : 0;
+            yu += Ap[4 * (yu + half)] <= vu ? half : 0;
+            len -= half;
+        }
+#pragma unroll
+        for (int j = 0; j < TAB_NR; j++)
+            if (j < ja) y[j] += Ap[4 * y[j]] <= m + K.R[j] ? 1 : 0;
+        ylim += Ap[4 * ylim] <= vl ? 1 : 0;
+        yu += Ap[4 * yu] <= vu ? 1 : 0;
+    }
+    int capU = min(max(yu - 1, w0), n - 1);  // b_{w0-1}
+    for (int k = w0; k < w1; k++) {
+        const float4 ak = A[k];
+        const float m = ak.w;
+        {
+            const float l = lim_of(k, m);
+            while (Ap[4 * ylim] <= l) ++ylim;
+        }
+        const int capW = min(max(ylim - 1, k + 1), n - 1);  // b_k
+        float W = 0.f, U = 0.f;
+        if (k + 1 < n) {
+            {   // advance every window end to the first i with P_i > m + R_j
+                float p[TAB_NR];
+#pragma unroll
+                for (int j = 0; j < TAB_NR; j++) p[j] = j < ja ? Ap[4 * y[j]] : __int_as_float(0x7f800000);
+#pragma unroll
+                for (int j = 0; j < TAB_NR; j++) {
+                    const bool adv = p[j] <= m + K.R[j];
+                    y[j] += adv ? 1 : 0;
+                    p[j] = adv ? Ap[4 * y[j]] : __int_as_float(0x7f800000);
+                }
+#pragma unroll
+                for (int j = 0; j < TAB_NR; j++) {
+                    const float t = m + K.R[j];
+                    if (p[j] <= t) {
+                        int yy = y[j] + 1;
+                        while (Ap[4 * yy] <= t) ++yy;
+                        y[j] = yy;
+                    }
+                }
+            }
+            const float4 aW = A[capW + 1], aU = A[capU + 1], a0 = A[k + 1];
+            // bottom end k + 1: beta_0 (m Sg - SgP)
+            const float bot = K.B[0] * fmaf(m, a0.y, -a0.z);
+            float W1 = 0.f, U1 = 0.f;
+            W = bot;
+            U = bot;
+#pragma unroll
+            for (int j = 0; j < TAB_NR; j++) {
+                const float4 v = A[y[j]];
+                const float4 vW = y[j] <= capW + 1 ? v : aW;
+                const float4 vU = y[j] <= capU + 1 ? v : aU;
+                if (j < TAB_NR - 1) {
+                    const float t = m + K.R[j];
+                    const float tw = K.G[j + 1] * fmaf(t, vW.y, -vW.z), tu = K.G[j + 1] * fmaf(t, vU.y, -vU.z);
+                    if (j & 1) { W1 += tw; U1 += tu; }
+                    else { W += tw; U += tu; }
+                } else {  // top end: coef'_{nr-1} Sg + beta_{nr-1} SgP
+                    const float coef = K.Km[j] - K.B[j] * (m + K.Rm[j]);
+                    W = fmaf(coef, vW.y, fmaf(K.B[j], vW.z, W));
+                    U = fmaf(coef, vU.y, fmaf(K.B[j], vU.z, U));
+                }
+            }
+            W += W1;
+            U += U1;
+        }
+        Wk[k] = W;
+        Uk[k] = U;
+        capU = capW;
+    }
+}
+
+// Exact-table cone kernel (mode EE_KERNEL_TABLE, nr = 24): REV resample of a
+// line into shared memory, then the two walk directions.
+constexpr int TAB_WARPS = 4;
+
+__host__ __device__ constexpr int tab_lp(int maxL) { return ((maxL + 3) & ~3) + 4; }
+
+__global__ void __launch_bounds__(TAB_WARPS * 32) k_cone_tab(EeParams P, const EeBeamSpec* __restrict__ specs,
+                                                             const EeBeamGeom* __restrict__ geoms,
+                                                             const float* __restrict__ terma, float* __restrict__ rev,
+                                                             int maxL) {
+    extern __shared__ float4 sm4[];
+    float* sm = reinterpret_cast<float*>(sm4);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int ray = blockIdx.y, b = blockIdx.z;
+    const int Lp = tab_lp(maxL);
+    float* tab = sm + (size_t)TAB_WARPS * 7 * Lp;
+    const EeRayConst& RC = P.rays[ray];
+    tab_tables(P, RC, tab);
+    __syncthreads();
+    const EeBeamGeom& G = geoms[b];
+    if (G.status != 0) return;
+    const EeRayGeom& R = G.ray[ray];
+    const int line = blockIdx.x * TAB_WARPS + warp;
+    if (line >= R.nlines) return;
+    const int L = R.rev[0];
+    const int tY = line % R.rev[1], tZ = line / R.rev[1];
+    float4* A = reinterpret_cast<float4*>(sm + (size_t)warp * 7 * Lp);
+    float* rho = sm + (size_t)warp * 7 * Lp + 4 * Lp;
+    float* T = rho + Lp;
+    float* D = T + Lp;
+    const Brick Bv = rev_brick(R.rev[0], R.rev[1], R.rev[2]);
+    float* out = rev + G.arena_off + R.offset + rev_line(Bv, tY, tZ);
+    int i0, n, z0, z1;
+    line_segment(P, G, R, tY, tZ, L, i0, n);
+    line_read_span(G, R, tY, tZ, L, z0, z1);
+    zero_outside_segment(out, Bv, z0, z1, i0, n, lane, 32);
+    if (n <= 0) return;
+    gather_line(P, specs[b], G, R, terma + specs[b].t_off, tY, tZ, i0, n, lane, rho, T);
+    __syncwarp();
+    const float nphi = (float)P.nphi;
+    tab_build<true>(rho, T, n, lane, P.lng, A);
+    __syncwarp();
+    tab_receivers<true>(A, rho, n, lane, tab_row(tab, true), D, nphi);
+    __syncwarp();
+    tab_build<false>(rho, T, n, lane, P.lng, A);
+    __syncwarp();
+    tab_receivers<false>(A, rho, n, lane, tab_row(tab, false), D, nphi);
+    __syncwarp();
+    for (int k = lane; k < n; k += 32) out[bk_x(i0 + k)] = D[k];
+}
+
+// Its adjoint followed by the transpose of the REV TERMA resample.
+__global__ void __launch_bounds__(TAB_WARPS * 32) k_cone_T_tab(EeParams P, const EeBeamSpec* __restrict__ specs,
+                                                               const EeBeamGeom* __restrict__ geoms,
+                                                               const float* __restrict__ rev_grad,
+                                                               float* __restrict__ terma_grad, int maxL) {
+    extern __shared__ float4 sm4[];
+    float* sm = reinterpret_cast<float*>(sm4);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int ray = blockIdx.y, b = blockIdx.z;
+    const int Lp = tab_lp(maxL);
+    float* tab = sm + (size_t)TAB_WARPS * 9 * Lp;
+    const EeRayConst& RC = P.rays[ray];
+    tab_tables(P, RC, tab);
+    __syncthreads();
+    const EeBeamGeom& G = geoms[b];
+    if (G.status != 0) return;
+    const EeRayGeom& R = G.ray[ray];
+    const int line = blockIdx.x * TAB_WARPS + warp;
+    if (line >= R.nlines) return;
+    const int L = R.rev[0];
+    const int tY = line % R.rev[1], tZ = line / R.rev[1];
+    float4* A = reinterpret_cast<float4*>(sm + (size_t)warp * 9 * Lp);
+    float* rho = sm + (size_t)warp * 9 * Lp + 4 * Lp;
+    float* g = rho + Lp;
+    float* Tb = g + Lp;
+    float* Wk = Tb + Lp;
+    float* Uk = Wk + Lp;
+    const EeBeamSpec& S = specs[b];
+    int i0, n;
+    line_segment(P, G, R, tY, tZ, L, i0, n);
+    if (n <= 0) return;
+    gather_line(P, S, G, R, nullptr, tY, tZ, i0, n, lane, rho, nullptr);
+    const Brick Bv = rev_brick(R.rev[0], R.rev[1], R.rev[2]);
+    const float* gin = rev_grad + G.arena_off + R.offset + rev_line(Bv, tY, tZ);
+    const float inv_nphi = 1.f / (float)P.nphi;
+    __syncwarp();
+    for (int k = lane; k < n; k += 32) {
+        g[k] = rho[k] >= 0.f ? gin[bk_x(i0 + k)] * inv_nphi : 0.f;
+        Tb[k] = 0.f;
+    }
+    __syncwarp();
+#pragma unroll 1
+    for (int dir = 0; dir < 2; dir++) {
+        if (dir == 0) tab_build_T<true>(rho, g, n, lane, P.lng, A);
+        else tab_build_T<false>(rho, g, n, lane, P.lng, A);
+        __syncwarp();
+        if (dir == 0) tab_sources<true>(A, n, lane, tab_row(tab, true), Wk, Uk);
+        else tab_sources<false>(A, n, lane, tab_row(tab, false), Wk, Uk);
+        __syncwarp();
+        for (int w = lane; w < n; w += 32) {
+            const float v = Wk[w] - (w + 1 < n ? Uk[w + 1] : 0.f);
+            Tb[dir == 0 ? w : n - 1 - w] += v;
+        }
+        __syncwarp();
+    }
+    // transpose of the REV TERMA resample
+    const f3 gl = ld3(R.G0) + ld3(R.Gy) * (float)tY + ld3(R.Gz) * (float)tZ;
+    const f3 gx = ld3(R.Gx);
+    float* tg = terma_grad + S.t_off;
+    for (int k = lane; k < n; k += 32) {
+        const float v = Tb[k];
+        if (rho[k] < 0.f || v == 0.f) continue;
+        const f3 gp = gl + gx * (float)(i0 + k);
+        tri_brick_scatter(tg, brick_of(S.tn), gp.x - (float)S.t0[0], gp.y - (float)S.t0[1], gp.z - (float)S.t0[2], v);
+    }
 }
 
 // ------------------------------------------- cone: one lane per line ----
@@ -971,7 +1451,7 @@ __global__ void __launch_bounds__(CONE_WARPS * 32) k_cone_T(EeParams P, const Ee
     const EeBeamGeom& G = geoms[b];
     float* tabK = sm + (size_t)CONE_WARPS * 3 * maxL;
     float* tabR = tabK + 2 * EE_MAX_RADII;
-    if (P.mode == 0) {
+    if (P.mode != EE_KERNEL_EXP) {
         const EeRayConst& RC = P.rays[ray];
         for (int k = threadIdx.x; k < P.nradii; k += blockDim.x) {
             tabK[k] = P.cumkern[RC.row_fwd * P.nradii + k];
@@ -1004,7 +1484,7 @@ __global__ void __launch_bounds__(CONE_WARPS * 32) k_cone_T(EeParams P, const Ee
     }
     __syncwarp();
     const EeRayConst& RC = P.rays[ray];
-    if (P.mode == 1) {
+    if (P.mode == EE_KERNEL_EXP) {
         line_scan_T<true>(rho, g, n, lane, P.lng, P.expp + 4 * RC.row_fwd, Tb);
         __syncwarp();
         line_scan_T<false>(rho, g, n, lane, P.lng, P.expp + 4 * RC.row_rev, Tb);
@@ -1472,6 +1952,14 @@ cudaError_t ee_launch_cone(const EeParams& P, const EeBeamSpec* specs, const EeB
         else k_cone_lane<128><<<dim3(grid1(max_lines, 128), P.nrays, nbeams), 128, 0, s>>>(P, specs, geoms, terma, rev, samples);
         return cudaGetLastError();
     }
+    if (P.mode == EE_KERNEL_TABLE && P.nradii == TAB_NR) {  // exact O(n nr) table scan
+        const size_t smem = sizeof(float) * ((size_t)TAB_WARPS * 7 * tab_lp(max_line) + TAB_SMEM);
+        cudaError_t e = smem_attr((const void*)k_cone_tab, smem);
+        if (e != cudaSuccess) return e;
+        dim3 grid(grid1(max_lines, TAB_WARPS), P.nrays, nbeams);
+        k_cone_tab<<<grid, TAB_WARPS * 32, smem, s>>>(P, specs, geoms, terma, rev, max_line);
+        return cudaGetLastError();
+    }
     size_t smem = cone_smem(max_line);
     cudaError_t e = smem_attr((const void*)k_cone, smem);
     if (e != cudaSuccess) return e;
@@ -1514,6 +2002,14 @@ cudaError_t ee_launch_cone_T(const EeParams& P, const EeBeamSpec* specs, const E
         else
             k_cone_T_lane<128><<<dim3(grid1(max_lines, 128), P.nrays, nbeams), 128, 0, s>>>(P, specs, geoms, rev_grad,
                                                                                           scratch, terma_grad);
+        return cudaGetLastError();
+    }
+    if (P.mode == EE_KERNEL_TABLE && P.nradii == TAB_NR) {
+        const size_t smem = sizeof(float) * ((size_t)TAB_WARPS * 9 * tab_lp(max_line) + TAB_SMEM);
+        cudaError_t e = smem_attr((const void*)k_cone_T_tab, smem);
+        if (e != cudaSuccess) return e;
+        dim3 grid(grid1(max_lines, TAB_WARPS), P.nrays, nbeams);
+        k_cone_T_tab<<<grid, TAB_WARPS * 32, smem, s>>>(P, specs, geoms, rev_grad, terma_grad, max_line);
         return cudaGetLastError();
     }
     size_t smem = cone_smem(max_line);

@@ -34,6 +34,7 @@ EE_ERR_IO = 9
 
 KERNEL_TABLE = 0
 KERNEL_EXP = 1
+KERNEL_TABLE_WALK = 2
 
 DOSE_SUM = 0
 DOSE_ACCUMULATE = 1
@@ -293,7 +294,10 @@ class Engine:
         self.phys = phys
 
     def set_mode(self, mode: str):
-        self._check(self.lib.ee_set_kernel_mode(self.h, KERNEL_EXP if mode == "exp" else KERNEL_TABLE))
+        modes = {"exp": KERNEL_EXP, "table": KERNEL_TABLE, "walk": KERNEL_TABLE_WALK}
+        if mode not in modes:
+            raise ValueError(f"kernel mode {mode!r}: one of {sorted(modes)}")
+        self._check(self.lib.ee_set_kernel_mode(self.h, modes[mode]))
 
     def set_terma_supersampling(self, ss_factor: int):
         """TERMA supersampling (omni-header ss_factor), forward dose only."""

@@ -58,8 +58,12 @@ typedef enum {
 typedef enum {
     EE_KERNEL_TABLE = 0,  /* cumulative kernel table, linear interpolation in
                              radius: the reference's discretisation           */
-    EE_KERNEL_EXP = 1     /* double exponential A e^{-ar} + B e^{-br} per
+    EE_KERNEL_EXP = 1,    /* double exponential A e^{-ar} + B e^{-br} per
                              zenith bin: O(L) recurrence (fast path)          */
+    EE_KERNEL_TABLE_WALK = 2 /* the table discretisation evaluated by the
+                             reference's step-by-step walk, O(L^2) per line
+                             (EE_KERNEL_TABLE evaluates the same sums in
+                             O(L * nradii) when nradii is 24)                 */
 } ee_kernel_mode;
 
 /* dose output modes for ee_beam_dose* */

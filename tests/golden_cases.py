@@ -135,3 +135,19 @@ def kernel_names():
 
 def load_kernel(name):
     return dict(np.load(os.path.join(KERNEL, name + ".npz")))
+
+
+def measured_physics(spacing=0.25):
+    """Physics with the measured 6 MV cumulative table of the fixture
+    spec_6X_measured (the reference's kernel build from its own data files)
+    and the double-exponential fit of it; also returns the fit's error per
+    cone."""
+    from endtoend_gb300 import engine
+    z = load_kernel("spec_6X_measured")
+    g = lambda k: z["nt8_np6_" + k]
+    params, err = engine.fit_exp_kernel(g("radii"), g("cum_total"))
+    return inputs.Physics(energy=g("energy"), fluence=g("fluence"), mu=g("mu"), mu_en=g("mu_en"), ntheta=8, nphi=6,
+                          radii=g("radii").astype(np.float64), exp_params=params.astype(np.float64),
+                          cumkern=g("cum_total").astype(np.float64), theta_deg=g("conv_theta").astype(np.float64),
+                          phi_deg=g("conv_phi").astype(np.float64), rev_latspacing=spacing, rev_longspacing=spacing,
+                          penumbra=1.0), err

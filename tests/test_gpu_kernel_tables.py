@@ -49,14 +49,7 @@ def test_gpu_tables_errors():
 
 
 def _measured_physics(spacing=0.25):
-    z = golden_cases.load_kernel("spec_6X_measured")
-    g = lambda k: z["nt8_np6_" + k]
-    params, err = engine.fit_exp_kernel(g("radii"), g("cum_total"))
-    return inputs.Physics(energy=g("energy"), fluence=g("fluence"), mu=g("mu"), mu_en=g("mu_en"), ntheta=8, nphi=6,
-                          radii=g("radii").astype(np.float64), exp_params=params.astype(np.float64),
-                          cumkern=g("cum_total").astype(np.float64), theta_deg=g("conv_theta").astype(np.float64),
-                          phi_deg=g("conv_phi").astype(np.float64), rev_latspacing=spacing, rev_longspacing=spacing,
-                          penumbra=1.0), err
+    return golden_cases.measured_physics(spacing)
 
 
 @pytest.mark.parametrize("gantry,couch", [(0.0, 0.0), (40.0, 20.0)])
