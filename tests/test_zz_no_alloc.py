@@ -7,7 +7,8 @@ cudaMalloc/cudaFree would stall the device.  For them the library keeps one
 static 64 MiB device array as scratch.  This test calls that entry point
 twice in a row (two different beams, so the second call reuses scratch the
 first one left behind) and checks each result against the allocating entry
-point ee_beam_dose_device, with the tolerance of the other multi-call tests
+point ee_beam_dose_device, in both kernel modes (the double-exponential
+recurrence and the cumulative-kernel table), with the tolerance of the other multi-call tests
 (rtol 1e-5, atol 1e-6 of the dose maximum); the second call must not change
 the device's free memory.  The file is named to be collected last.
 """
@@ -21,7 +22,8 @@ from endtoend_gb300 import engine, inputs
 pytestmark = pytest.mark.gpu
 
 
-def test_noalloc_matches_allocating_entry_point_two_calls():
+@pytest.mark.parametrize("mode", ["exp", "table"])
+def test_noalloc_matches_allocating_entry_point_two_calls(mode):
     import torch
 
     vol, phys, beams = inputs.config0()
@@ -30,7 +32,7 @@ def test_noalloc_matches_allocating_entry_point_two_calls():
     nvox = vol.nvoxels
     with engine.Engine(0) as e:
         e.set_volume(vol)
-        e.set_physics(phys, mode="exp")
+        e.set_physics(phys, mode=mode)
         stream = C.c_void_p(e.stream)
         for call, beam in enumerate([beams[0], second]):
             fl = torch.from_numpy(np.ascontiguousarray(beam.fluence.ravel())).cuda()
