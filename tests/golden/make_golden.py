@@ -15,6 +15,7 @@ generators in endtoend_gb300/inputs.py staying unchanged.
     python tests/golden/make_golden.py kernel   # the kernel-table fixtures only
     python tests/golden/make_golden.py beam [name ...]   # dosecalc-beam fixtures (all, or the named)
     python tests/golden/make_golden.py beamlet [name ...]   # dosecalc-beamlet fixtures (all, or the named)
+    python tests/golden/make_golden.py cfg4     # 200 beamlets of the beamlet-coefficient configuration
 
 The kernel-table fixtures in tests/golden/kernel come from the reference's
 spectrum and kernel-table build (spectra.cpp, kernel.cpp) run on the CPU by
@@ -191,9 +192,63 @@ def main():
     if sys.argv[1:2] == ["beamlet"]:
         main_beamlet(sys.argv[2:] or None)
         return
+    if sys.argv[1:] == ["cfg4"]:
+        main_cfg4()
+        return
     main_kernel()
     main_beamlet()
     main_beam()
+    main_cfg4()
+
+
+def main_cfg4():
+    """200 beamlet columns of the beamlet-coefficient configuration
+    (golden_cases.cfg4_problem: the 200x200x160 phantom at 2 mm, 8 beams of
+    the 1162-beam grid, 25 beamlets each, kernel extent 2 cm, threshold 1e-4
+    of each column's maximum) from the reference's dosecalc-beamlet kernels,
+    stored as per-column summaries (golden_cases.column_summary), with the
+    reference's own change per column under rounding-level isocentre and REV
+    lattice shifts."""
+    vol, phys, beams = golden_cases.cfg4_problem()
+    ke, max_rev, thresh = 2.0, (500, 500, 500), 1e-4
+    h = BeamletHarness(vol, phys, tex_emulate=True)
+    out = physics_fields(vol, phys)
+    del out["density"]
+    out.update({"density_sha256": golden_cases.density_digest(vol), "kernel_extent": ke, "max_rev": list(max_rev),
+                "thresh": thresh, "nbeams": len(beams)})
+    fields = ("max", "sum", "nnz")
+    for k, b in enumerate(beams):
+        idx, cols, info = h.columns(b, kernel_extent=ke, max_rev_size=max_rev)
+        summ = []
+        for c in cols:
+            keys, vals = sparsify(c, thresh, vol.bbox_start, vol.size)
+            summ.append(golden_cases.column_summary(keys, vals, vol.size))
+        noise = np.zeros(len(idx))
+        for kind, amount in (("iso", (1e-5, 1e-5, -1e-5)), ("iso", (-1e-6, 1e-6, 1e-6)), ("rev", 1e-5),
+                             ("rev", -1e-5)):
+            if kind == "iso":
+                bp = inputs.Beam(**{**b.__dict__})
+                bp.isocenter = np.asarray(b.isocenter, np.float64) + np.array(amount)
+                _, cp_, _ = h.columns(bp, kernel_extent=ke, max_rev_size=max_rev)
+            else:
+                _, cp_, _ = h.columns(b, kernel_extent=ke, max_rev_size=max_rev, rev_jitter=amount)
+            for c in range(len(idx)):
+                noise[c] = max(noise[c], float(np.abs(cp_[c] - cols[c]).max() / cols[c].max()))
+            del cp_
+        out[f"beam{k}_angles"] = [b.azimuth, b.zenith, b.coll]
+        out[f"beam{k}_iso"] = b.isocenter
+        out[f"beam{k}_fluence"] = b.fluence
+        out[f"beam{k}_beamlet_index"] = idx
+        out[f"beam{k}_ref_noise"] = noise
+        for j, f in enumerate(fields):
+            out[f"beam{k}_{f}"] = np.array([s_[j] for s_ in summ])
+        for j, f in ((3, "top_key"), (4, "top_val"), (5, "blk_key"), (6, "blk_sum")):
+            out[f"beam{k}_{f}_ptr"] = np.cumsum([0] + [len(s_[j]) for s_ in summ]).astype(np.int64)
+            out[f"beam{k}_{f}"] = np.concatenate([s_[j] for s_ in summ])
+        print("cfg4 beam", k, "beamlets", len(idx), "info", info, "nnz", out[f"beam{k}_nnz"].tolist()[:5],
+              "ref noise", np.round(noise, 4), flush=True)
+        del cols
+    np.savez_compressed(golden_cases.CFG4, **out)
 
 
 def main_beam(only=None):

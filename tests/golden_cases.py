@@ -151,3 +151,74 @@ def measured_physics(spacing=0.25):
                           cumkern=g("cum_total").astype(np.float64), theta_deg=g("conv_theta").astype(np.float64),
                           phi_deg=g("conv_phi").astype(np.float64), rev_latspacing=spacing, rev_longspacing=spacing,
                           penumbra=1.0), err
+
+
+# ------------------------------------------- config-4 beamlet-column fixture --
+# 200 beamlets of the beamlet-coefficient configuration, checked column by
+# column against the reference's dosecalc-beamlet kernels.  The dense columns
+# (~35 k voxels each above the 1e-4 threshold) do not fit a fixture, so each
+# column is stored as a summary: its maximum, sum and entry count, its
+# CFG4_TOP largest entries exactly, and its sums over CFG4_BLOCK^3 voxel
+# blocks.  The phantom is regenerated from its generator and checked
+# against a stored SHA-256 of its density.
+CFG4 = os.path.join(GOLDEN, "beamlet_cfg4", "cfg4_200.npz")
+CFG4_BLOCK = 8
+CFG4_TOP = 128
+
+
+def cfg4_problem():
+    """The 200x200x160 head-and-neck phantom at 2 mm, 8x6 cones, and 8 beams
+    of the 1162-beam 4-pi grid (seed 5) with 40x40 beamlets of 2.5 mm, 25
+    seeded beamlets active per beam at unit weight: 200 beamlets."""
+    vol = inputs.head_neck_phantom(shape=(200, 200, 160), voxel_cm=0.2)
+    phys = inputs.make_physics(seed=0, spacing_cm=0.2)
+    angs = inputs.four_pi_angles(1162, seed=5)
+    rng = np.random.default_rng(404)
+    pick = np.sort(rng.choice(len(angs), 8, replace=False))
+    beams = []
+    for g, c in angs[pick]:
+        b = inputs.single_beam(fmap=(40, 40), beamlet_cm=0.25, gantry_deg=float(g), couch_deg=float(c))
+        f = np.zeros((40, 40), np.float32)
+        f.ravel()[rng.choice(1600, 25, replace=False)] = 1.0
+        b.fluence = f
+        beams.append(b)
+    return vol, phys, beams
+
+
+def density_digest(vol):
+    import hashlib
+    return hashlib.sha256(np.ascontiguousarray(vol.density, np.float32).tobytes()).hexdigest()
+
+
+def column_summary(keys, vals, size):
+    """Summary of one sparse column (full-grid linear keys, values):
+    (max, sum, nnz, top keys, top values, block keys, block sums)."""
+    keys = np.asarray(keys, np.int64)
+    vals = np.asarray(vals, np.float64)
+    nx, ny = int(size[0]), int(size[1])
+    B = CFG4_BLOCK
+    x, y, z = keys % nx, (keys // nx) % ny, keys // (nx * ny)
+    bx, by = (nx + B - 1) // B, (ny + B - 1) // B
+    bk = ((z // B) * by + y // B) * bx + x // B
+    ub, inv = np.unique(bk, return_inverse=True)
+    bs = np.bincount(inv, weights=vals)
+    top = np.argsort(-vals, kind="stable")[:CFG4_TOP]
+    return (float(vals.max()), float(vals.sum()), int(len(vals)), keys[top], vals[top], ub, bs)
+
+
+def load_cfg4():
+    """(vol, phys, beams, kernel_extent, max_rev, thresh, fixture dict)."""
+    z = dict(np.load(CFG4))
+    vol, _, beams = cfg4_problem()
+    if density_digest(vol) != str(z["density_sha256"]):
+        raise RuntimeError("the head-and-neck phantom generator no longer gives the fixture's density")
+    sp = z["spacing"]
+    phys = inputs.Physics(energy=z["energy"], fluence=z["sp_fluence"], mu=z["mu"], mu_en=z["mu_en"],
+                          ntheta=int(z["ntheta"]), nphi=int(z["nphi"]), radii=z["radii"], exp_params=z["exp_params"],
+                          cumkern=z["cumkern"], theta_deg=z["theta_deg"], phi_deg=z["phi_deg"],
+                          rev_latspacing=float(sp[0]), rev_longspacing=float(sp[1]), penumbra=float(z["penumbra"]))
+    for k, b in enumerate(beams):
+        b.azimuth, b.zenith, b.coll = (float(v) for v in z[f"beam{k}_angles"])
+        b.isocenter = z[f"beam{k}_iso"]
+        b.fluence = z[f"beam{k}_fluence"].astype(np.float32)
+    return (vol, phys, beams, float(z["kernel_extent"]), tuple(int(v) for v in z["max_rev"]), float(z["thresh"]), z)
