@@ -320,20 +320,20 @@ void worker(ee_server* S, Slot* slot) {
             std::unique_lock<std::mutex> lk(S->mu);
             S->cv_work.wait(lk, [&] { return S->stop || !S->queue.empty(); });
             if (S->stop && S->queue.empty()) break;
-            // the oldest request, plus every queued request for the same
-            // volume and kind, up to max_batch_beams beams
+            // the oldest request, plus the queued requests right behind it
+            // for the same volume and kind, up to max_batch_beams beams:
+            // merging stops at the first request it cannot take, so no
+            // request overtakes an older one of another volume or kind
             auto first = S->queue.front();
             int nbeams = 0;
-            for (auto it = S->queue.begin(); it != S->queue.end();) {
-                auto& r = *it;
-                if (r->volume == first->volume && r->kind == first->kind &&
-                    (batch.empty() || nbeams + (int)r->beams.size() <= S->max_batch_beams)) {
-                    nbeams += (int)r->beams.size();
-                    batch.push_back(r);
-                    it = S->queue.erase(it);
-                } else {
-                    ++it;
-                }
+            while (!S->queue.empty()) {
+                auto& r = S->queue.front();
+                if (!(r->volume == first->volume && r->kind == first->kind &&
+                      (batch.empty() || nbeams + (int)r->beams.size() <= S->max_batch_beams)))
+                    break;
+                nbeams += (int)r->beams.size();
+                batch.push_back(r);
+                S->queue.pop_front();
             }
         }
         run_batch(S, *slot, batch);
