@@ -642,13 +642,18 @@ __global__ void __launch_bounds__(CONE_WARPS * 32) k_cone(EeParams P, const EeBe
 constexpr int TAB_NR = 24;            // radial boundaries of the fast path
 constexpr int TAB_NB = TAB_NR - 1;    // receiver windows of the forward walk
 
-// Per-block kernel-row tables: R, Rm (shared by both rows), then Km, beta,
-// gamma of the forward row and of the reverse row (EE_MAX_RADII each).
+// Per-block kernel-row tables: R, Rm (shared by both rows), then for the
+// forward row and for the reverse row Km, beta, gamma and the suffix sums
+// SG_j = sum_{m=j}^{nr-2} gamma_{m+1} and SGR_j = sum_{m=j}^{nr-2}
+// gamma_{m+1} R_m (EE_MAX_RADII each).  Window ends that cannot move on a
+// line (radius at least the line's radiological length) all sit at the same
+// position, so their terms are summed in closed form from SG and SGR.
 struct TabRow {
-    const float *R, *Rm, *Km, *B, *G;
+    const float *R, *Rm, *Km, *B, *G, *SG, *SGR;
 };
-constexpr int TAB_SMEM = 8 * EE_MAX_RADII;
+constexpr int TAB_SMEM = 12 * EE_MAX_RADII;
 
+// Fills the tables; the caller synchronises the block before using them.
 __device__ __forceinline__ void tab_tables(const EeParams& P, const EeRayConst& RC, float* t) {
     for (int k = threadIdx.x; k < TAB_NR * 2; k += blockDim.x) {
         const int row = k < TAB_NR ? RC.row_fwd : RC.row_rev, j = k % TAB_NR;
@@ -658,7 +663,7 @@ __device__ __forceinline__ void tab_tables(const EeParams& P, const EeRayConst& 
         const float b = (K - Km) / (R - Rm);
         float bm = 0.f;
         if (j) bm = (Km - (j > 1 ? Kr[j - 2] : 0.f)) / (Rm - (j > 1 ? P.radii[j - 2] : 0.f));
-        float* o = t + (k < TAB_NR ? 2 : 5) * EE_MAX_RADII;
+        float* o = t + (k < TAB_NR ? 2 : 7) * EE_MAX_RADII;
         o[j] = Km;
         o[EE_MAX_RADII + j] = b;
         o[2 * EE_MAX_RADII + j] = b - bm;
@@ -667,11 +672,25 @@ __device__ __forceinline__ void tab_tables(const EeParams& P, const EeRayConst& 
             t[EE_MAX_RADII + j] = Rm;
         }
     }
+    __syncthreads();
+    if (threadIdx.x < 2) {
+        float* o = t + (threadIdx.x == 0 ? 2 : 7) * EE_MAX_RADII;
+        float sg = 0.f, sgr = 0.f;
+        o[3 * EE_MAX_RADII + TAB_NR - 1] = 0.f;
+        o[4 * EE_MAX_RADII + TAB_NR - 1] = 0.f;
+        for (int j = TAB_NR - 2; j >= 0; j--) {
+            sg += o[2 * EE_MAX_RADII + j + 1];
+            sgr = fmaf(o[2 * EE_MAX_RADII + j + 1], t[j], sgr);
+            o[3 * EE_MAX_RADII + j] = sg;
+            o[4 * EE_MAX_RADII + j] = sgr;
+        }
+    }
 }
 
 __device__ __forceinline__ TabRow tab_row(const float* t, bool fwd) {
-    const float* o = t + (fwd ? 2 : 5) * EE_MAX_RADII;
-    return TabRow{t, t + EE_MAX_RADII, o, o + EE_MAX_RADII, o + 2 * EE_MAX_RADII};
+    const float* o = t + (fwd ? 2 : 7) * EE_MAX_RADII;
+    return TabRow{t, t + EE_MAX_RADII, o, o + EE_MAX_RADII, o + 2 * EE_MAX_RADII, o + 3 * EE_MAX_RADII,
+                  o + 4 * EE_MAX_RADII};
 }
 
 __device__ __forceinline__ float warp_excl_scan(float x, int lane) {
@@ -695,9 +714,12 @@ __device__ __forceinline__ void tab_chunk(int n, int lane, int& w0, int& w1) {
     w1 = min(n, w0 + cs);
 }
 
-// A[w] = (M_w, SV_w = T_{w-1}, SVM_w, P_w) in walk order; T is 0 at sentinels.
+// M_w, P_w, SV_w = T_{w-1} and SVM_w in walk order (separate arrays: lanes
+// reading scattered samples then spread over all the banks); T is 0 at
+// sentinels.
 template <bool FWD>
-__device__ __forceinline__ void tab_build(const float* rho, const float* T, int n, int lane, float delr, float4* A) {
+__device__ __forceinline__ void tab_build(const float* rho, const float* T, int n, int lane, float delr, float* Mv,
+                                          float* Pv, float* SVv, float* SVMv) {
     int w0, w1;
     tab_chunk(n, lane, w0, w1);
     const float tp0 = (w0 > 0 && w0 < w1) ? T[wmap<FWD>(w0 - 1, n)] : 0.f;
@@ -719,7 +741,10 @@ __device__ __forceinline__ void tab_build(const float* rho, const float* T, int 
         const float r = rho[i], t = T[i];
         const float d = r >= 0.f ? delr * r : 0.f;
         const float M = fmaf(0.5f, d, Pw);
-        A[w] = make_float4(M, tp, S, Pw);
+        Mv[w] = M;
+        Pv[w] = Pw;
+        SVv[w] = tp;
+        SVMv[w] = S;
         S = fmaf(t - tp, M, S);
         Pw += d;
         tp = t;
@@ -727,90 +752,78 @@ __device__ __forceinline__ void tab_build(const float* rho, const float* T, int 
 }
 
 // Receivers of one walk direction.  FWD writes D[i]; the reverse direction
-// adds its part, divides by nphi and zeroes sentinel samples.  The window
-// ends are independent of one another, so each step issues its shared-memory
-// loads for every boundary before it uses any of them.
+// adds its part, divides by nphi and zeroes sentinel samples.  X: this lane's
+// window ends, X[32 j] = x_j (shared memory, so the loops over the window
+// ends stay loops).
 template <bool FWD>
-__device__ __forceinline__ void tab_receivers(const float4* A, const float* rho, int n, int lane, const TabRow& K,
-                                              float* D, float nphi) {
+__device__ __forceinline__ void tab_receivers(const float* Mv, const float* Pv, const float* SVv, const float* SVMv,
+                                              const float* rho, int n, int lane, const TabRow& K, int* X, float* D,
+                                              float nphi) {
     int w0, w1;
     tab_chunk(n, lane, w0, w1);
     if (w0 >= w1) return;
-    const float* Am = reinterpret_cast<const float*>(A);  // Am[4 k] = M_k
     const float Rl = K.R[TAB_NR - 1];
-    // boundaries at or beyond the line's radiological length minus M_0 keep
-    // x_j = 0 for every receiver: only the first `ja` move
+    // window ends with R_j >= M_{n-1} - M_0 stay at 0 for every receiver
+    const float span = Mv[n - 1] - Mv[0];
     int ja = 0;
-    {
-        const float span = (n > 1 ? A[n - 1].x : 0.f) - Am[0];
-#pragma unroll
-        for (int j = 0; j < TAB_NB; j++) ja += K.R[j] < span ? 1 : 0;
-    }
-    int x[TAB_NB];
-    {   // the chunk's first receiver: lockstep binary searches over [0, w0]
-        const float Pw = A[w0].w;
-#pragma unroll
-        for (int j = 0; j < TAB_NB; j++) x[j] = 0;
-        for (int len = w0 + 1; len > 1;) {
-            const int half = len >> 1;
-#pragma unroll
-            for (int j = 0; j < TAB_NB; j++)
-                if (j < ja) x[j] += Am[4 * (x[j] + half)] < Pw - K.R[j] ? half : 0;
-            len -= half;
+    while (ja < TAB_NB && K.R[ja] < span) ++ja;
+    const int jm = min(ja, TAB_NB - 1);  // moving middle window ends: j < jm
+    // closed form of the fixed middle ends j in [jm, nr-3]
+    const float sgf = K.SG[jm] - K.SG[TAB_NB - 1], sgrf = K.SGR[jm] - K.SGR[TAB_NB - 1];
+    {   // the chunk's first receiver: binary searches (x_j <= x_{j-1})
+        const float Pw = Pv[w0];
+        int hi = w0;
+        for (int j = 0; j < ja; j++) {
+            const float t = Pw - K.R[j];
+            int lo = 0, h = hi;
+            while (lo < h) {
+                const int mid = (lo + h) >> 1;
+                if (Mv[mid] >= t) h = mid;
+                else lo = mid + 1;
+            }
+            X[32 * j] = lo;
+            hi = lo;
         }
-#pragma unroll
-        for (int j = 0; j < TAB_NB; j++)
-            if (j < ja) x[j] += Am[4 * x[j]] < Pw - K.R[j] ? 1 : 0;
+        for (int j = ja; j < TAB_NB; j++) X[32 * j] = 0;
     }
     for (int w = w0; w < w1; w++) {
-        const float4 aw = A[w];
-        const float Pw = aw.w;
-        {   // advance every window end to the first k with M_k >= P_w - R_j
-            float m[TAB_NB];
-#pragma unroll
-            for (int j = 0; j < TAB_NB; j++) m[j] = j < ja ? Am[4 * x[j]] : FLT_MAX;
-#pragma unroll
-            for (int j = 0; j < TAB_NB; j++) {
-                const bool adv = x[j] < w && m[j] < Pw - K.R[j];
-                x[j] += adv ? 1 : 0;
-                m[j] = adv ? Am[4 * x[j]] : FLT_MAX;
-            }
-#pragma unroll
-            for (int j = 0; j < TAB_NB; j++) {
-                const float t = Pw - K.R[j];
-                if (x[j] < w && m[j] < t) {
-                    int xx = x[j] + 1;
-                    while (xx < w && Am[4 * xx] < t) ++xx;
-                    x[j] = xx;
-                }
+        const float Pw = Pv[w];
+        // the last window end (radius R_{nr-2}) decides the last included source s
+        int xs = X[32 * (TAB_NB - 1)];
+        if (TAB_NB - 1 < ja) {
+            const float t = Pw - K.R[TAB_NB - 1];
+            while (xs < w && Mv[xs] < t) ++xs;
+            X[32 * (TAB_NB - 1)] = xs;
+        }
+        const bool back = xs >= 1 && Pw - Mv[xs - 1] <= Rl;
+        const int s = back ? xs - 1 : xs;
+        const int clip = s + 1;  // window ends are clipped below at s + 1
+        float tot = 0.f;
+        int seg = 0;
+#pragma unroll 1
+        for (int j = 0; j < jm; j++) {
+            const float t = Pw - K.R[j];
+            int xx = X[32 * j];
+            while (xx < w && Mv[xx] < t) ++xx;
+            X[32 * j] = xx;
+            if (s < w) {
+                seg += xx > s ? 1 : 0;
+                const int lo = max(xx, clip);
+                tot = fmaf(K.G[j + 1], fmaf(t, SVv[lo], -SVMv[lo]), tot);
             }
         }
-        // the last boundary (radius R_{nr-2}) decides the last included source s
-        const int xs = x[TAB_NB - 1];
-        const bool back = xs >= 1 && Pw - Am[4 * (xs - 1)] <= Rl;
-        const int s = back ? xs - 1 : xs;
-        float tot = 0.f;
         if (s < w) {
-            const int clip = s + 1;
-            const float4 a_s = A[s], a_s1 = A[clip];
-            float t0 = K.B[0] * fmaf(Pw, aw.y, -aw.z), t1 = 0.f;
-            int seg = 0;
-#pragma unroll
-            for (int j = 0; j < TAB_NB - 1; j++) {
-                const float4 v = A[max(x[j], clip)];
-                seg += x[j] > s ? 1 : 0;
-                const float term = K.G[j + 1] * fmaf(Pw - K.R[j], v.y, -v.z);
-                if (j & 1) t1 += term;
-                else t0 += term;
-            }
+            const float svc = SVv[clip], svmc = SVMv[clip];
+            tot += fmaf(svc, fmaf(Pw, sgf, -sgrf), -svmc * sgf);  // fixed middle ends
+            tot = fmaf(K.B[0], fmaf(Pw, SVv[w], -SVMv[w]), tot);   // top end w
             {   // the lowest window's lower end
                 seg += xs > s ? 1 : 0;
-                const float4 v = A[max(xs, clip)];
+                const int lo = max(xs, clip);
                 const float coef = fmaf(K.B[TAB_NB - 1], Pw - K.Rm[TAB_NB - 1], K.Km[TAB_NB - 1]);
-                t1 = fmaf(K.B[TAB_NB - 1], v.z, fmaf(-coef, v.y, t1));
+                tot = fmaf(K.B[TAB_NB - 1], SVMv[lo], fmaf(-coef, SVv[lo], tot));
             }
             const int sg = back ? TAB_NR - 1 : seg;  // segment of c_s
-            tot = fmaf(a_s1.y, fmaf(K.B[sg], (Pw - a_s.x) - K.Rm[sg], K.Km[sg]), t0 + t1);
+            tot = fmaf(svc, fmaf(K.B[sg], (Pw - Mv[s]) - K.Rm[sg], K.Km[sg]), tot);
         }
         const int i = wmap<FWD>(w, n);
         if (FWD) D[i] = tot;
@@ -818,9 +831,10 @@ __device__ __forceinline__ void tab_receivers(const float4* A, const float* rho,
     }
 }
 
-// A[w] = (P_w, Sg_w, SgP_w, M_w), w = 0..n, A[n].x = +inf (pointer stop).
+// P_w, Sg_w, SgP_w (w = 0..n, P_n = +inf: pointer stop) and M_w in walk order.
 template <bool FWD>
-__device__ __forceinline__ void tab_build_T(const float* rho, const float* g, int n, int lane, float delr, float4* A) {
+__device__ __forceinline__ void tab_build_T(const float* rho, const float* g, int n, int lane, float delr, float* Pv,
+                                            float* Sgv, float* SgPv, float* Mv) {
     int w0, w1;
     tab_chunk(n, lane, w0, w1);
     float sd = 0.f, sg = 0.f, sgp = 0.f;
@@ -838,118 +852,102 @@ __device__ __forceinline__ void tab_build_T(const float* rho, const float* g, in
         const int i = wmap<FWD>(w, n);
         const float r = rho[i], gi = g[i];
         const float d = r >= 0.f ? delr * r : 0.f;
-        A[w] = make_float4(Pw, Sg, SgP, fmaf(0.5f, d, Pw));
+        Pv[w] = Pw;
+        Sgv[w] = Sg;
+        SgPv[w] = SgP;
+        Mv[w] = fmaf(0.5f, d, Pw);
         SgP = fmaf(gi, Pw, SgP);
         Sg += gi;
         Pw += d;
     }
-    if (w1 == n && w0 < w1) A[n] = make_float4(__int_as_float(0x7f800000), Sg, SgP, Pw);
+    if (w1 == n && w0 < w1) {
+        Pv[n] = __int_as_float(0x7f800000);
+        Sgv[n] = Sg;
+        SgPv[n] = SgP;
+    }
 }
 
 // Sources of one walk direction: W[k] = Phi_{b_k}(M_k), U[k] = Phi_{b_{k-1}}(M_k),
-// with the window ends y_j of source k clipped above at cap + 1 for each cap.
+// with the window ends y_j (Y[32 j], shared memory) clipped above at cap + 1
+// for each cap.
 template <bool FWD>
-__device__ __forceinline__ void tab_sources(const float4* A, int n, int lane, const TabRow& K, float* Wk, float* Uk) {
+__device__ __forceinline__ void tab_sources(const float* Pv, const float* Sgv, const float* SgPv, const float* Mv,
+                                            int n, int lane, const TabRow& K, int* Y, float* Wk, float* Uk) {
     int w0, w1;
     tab_chunk(n, lane, w0, w1);
     if (w0 >= w1) return;
-    const float* Ap = reinterpret_cast<const float*>(A);  // Ap[4 i] = P_i, Ap[4 n] = +inf
     const float Rl = K.R[TAB_NR - 1], Rl2 = K.R[TAB_NR - 2];
-    // the last receiver whose walk reaches source k is the last i with
-    // P_i <= lim_k (or k + 1)
-    auto lim_of = [&](int k, float mk) {
-        float l = mk + Rl;
-        if (k + 1 < n) l = fminf(l, A[k + 1].w + Rl2);
+    // window ends with R_j >= P_{n-1} - M_0 stay at n for every source
+    const float span = Pv[n - 1] - Mv[0];
+    int ja = 0;
+    while (ja < TAB_NR && K.R[ja] < span) ++ja;
+    const int jm = min(ja, TAB_NR - 1);  // moving middle window ends: j < jm
+    auto lim_of = [&](int k) {
+        float l = Mv[k] + Rl;
+        if (k + 1 < n) l = fminf(l, Mv[k + 1] + Rl2);
         return l;
     };
-    // window ends at or beyond the line's radiological length minus M_0
-    // stay at n for every source: only the first `ja` move
-    int ja = 0;
-    {
-        const float span = Ap[4 * (n - 1)] - A[0].w;
-#pragma unroll
-        for (int j = 0; j < TAB_NR; j++) ja += K.R[j] < span ? 1 : 0;
-    }
-    int y[TAB_NR];
-    int ylim, yu;
-    {   // lockstep searches over [w0 + 1, n]: the first i with P_i > v
-        const float m = A[w0].w;
-        const float vl = lim_of(w0, m), vu = w0 >= 1 ? lim_of(w0 - 1, A[w0 - 1].w) : -FLT_MAX;
-        const int lo = min(w0 + 1, n);
-#pragma unroll
-        for (int j = 0; j < TAB_NR; j++) y[j] = j < ja ? lo : n;
-        ylim = lo;
-        yu = lo;
-        for (int len = n - lo + 1; len > 1;) {
-            const int half = len >> 1;
-#pragma unroll
-            for (int j = 0; j < TAB_NR; j++)
-                if (j < ja) y[j] += Ap[4 * (y[j] + half)] <= m + K.R[j] ? half : 0;
-            ylim += Ap[4 * (ylim + half)] <= vl ? half : 0;
-            yu += Ap[4 * (yu + half)] <= vu ? half : 0;
-            len -= half;
+    // the first receiver i in [lo, n] with P_i > v (P_n = +inf)
+    auto ub = [&](float v, int lo) {
+        int h = n;
+        while (lo < h) {
+            const int mid = (lo + h) >> 1;
+            if (Pv[mid] > v) h = mid;
+            else lo = mid + 1;
         }
-#pragma unroll
-        for (int j = 0; j < TAB_NR; j++)
-            if (j < ja) y[j] += Ap[4 * y[j]] <= m + K.R[j] ? 1 : 0;
-        ylim += Ap[4 * ylim] <= vl ? 1 : 0;
-        yu += Ap[4 * yu] <= vu ? 1 : 0;
+        return lo;
+    };
+    {   // the chunk's first source: binary searches (y_j >= y_{j-1})
+        const float m = Mv[w0];
+        int lo = min(w0 + 1, n);
+        for (int j = 0; j < ja; j++) {
+            lo = ub(m + K.R[j], lo);
+            Y[32 * j] = lo;
+        }
+        for (int j = ja; j < TAB_NR; j++) Y[32 * j] = n;
     }
-    int capU = min(max(yu - 1, w0), n - 1);  // b_{w0-1}
+    int ylim = ub(lim_of(w0), min(w0 + 1, n));
+    int capU = w0 >= 1 ? min(max(ub(lim_of(w0 - 1), w0) - 1, w0), n - 1) : w0;  // b_{w0-1}
     for (int k = w0; k < w1; k++) {
-        const float4 ak = A[k];
-        const float m = ak.w;
+        const float m = Mv[k];
         {
-            const float l = lim_of(k, m);
-            while (Ap[4 * ylim] <= l) ++ylim;
+            const float l = lim_of(k);
+            while (Pv[ylim] <= l) ++ylim;
         }
         const int capW = min(max(ylim - 1, k + 1), n - 1);  // b_k
         float W = 0.f, U = 0.f;
         if (k + 1 < n) {
-            {   // advance every window end to the first i with P_i > m + R_j
-                float p[TAB_NR];
-#pragma unroll
-                for (int j = 0; j < TAB_NR; j++) p[j] = j < ja ? Ap[4 * y[j]] : __int_as_float(0x7f800000);
-#pragma unroll
-                for (int j = 0; j < TAB_NR; j++) {
-                    const bool adv = p[j] <= m + K.R[j];
-                    y[j] += adv ? 1 : 0;
-                    p[j] = adv ? Ap[4 * y[j]] : __int_as_float(0x7f800000);
-                }
-#pragma unroll
-                for (int j = 0; j < TAB_NR; j++) {
-                    const float t = m + K.R[j];
-                    if (p[j] <= t) {
-                        int yy = y[j] + 1;
-                        while (Ap[4 * yy] <= t) ++yy;
-                        y[j] = yy;
-                    }
-                }
-            }
-            const float4 aW = A[capW + 1], aU = A[capU + 1], a0 = A[k + 1];
+            const float sW = Sgv[capW + 1], sWp = SgPv[capW + 1], sU = Sgv[capU + 1], sUp = SgPv[capU + 1];
             // bottom end k + 1: beta_0 (m Sg - SgP)
-            const float bot = K.B[0] * fmaf(m, a0.y, -a0.z);
-            float W1 = 0.f, U1 = 0.f;
-            W = bot;
-            U = bot;
-#pragma unroll
-            for (int j = 0; j < TAB_NR; j++) {
-                const float4 v = A[y[j]];
-                const float4 vW = y[j] <= capW + 1 ? v : aW;
-                const float4 vU = y[j] <= capU + 1 ? v : aU;
-                if (j < TAB_NR - 1) {
-                    const float t = m + K.R[j];
-                    const float tw = K.G[j + 1] * fmaf(t, vW.y, -vW.z), tu = K.G[j + 1] * fmaf(t, vU.y, -vU.z);
-                    if (j & 1) { W1 += tw; U1 += tu; }
-                    else { W += tw; U += tu; }
-                } else {  // top end: coef'_{nr-1} Sg + beta_{nr-1} SgP
-                    const float coef = K.Km[j] - K.B[j] * (m + K.Rm[j]);
-                    W = fmaf(coef, vW.y, fmaf(K.B[j], vW.z, W));
-                    U = fmaf(coef, vU.y, fmaf(K.B[j], vU.z, U));
-                }
+            W = K.B[0] * fmaf(m, Sgv[k + 1], -SgPv[k + 1]);
+            U = W;
+#pragma unroll 1
+            for (int j = 0; j < jm; j++) {
+                const float t = m + K.R[j];
+                int yy = Y[32 * j];
+                while (Pv[yy] <= t) ++yy;
+                Y[32 * j] = yy;
+                const float a = Sgv[yy], ap = SgPv[yy];
+                const bool inW = yy <= capW + 1, inU = yy <= capU + 1;
+                W = fmaf(K.G[j + 1], fmaf(t, inW ? a : sW, -(inW ? ap : sWp)), W);
+                U = fmaf(K.G[j + 1], fmaf(t, inU ? a : sU, -(inU ? ap : sUp)), U);
             }
-            W += W1;
-            U += U1;
+            // fixed middle ends j in [jm, nr-2] sit at n: past both caps
+            const float sg = K.SG[jm], sgr = K.SGR[jm];
+            W += fmaf(sW, fmaf(m, sg, sgr), -sWp * sg);
+            U += fmaf(sU, fmaf(m, sg, sgr), -sUp * sg);
+            {   // top end (radius R_{nr-1}): coef'_{nr-1} Sg + beta_{nr-1} SgP
+                const int j = TAB_NR - 1;
+                int yy = Y[32 * j];
+                if (j < ja) {
+                    while (Pv[yy] <= m + K.R[j]) ++yy;
+                    Y[32 * j] = yy;
+                }
+                const float coef = K.Km[j] - K.B[j] * (m + K.Rm[j]);
+                const bool inW = yy <= capW + 1, inU = yy <= capU + 1;
+                W = fmaf(coef, inW ? Sgv[yy] : sW, fmaf(K.B[j], inW ? SgPv[yy] : sWp, W));
+                U = fmaf(coef, inU ? Sgv[yy] : sU, fmaf(K.B[j], inU ? SgPv[yy] : sUp, U));
+            }
         }
         Wk[k] = W;
         Uk[k] = U;
@@ -962,6 +960,8 @@ __device__ __forceinline__ void tab_sources(const float4* A, int n, int lane, co
 constexpr int TAB_WARPS = 4;
 
 __host__ __device__ constexpr int tab_lp(int maxL) { return ((maxL + 3) & ~3) + 4; }
+__host__ __device__ constexpr int tab_fwd_stride(int maxL) { return 7 * tab_lp(maxL) + 32 * TAB_NB; }
+__host__ __device__ constexpr int tab_adj_stride(int maxL) { return 9 * tab_lp(maxL) + 32 * TAB_NR; }
 
 __global__ void __launch_bounds__(TAB_WARPS * 32) k_cone_tab(EeParams P, const EeBeamSpec* __restrict__ specs,
                                                              const EeBeamGeom* __restrict__ geoms,
@@ -972,7 +972,7 @@ __global__ void __launch_bounds__(TAB_WARPS * 32) k_cone_tab(EeParams P, const E
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int ray = blockIdx.y, b = blockIdx.z;
     const int Lp = tab_lp(maxL);
-    float* tab = sm + (size_t)TAB_WARPS * 7 * Lp;
+    float* tab = sm + (size_t)TAB_WARPS * tab_fwd_stride(maxL);
     const EeRayConst& RC = P.rays[ray];
     tab_tables(P, RC, tab);
     __syncthreads();
@@ -983,10 +983,14 @@ __global__ void __launch_bounds__(TAB_WARPS * 32) k_cone_tab(EeParams P, const E
     if (line >= R.nlines) return;
     const int L = R.rev[0];
     const int tY = line % R.rev[1], tZ = line / R.rev[1];
-    float4* A = reinterpret_cast<float4*>(sm + (size_t)warp * 7 * Lp);
-    float* rho = sm + (size_t)warp * 7 * Lp + 4 * Lp;
+    float* Mv = sm + (size_t)warp * tab_fwd_stride(maxL);
+    float* Pv = Mv + Lp;
+    float* SVv = Pv + Lp;
+    float* SVMv = SVv + Lp;
+    float* rho = SVMv + Lp;
     float* T = rho + Lp;
     float* D = T + Lp;
+    int* X = reinterpret_cast<int*>(D + Lp) + lane;
     const Brick Bv = rev_brick(R.rev[0], R.rev[1], R.rev[2]);
     float* out = rev + G.arena_off + R.offset + rev_line(Bv, tY, tZ);
     int i0, n, z0, z1;
@@ -997,13 +1001,13 @@ __global__ void __launch_bounds__(TAB_WARPS * 32) k_cone_tab(EeParams P, const E
     gather_line(P, specs[b], G, R, terma + specs[b].t_off, tY, tZ, i0, n, lane, rho, T);
     __syncwarp();
     const float nphi = (float)P.nphi;
-    tab_build<true>(rho, T, n, lane, P.lng, A);
+    tab_build<true>(rho, T, n, lane, P.lng, Mv, Pv, SVv, SVMv);
     __syncwarp();
-    tab_receivers<true>(A, rho, n, lane, tab_row(tab, true), D, nphi);
+    tab_receivers<true>(Mv, Pv, SVv, SVMv, rho, n, lane, tab_row(tab, true), X, D, nphi);
     __syncwarp();
-    tab_build<false>(rho, T, n, lane, P.lng, A);
+    tab_build<false>(rho, T, n, lane, P.lng, Mv, Pv, SVv, SVMv);
     __syncwarp();
-    tab_receivers<false>(A, rho, n, lane, tab_row(tab, false), D, nphi);
+    tab_receivers<false>(Mv, Pv, SVv, SVMv, rho, n, lane, tab_row(tab, false), X, D, nphi);
     __syncwarp();
     for (int k = lane; k < n; k += 32) out[bk_x(i0 + k)] = D[k];
 }
@@ -1018,7 +1022,7 @@ __global__ void __launch_bounds__(TAB_WARPS * 32) k_cone_T_tab(EeParams P, const
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int ray = blockIdx.y, b = blockIdx.z;
     const int Lp = tab_lp(maxL);
-    float* tab = sm + (size_t)TAB_WARPS * 9 * Lp;
+    float* tab = sm + (size_t)TAB_WARPS * tab_adj_stride(maxL);
     const EeRayConst& RC = P.rays[ray];
     tab_tables(P, RC, tab);
     __syncthreads();
@@ -1029,12 +1033,16 @@ __global__ void __launch_bounds__(TAB_WARPS * 32) k_cone_T_tab(EeParams P, const
     if (line >= R.nlines) return;
     const int L = R.rev[0];
     const int tY = line % R.rev[1], tZ = line / R.rev[1];
-    float4* A = reinterpret_cast<float4*>(sm + (size_t)warp * 9 * Lp);
-    float* rho = sm + (size_t)warp * 9 * Lp + 4 * Lp;
+    float* Pv = sm + (size_t)warp * tab_adj_stride(maxL);
+    float* Sgv = Pv + Lp;
+    float* SgPv = Sgv + Lp;
+    float* Mv = SgPv + Lp;
+    float* rho = Mv + Lp;
     float* g = rho + Lp;
     float* Tb = g + Lp;
     float* Wk = Tb + Lp;
     float* Uk = Wk + Lp;
+    int* Y = reinterpret_cast<int*>(Uk + Lp) + lane;
     const EeBeamSpec& S = specs[b];
     int i0, n;
     line_segment(P, G, R, tY, tZ, L, i0, n);
@@ -1051,11 +1059,11 @@ __global__ void __launch_bounds__(TAB_WARPS * 32) k_cone_T_tab(EeParams P, const
     __syncwarp();
 #pragma unroll 1
     for (int dir = 0; dir < 2; dir++) {
-        if (dir == 0) tab_build_T<true>(rho, g, n, lane, P.lng, A);
-        else tab_build_T<false>(rho, g, n, lane, P.lng, A);
+        if (dir == 0) tab_build_T<true>(rho, g, n, lane, P.lng, Pv, Sgv, SgPv, Mv);
+        else tab_build_T<false>(rho, g, n, lane, P.lng, Pv, Sgv, SgPv, Mv);
         __syncwarp();
-        if (dir == 0) tab_sources<true>(A, n, lane, tab_row(tab, true), Wk, Uk);
-        else tab_sources<false>(A, n, lane, tab_row(tab, false), Wk, Uk);
+        if (dir == 0) tab_sources<true>(Pv, Sgv, SgPv, Mv, n, lane, tab_row(tab, true), Y, Wk, Uk);
+        else tab_sources<false>(Pv, Sgv, SgPv, Mv, n, lane, tab_row(tab, false), Y, Wk, Uk);
         __syncwarp();
         for (int w = lane; w < n; w += 32) {
             const float v = Wk[w] - (w + 1 < n ? Uk[w + 1] : 0.f);
@@ -1953,7 +1961,7 @@ cudaError_t ee_launch_cone(const EeParams& P, const EeBeamSpec* specs, const EeB
         return cudaGetLastError();
     }
     if (P.mode == EE_KERNEL_TABLE && P.nradii == TAB_NR) {  // exact O(n nr) table scan
-        const size_t smem = sizeof(float) * ((size_t)TAB_WARPS * 7 * tab_lp(max_line) + TAB_SMEM);
+        const size_t smem = sizeof(float) * ((size_t)TAB_WARPS * tab_fwd_stride(max_line) + TAB_SMEM);
         cudaError_t e = smem_attr((const void*)k_cone_tab, smem);
         if (e != cudaSuccess) return e;
         dim3 grid(grid1(max_lines, TAB_WARPS), P.nrays, nbeams);
@@ -2005,7 +2013,7 @@ cudaError_t ee_launch_cone_T(const EeParams& P, const EeBeamSpec* specs, const E
         return cudaGetLastError();
     }
     if (P.mode == EE_KERNEL_TABLE && P.nradii == TAB_NR) {
-        const size_t smem = sizeof(float) * ((size_t)TAB_WARPS * 9 * tab_lp(max_line) + TAB_SMEM);
+        const size_t smem = sizeof(float) * ((size_t)TAB_WARPS * tab_adj_stride(max_line) + TAB_SMEM);
         cudaError_t e = smem_attr((const void*)k_cone_T_tab, smem);
         if (e != cudaSuccess) return e;
         dim3 grid(grid1(max_lines, TAB_WARPS), P.nrays, nbeams);
