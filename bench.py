@@ -55,6 +55,10 @@ def parse():
     ap.add_argument("--no-beamlet", action="store_true")
     ap.add_argument("--no-anneal", action="store_true")
     ap.add_argument("--clocks-csv", default=None, help="keep the nvidia-smi samples of the timed region here")
+    ap.add_argument("--profile-case", default=None, choices=["exp", "table", "walk"],
+                    help="small case for ncu captures: forward + adjoint of --profile-beams beams of the workload, "
+                         "twice, in this kernel mode; prints one line and exits")
+    ap.add_argument("--profile-beams", type=int, default=2)
     return ap.parse_args()
 
 
@@ -471,8 +475,35 @@ def algorithmic_bytes(infos):
     return 392.0 * vb, vb
 
 
+def profile_case(args):
+    """Two forward + adjoint calls on a few beams spread over the workload
+    (the launches an ncu capture selects with -k / -s / -c)."""
+    import torch
+    from endtoend_gb300 import engine
+    vol, phys, beams = make_workload(args.beams)
+    nb = max(1, args.profile_beams)
+    beams = beams[::max(1, len(beams) // nb)][:nb]
+    eng = engine.Engine(0)
+    eng.set_volume(vol)
+    eng.set_physics(phys, mode=args.profile_case)
+    fl = torch.from_numpy(engine.concat_fluence(beams)).cuda()
+    dose = torch.zeros(vol.nvoxels, device="cuda")
+    g = torch.from_numpy(np.random.default_rng(11).standard_normal(vol.nvoxels).astype(np.float32)).cuda()
+    fg = torch.zeros_like(fl)
+    for _ in range(2):
+        eng.dose_and_adjoint_device(beams, fl.data_ptr(), dose.data_ptr(), g.data_ptr(), fg.data_ptr())
+    eng.synchronize()
+    infos = [eng.beam_info(i) for i in range(nb)]
+    print(json.dumps({"profile_case": args.profile_case, "beams": nb, "v_beam": sum(i["v_beam"] for i in infos),
+                      "max_line": [i["max_line"] for i in infos]}))
+    eng.close()
+
+
 def main():
     args = parse()
+    if args.profile_case:
+        profile_case(args)
+        return
     ws, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, ws, rank)
