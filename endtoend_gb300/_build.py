@@ -18,7 +18,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 OUT_DIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(OUT_DIR, "libee_cccs.so")
-SOURCES = ["ee_kernels.cu", "ee_api.cpp", "ee_noalloc.cu", "ee_server.cpp", "ee_beamlet.cu", "ee_anneal.cu", "ee_preprocess.cu", "ee_kernel_tables.cu"]
+SOURCES = ["ee_kernels.cu", "ee_api.cpp", "ee_noalloc.cu", "ee_server.cpp", "ee_beamlet.cu", "ee_anneal.cu", "ee_preprocess.cu", "ee_kernel_tables.cu", "ee_roi.cpp"]
 HEADERS = ["ee_internal.h", "ee_device.cuh", os.path.join("..", "..", "include", "ee_cccs.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CLI_SRC = os.path.join(CSRC, "ee_dosecalc_beam.cpp")

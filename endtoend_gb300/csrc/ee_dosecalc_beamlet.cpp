@@ -20,6 +20,20 @@
 //   beam_NNNNN_col_ptr.raw         int64  [N_beamlets+1]
 //   beam_NNNNN_lindex.raw          uint32 [nnz]  full-grid voxel index, x fastest, ascending per column
 //   beam_NNNNN_coeffs.raw          float32 [nnz]
+//
+// ROI reduction (the header's `reduce` flag, as main.cu:293-308 and
+// sparse_io.cpp:160-172): the reference reads the ROI masks from
+// <temp>/roi_list.h5, which needs HDF5.  Here they come from
+// <temp>/roi_list.txt (or --roi-list=FILE): one ROI per line,
+//   name x0 y0 z0 nx ny nz mask_file
+// mask_file (relative to the list's directory) holds the crop box's
+// nx*ny*nz uint8 flags, x fastest.  With ROIs, every column is reduced by
+// ee_roi_reduce and the coefficient files become
+//   beam_NNNNN_lindex.raw          uint64 [nnz]  row within the ROI row blocks
+//   beam_NNNNN_row_blocks.raw      int64  [N_beamlets][N_rois]  rows kept per ROI
+// and calc_specs.txt gains roi_order and row_block_capacities.  Without a
+// list the columns are written unreduced, as the reference does when it
+// finds no ROI file.
 #include <chrono>
 #include <cstdio>
 #include <string>
@@ -32,7 +46,7 @@ using namespace contract;
 namespace {
 
 struct Options {
-    std::string out = "./Dose_Coefficients.h5", temp, data;
+    std::string out = "./Dose_Coefficients.h5", temp, data, roi_list;
     float thresh = 1e-6f;
     int device = 0, ndevices = 1;
     bool verbose = false, timing = false, dry_run = false;
@@ -49,6 +63,8 @@ void usage() {
         "  --ndevices=[<int>]               accepted; the engine runs every beam on one GPU\n"
         "  --device=[<int>]                 GPU to use\n"
         "  --sparsify-threshold=[<float>]   keep value > threshold * column max [default: 1.00e-06]\n"
+        "  --roi-list=[<file>]              ROI masks for the row reduction (default <temp>/roi_list.txt when\n"
+        "                                   the header requests a reduction)\n"
         "                                   (also --thresh, --sparsity-threshold)\n"
         "  --temp=[<dir>]                   temp directory (default /tmp/dosecalc/$USER)\n"
         "  --data=[<dir>]                   data directory with spectra/ and dsa/ (default $DOSECALC_DATA or ./data)\n"
@@ -98,6 +114,7 @@ int main(int argc, char** argv) {
             O.thresh = std::strtof(v.c_str(), &end);
             if (v.empty() || *end != '\0' || !(O.thresh >= 0.f)) return fail("bad sparsify threshold", v);
         } else if (flag(a, "temp", &v)) O.temp = v;
+        else if (flag(a, "roi-list", &v)) O.roi_list = v;
         else if (flag(a, "data", &v)) O.data = v;
         else if (flag(a, "dry-run", nullptr)) O.dry_run = true;
         else if (flag(a, "verbose-extra", nullptr) || flag(a, "verbose", nullptr)) O.verbose = true;
@@ -141,6 +158,65 @@ int main(int argc, char** argv) {
     const std::string tf = O.temp + "/convolution_theta_angles.raw", pf = O.temp + "/convolution_phi_angles.raw";
     const bool angle_files = exists(tf) && exists(pf);
     if (angle_files && (read_floats(tf, nrays, theta) || read_floats(pf, nrays, phi))) return 1;
+    // ---- ROI masks for the row reduction
+    std::string roi_path = O.roi_list;
+    if (roi_path.empty() && H.reduce) {
+        if (exists(O.temp + "/roi_list.txt")) roi_path = O.temp + "/roi_list.txt";
+        else if (exists(O.temp + "/roi_list.h5"))
+            std::printf("note: %s/roi_list.h5 needs HDF5, which is not available; give the masks as roi_list.txt "
+                        "(see --help); columns are written unreduced\n", O.temp.c_str());
+    }
+    std::vector<std::string> roi_names;
+    std::vector<std::vector<unsigned char>> roi_bytes;
+    std::vector<ee_roi_mask> roi_masks;
+    if (!roi_path.empty()) {
+        FILE* rf = std::fopen(roi_path.c_str(), "r");
+        if (!rf) return fail("cannot open the ROI list", roi_path);
+        const size_t sl = roi_path.find_last_of('/');
+        const std::string rdir = sl == std::string::npos ? "." : roi_path.substr(0, sl);
+        char line[4096];
+        while (std::fgets(line, sizeof(line), rf)) {
+            char name[1024], file[2048];
+            int c0[3], cn[3];
+            if (line[0] == '#') continue;
+            const int got = std::sscanf(line, "%1023s %d %d %d %d %d %d %2047s", name, &c0[0], &c0[1], &c0[2], &cn[0],
+                                        &cn[1], &cn[2], file);
+            if (got <= 0) continue;
+            if (got != 8 || cn[0] <= 0 || cn[1] <= 0 || cn[2] <= 0) {
+                std::fclose(rf);
+                return fail("malformed ROI list line", line);
+            }
+            std::vector<unsigned char> m((size_t)cn[0] * cn[1] * cn[2]);
+            const std::string mp = file[0] == '/' ? std::string(file) : rdir + "/" + file;
+            FILE* mf = std::fopen(mp.c_str(), "rb");
+            const size_t got_b = mf ? std::fread(m.data(), 1, m.size(), mf) : 0;
+            if (mf) std::fclose(mf);
+            if (got_b != m.size()) {
+                std::fclose(rf);
+                return fail("ROI mask file missing or short", mp);
+            }
+            roi_names.push_back(name);
+            roi_bytes.push_back(std::move(m));
+            ee_roi_mask rm;
+            for (int a = 0; a < 3; a++) {
+                rm.crop_start[a] = c0[a];
+                rm.crop_size[a] = cn[a];
+            }
+            rm.mask = nullptr;
+            roi_masks.push_back(rm);
+        }
+        std::fclose(rf);
+        for (size_t r = 0; r < roi_masks.size(); r++) roi_masks[r].mask = roi_bytes[r].data();
+        if (roi_masks.empty()) return fail("no ROI in the list", roi_path);
+    }
+    ee_roi_list* rois = nullptr;
+    std::vector<long long> capacities(roi_masks.size());
+    if (!roi_masks.empty()) {
+        const int vsize[3] = {(int)H.size[0], (int)H.size[1], (int)H.size[2]};
+        if (check(ee_roi_list_create(vsize, roi_masks.data(), (int)roi_masks.size(), &rois), "reading the ROI masks") ||
+            check(ee_roi_list_capacities(rois, capacities.data()), "reading the ROI masks"))
+            return 1;
+    }
     long long active = 0;
     for (const Beam& B : beams)
         for (float v : B.fluence) active += v > 0.f;
@@ -151,7 +227,10 @@ int main(int argc, char** argv) {
                     H.size[0], H.size[1], H.size[2], H.bbox_start[0], H.bbox_start[1], H.bbox_start[2],
                     H.bbox_size[0], H.bbox_size[1], H.bbox_size[2], H.nphi, H.ntheta, H.kernel_extent, H.max_rev[0],
                     H.max_rev[1], H.max_rev[2], H.beam_spec.c_str(), beams.size(), active, O.thresh);
+    if ((O.verbose || O.dry_run) && rois)
+        std::printf("ROI reduction: %zu ROIs from %s\n", roi_masks.size(), roi_path.c_str());
     if (O.dry_run) {
+        ee_roi_list_destroy(rois);
         std::printf("dry run: inputs read in %.1f ms\n", t_read - t0);
         return 0;
     }
@@ -229,8 +308,35 @@ int main(int argc, char** argv) {
             char base[64];
             std::snprintf(base, sizeof(base), "/beam_%05zu", b);
             const std::string pre = odir + base;
-            if ((rc = write_raw(pre + "_beamlet_index.raw", bidx)) || (rc = write_raw(pre + "_col_ptr.raw", cptr)) ||
-                (rc = write_raw(pre + "_lindex.raw", lidx)) || (rc = write_raw(pre + "_coeffs.raw", coef)))
+            long long nnz_out = csr.nnz;
+            if (rois) {  // _sparsify_and_reduce: the sparsified column, then the ROI rows
+                const size_t nr = roi_masks.size();
+                std::vector<unsigned long long> rkeys;
+                std::vector<float> rvals;
+                std::vector<long long> rptr(1, 0), blocks((size_t)csr.nbeamlets * nr);
+                for (int c = 0; c < csr.nbeamlets && !rc; c++) {
+                    const long long a0 = cptr[c], n = cptr[c + 1] - cptr[c];
+                    const size_t at = rkeys.size();
+                    rkeys.resize(at + (size_t)n * nr);
+                    rvals.resize(at + (size_t)n * nr);
+                    long long got = 0;
+                    rc = check(ee_roi_reduce(rois, reinterpret_cast<const int*>(lidx.data()) + a0, coef.data() + a0, n,
+                                             rkeys.data() + at, rvals.data() + at, n * (long long)nr, &got,
+                                             blocks.data() + (size_t)c * nr),
+                               "reducing a column to the ROIs");
+                    rkeys.resize(at + (size_t)got);
+                    rvals.resize(at + (size_t)got);
+                    rptr.push_back((long long)rkeys.size());
+                }
+                if (rc) break;
+                nnz_out = (long long)rkeys.size();
+                if ((rc = write_raw(pre + "_beamlet_index.raw", bidx)) || (rc = write_raw(pre + "_col_ptr.raw", rptr)) ||
+                    (rc = write_raw(pre + "_lindex.raw", rkeys)) || (rc = write_raw(pre + "_coeffs.raw", rvals)) ||
+                    (rc = write_raw(pre + "_row_blocks.raw", blocks)))
+                    break;
+            } else if ((rc = write_raw(pre + "_beamlet_index.raw", bidx)) ||
+                       (rc = write_raw(pre + "_col_ptr.raw", cptr)) || (rc = write_raw(pre + "_lindex.raw", lidx)) ||
+                       (rc = write_raw(pre + "_coeffs.raw", coef)))
                 break;
             FILE* m = std::fopen((pre + ".txt").c_str(), "w");
             if (!m) {
@@ -241,17 +347,18 @@ int main(int argc, char** argv) {
             std::fprintf(m, "beam_uid %zu\nN_beamlets %d\nN_coeffs %lld\ngantry_rot_rad %.9g\ncouch_rot_rad %.9g\n"
                             "coll_rot_rad %.9g\niso_coords_cm %.9g %.9g %.9g\nsad_cm %.9g\nfmap_size %d %d\n"
                             "beamlet_size_cm %.9g %.9g\nfmap_file %s\n",
-                         b, csr.nbeamlets, csr.nnz, e.azimuth, e.zenith, e.coll, e.isocenter[0], e.isocenter[1],
+                         b, csr.nbeamlets, nnz_out, e.azimuth, e.zenith, e.coll, e.isocenter[0], e.isocenter[1],
                          e.isocenter[2], e.sad, e.fmap_size[0], e.fmap_size[1], e.beamlet_size[0], e.beamlet_size[1],
                          beams[b].fmap_fname.c_str());
             std::fclose(m);
-            total_nnz += csr.nnz;
+            total_nnz += nnz_out;
             total_cols += csr.nbeamlets;
             if (O.verbose) std::printf("beam %zu: %d columns, %lld coefficients\n", b, csr.nbeamlets, csr.nnz);
         }
         t_cols = now_ms();
     } while (false);
     ee_destroy(ctx);
+    ee_roi_list_destroy(rois);
     if (rc) return rc;
     FILE* f = std::fopen((odir + "/calc_specs.txt").c_str(), "w");
     if (!f) return fail("cannot open the output file", odir + "/calc_specs.txt");
@@ -263,6 +370,13 @@ int main(int argc, char** argv) {
                  H.bbox_size[2], H.penumbra, H.latspacing, H.longspacing, H.start[0], H.start[1], H.start[2],
                  H.size[0], H.size[1], H.size[2], H.nphi, H.nradii, H.ntheta, O.thresh, H.voxel[0], H.voxel[1],
                  H.voxel[2], H.kernel_extent, H.beam_spec.c_str(), H.target_structure.c_str());
+    if (!roi_names.empty()) {
+        std::fprintf(f, "roi_order");
+        for (const auto& n : roi_names) std::fprintf(f, " %s", n.c_str());
+        std::fprintf(f, "\nrow_block_capacities");
+        for (long long c : capacities) std::fprintf(f, " %lld", c);
+        std::fprintf(f, "\n");
+    }
     std::fclose(f);
     std::printf("Data written to \"%s/\" (%zu beams, %lld columns, %lld coefficients); Dose_Coefficients.h5 not "
                 "written (no HDF5 library)\n",

@@ -152,6 +152,11 @@ _SIGS = {
     "ee_read_profile": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_longlong), C.c_int]),
     "ee_set_beamlet_options": (C.c_int, [C.c_void_p, C.c_float, C.POINTER(C.c_int)]),
     "ee_beamlet_columns_device": (C.c_int, [C.c_void_p, C.POINTER(EEBeam), C.c_void_p, C.c_float, C.POINTER(Csr)]),
+    "ee_roi_list_create": (C.c_int, [C.POINTER(C.c_int), C.c_void_p, C.c_int, C.POINTER(C.c_void_p)]),
+    "ee_roi_list_capacities": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "ee_roi_reduce": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_longlong, C.c_void_p, C.c_void_p,
+                                C.c_longlong, C.POINTER(C.c_longlong), C.c_void_p]),
+    "ee_roi_list_destroy": (C.c_int, [C.c_void_p]),
     "ee_beamlet_columns": (C.c_int, [C.c_void_p, C.POINTER(EEBeam), C.c_void_p, C.c_float, C.c_longlong, C.c_void_p,
                                      C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_longlong),
                                      C.POINTER(C.c_int)]),
@@ -656,6 +661,59 @@ class Server:
 SIEMENS_LUT = (  # HU -> g/cc, the reference's default table (dosecalc-preprocess/main.cu:187-200)
     [-969.8, -712.9, -536.5, -95.6, -45.6, -5.6, -1.9, 25.7, 65.6, 207.5, 220.7, 429.9, 775.3, 1173.7],
     [0.0, 0.290, 0.450, 0.943, 0.985, 1.000, 1.016, 1.052, 1.089, 1.145, 1.159, 1.335, 1.560, 1.823])
+
+
+class RoiMask(C.Structure):
+    _fields_ = [("crop_start", C.c_int * 3), ("crop_size", C.c_int * 3), ("mask", C.c_void_p)]
+
+
+class RoiList:
+    """ROI row blocks for sparse beamlet columns (ee_roi_*; the reference's
+    _reduce_by_roi, CCCS/DoseCalcIO/sparse_io.cpp:62-158).  rois: list of
+    (crop_start xyz, mask [nz][ny][nx] bool array of the crop box)."""
+
+    def __init__(self, size_xyz, rois):
+        self.lib = load_library()
+        self._masks = [np.ascontiguousarray(m, np.uint8) for _, m in rois]
+        arr = (RoiMask * max(1, len(rois)))()
+        for k, ((c0, _), m) in enumerate(zip(rois, self._masks)):
+            arr[k].crop_start[:] = [int(v) for v in c0]
+            arr[k].crop_size[:] = [m.shape[2], m.shape[1], m.shape[0]]
+            arr[k].mask = m.ctypes.data
+        h = C.c_void_p()
+        size = (C.c_int * 3)(*[int(v) for v in size_xyz])
+        _raise_status(self.lib, self.lib.ee_roi_list_create(size, arr, len(rois), C.byref(h)))
+        self.h = h
+        self.nrois = len(rois)
+
+    def capacities(self) -> np.ndarray:
+        out = np.zeros(max(1, self.nrois), np.int64)
+        _raise_status(self.lib, self.lib.ee_roi_list_capacities(self.h, out.ctypes.data))
+        return out[:self.nrois]
+
+    def reduce(self, row_index, values):
+        """(keys uint64, values float32, row_block_sizes int64) of one column."""
+        ri = np.ascontiguousarray(row_index, np.int32)
+        va = np.ascontiguousarray(values, np.float32)
+        cap = len(ri) * max(1, self.nrois)
+        keys = np.zeros(max(1, cap), np.uint64)
+        vals = np.zeros(max(1, cap), np.float32)
+        blocks = np.zeros(max(1, self.nrois), np.int64)
+        n = C.c_longlong()
+        _raise_status(self.lib, self.lib.ee_roi_reduce(self.h, ri.ctypes.data, va.ctypes.data, len(ri), keys.ctypes.data,
+                                                       vals.ctypes.data, cap, C.byref(n), blocks.ctypes.data))
+        return keys[:n.value], vals[:n.value], blocks[:self.nrois]
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.ee_roi_list_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def ct_to_density(hu: np.ndarray, voxel_cm, iso_voxel_cm: float, lut=SIEMENS_LUT, start_cm=(0.0, 0.0, 0.0),

@@ -270,6 +270,34 @@ int ee_beamlet_columns(ee_context *ctx, const ee_beam *beam, const float *fluenc
                        int *beamlet_index, long long *col_ptr, int *row_index, float *value, long long *nnz,
                        int *nbeamlets);
 
+/* ---- ROI reduction of sparse columns (dosecalc-beamlet, header `reduce`) ----
+ * Replaces _reduce_by_roi (CCCS/DoseCalcIO/sparse_io.cpp:62-158), host code
+ * as in the reference.  A column's rows are kept only where the voxel lies in
+ * an ROI; the ROIs form row blocks in list order, and a kept row's key is the
+ * block's first row (the sum of the previous ROIs' masked voxel counts) plus
+ * the voxel's position among its ROI's masked voxels, counted over the ROI's
+ * crop box with x slowest and z fastest (the reference's loop order).  A
+ * voxel in several ROIs gives one row in each block; rows with value 0 are
+ * dropped.  Keys are 64-bit, as the reference's lindex dataset. */
+typedef struct {
+    int crop_start[3];          /* voxel index of the crop box in the volume */
+    int crop_size[3];
+    const unsigned char *mask;  /* crop_size[0]*crop_size[1]*crop_size[2], x fastest; non-zero = in the ROI */
+} ee_roi_mask;
+typedef struct ee_roi_list ee_roi_list;
+/* size: the full volume (x, y, z); the masks are copied into position tables. */
+int ee_roi_list_create(const int size[3], const ee_roi_mask *rois, int nrois, ee_roi_list **out);
+/* capacities[r] = masked voxel count of ROI r (the reference's row_block_capacities). */
+int ee_roi_list_capacities(const ee_roi_list *list, long long *capacities);
+/* One column: row_index (full-volume voxel keys, as ee_csr) and values of n
+ * entries in; out_keys / out_values receive the reduced rows (capacity
+ * entries), *out_n their count, row_block_sizes[r] the rows kept per ROI.
+ * EE_ERR_CAPACITY when *out_n > capacity (rows beyond capacity not copied). */
+int ee_roi_reduce(const ee_roi_list *list, const int *row_index, const float *values, long long n,
+                  unsigned long long *out_keys, float *out_values, long long capacity, long long *out_n,
+                  long long *row_block_sizes);
+int ee_roi_list_destroy(ee_roi_list *list);
+
 /* ---- request server (continuous batching) ----
  * No counterpart in the reference (dosecalc-beam is a one-shot batch job):
  * a serving loop for many small dose / dose+gradient requests on one GPU.

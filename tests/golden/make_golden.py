@@ -16,6 +16,7 @@ generators in endtoend_gb300/inputs.py staying unchanged.
     python tests/golden/make_golden.py beam [name ...]   # dosecalc-beam fixtures (all, or the named)
     python tests/golden/make_golden.py beamlet [name ...]   # dosecalc-beamlet fixtures (all, or the named)
     python tests/golden/make_golden.py cfg4     # 200 beamlets of the beamlet-coefficient configuration
+    python tests/golden/make_golden.py cfg4_noise   # ... its reference sensitivity over the full shift set
 
 The kernel-table fixtures in tests/golden/kernel come from the reference's
 spectrum and kernel-table build (spectra.cpp, kernel.cpp) run on the CPU by
@@ -195,10 +196,47 @@ def main():
     if sys.argv[1:] == ["cfg4"]:
         main_cfg4()
         return
+    if sys.argv[1:] == ["cfg4_noise"]:
+        main_cfg4_noise()
+        return
     main_kernel()
     main_beamlet()
     main_beam()
     main_cfg4()
+
+
+# the rounding-level shifts of the other beamlet fixtures: isocentre moves
+# of 1e-5 / 1e-6 cm along eight directions and REV lattice moves
+ISO_SHIFTS = [(1, -1, 1), (-1, 1, -1), (1, 0, 0), (0, 1, 0), (0, 0, 1), (-1, -1, 0), (0, -1, 1), (1, 1, 1)]
+REV_JITTERS = (1e-5, -1e-5, 1e-6, -1e-6)
+
+
+def main_cfg4_noise():
+    """Extend the config-4 fixture's per-column reference sensitivity to the
+    full shift set of the other beamlet fixtures (the first pass used four
+    of these moves); the stored value becomes the maximum over all."""
+    z = dict(np.load(golden_cases.CFG4))
+    vol, phys, beams, ke, max_rev, thresh, _ = golden_cases.load_cfg4()
+    h = BeamletHarness(vol, phys, tex_emulate=True)
+    for k, b in enumerate(beams):
+        idx, cols, _ = h.columns(b, kernel_extent=ke, max_rev_size=max_rev)
+        noise = np.array(z[f"beam{k}_ref_noise"], np.float64)
+        moves = [("iso", (1e-5 if j % 2 == 0 else 1e-6) * np.array(sh, float)) for j, sh in enumerate(ISO_SHIFTS)]
+        moves += [("rev", jit) for jit in REV_JITTERS]
+        for kind, amount in moves:
+            if kind == "iso":
+                bp = inputs.Beam(**{**b.__dict__})
+                bp.isocenter = np.asarray(b.isocenter, np.float64) + amount
+                _, cp_, _ = h.columns(bp, kernel_extent=ke, max_rev_size=max_rev)
+            else:
+                _, cp_, _ = h.columns(b, kernel_extent=ke, max_rev_size=max_rev, rev_jitter=amount)
+            for c in range(len(idx)):
+                noise[c] = max(noise[c], float(np.abs(cp_[c] - cols[c]).max() / cols[c].max()))
+            del cp_
+        z[f"beam{k}_ref_noise"] = noise
+        print("cfg4 noise beam", k, np.round(noise, 4), flush=True)
+        del cols
+    np.savez_compressed(golden_cases.CFG4, **z)
 
 
 def main_cfg4():

@@ -96,3 +96,27 @@ def test_beamlet_program_dry_run_and_errors(cli, tmp_path):
     assert "kernel_extent 2 cm" in r.stdout
     r = run(bl, f"--temp={temp}", f"--data={data}", "--dry-run", "--sparsify-threshold=abc")
     assert r.returncode != 0 and "threshold" in r.stderr
+
+
+def test_beamlet_program_roi_list(cli, tmp_path):
+    """dosecalc-beamlet reads an ROI list for the row reduction (dry run:
+    parsing and mask files checked, no GPU work), and rejects a malformed
+    list or a mask file that is too short."""
+    bl = os.path.join(os.path.dirname(cli), "dosecalc-beamlet")
+    vol, beams = dc.slab_case()
+    temp, data = dc.write_contract(str(tmp_path), vol, beams)
+    np.ones(4 * 5 * 6, np.uint8).tofile(os.path.join(temp, "ptv.raw"))
+    lst = os.path.join(temp, "rois.txt")
+    open(lst, "w").write("# name x0 y0 z0 nx ny nz mask\nptv 3 4 5 4 5 6 ptv.raw\n")
+    r = subprocess.run([bl, f"--temp={temp}", f"--data={data}", "--dry-run", f"--roi-list={lst}"],
+                       capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "ROI reduction: 1 ROIs" in r.stdout
+    open(lst, "w").write("ptv 3 4 5 4 5 7 ptv.raw\n")  # 140 flags needed, 120 present
+    r = subprocess.run([bl, f"--temp={temp}", f"--data={data}", "--dry-run", f"--roi-list={lst}"],
+                       capture_output=True, text=True, timeout=60)
+    assert r.returncode != 0 and "short" in (r.stdout + r.stderr)
+    open(lst, "w").write("ptv 3 4 5\n")
+    r = subprocess.run([bl, f"--temp={temp}", f"--data={data}", "--dry-run", f"--roi-list={lst}"],
+                       capture_output=True, text=True, timeout=60)
+    assert r.returncode != 0 and "malformed" in (r.stdout + r.stderr)
