@@ -424,9 +424,6 @@ int pipeline(ee_context* c, const PipeArgs& A) {
     const bool adj = A.d_fgrad != nullptr;
     if (adj && !A.d_dose_grad && !A.loss) return fail(EE_ERR_INVALID_ARG, "adjoint needs a dose gradient or a loss");
     if (A.loss && (!fwd || A.dose_mode != EE_DOSE_SUM)) return fail(EE_ERR_INVALID_ARG, "loss needs the summed dose");
-    if (adj && c->P.ss > 1)
-        return fail(EE_ERR_INVALID_ARG, "TERMA supersampling (ss_factor %d) is forward-only; set it to 1 for adjoints",
-                    c->P.ss);
     EE_CUDA(cudaSetDevice(c->device));
     cudaStream_t s = c->stream;
     const int n = A.nbeams;

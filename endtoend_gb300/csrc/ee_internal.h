@@ -32,7 +32,7 @@ struct EeParams {
     float lat, lng, penumbra;
     int max_rev[3];
     int mode;                   // ee_kernel_mode
-    int ss;                     // TERMA supersampling per axis (1: off); forward only
+    int ss;                     // TERMA supersampling per axis (1: off)
     const float* cumkern;       // [ntheta][nradii]
     const float* expp;          // [ntheta][4]
     const struct EeRayConst* rays;  // [nrays]

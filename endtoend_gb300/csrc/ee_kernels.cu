@@ -69,8 +69,8 @@ __global__ void __launch_bounds__(256, SUPERSAMPLE ? 1 : 5) k_terma(EeParams P, 
         if (SUPERSAMPLE) {
             // supersampled TERMA (cudaSiddon.cu:248-258, 297-306): the mean
             // over ss^3 sub-voxel centres, each with its own beamlet lookup
-            // and ray trace, summed x fastest (forward only: unit and bl_idx
-            // are not requested)
+            // and ray trace, summed x fastest (unit and bl_idx are not kept:
+            // k_terma_T_ss recomputes the sub-voxel beamlets)
             const int ss = P.ss, nsub = ss * ss * ss;
             const float sv0 = P.voxel[0] / (float)ss, sv1 = P.voxel[1] / (float)ss, sv2 = P.voxel[2] / (float)ss;
             float acc = 0.f;
@@ -1827,6 +1827,59 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
     }
 }
 
+// TERMA adjoint with supersampling (ss > 1): the transpose of k_terma<true>,
+// whose voxel TERMA is the mean over ss^3 sub-voxel centres of fluence x
+// unit TERMA, each centre with its own beamlet lookup and ray trace
+// (cudaSiddon.cu:248-258, 297-306).  The forward keeps neither the beamlets
+// nor the unit TERMA of the centres, so each voxel with a non-zero TERMA
+// gradient recomputes them (the same centres, lookups and traces) and adds
+// gradient x unit / ss^3 to its centres' beamlets; consecutive centres that
+// share a beamlet add once.  The fluence enters linearly, as in the ss = 1
+// adjoint (a centre whose beamlet has zero fluence still has its slope).
+__global__ void __launch_bounds__(256) k_terma_T_ss(EeParams P, const EeBeamSpec* __restrict__ specs,
+                                                    const float* __restrict__ terma_grad, float* __restrict__ fgrad) {
+    const int b = blockIdx.z;
+    const EeBeamSpec& S = specs[b];
+    const long long bvol = ee_brick_vol(S.tn);
+    const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= bvol) return;
+    const long long brick = v >> 6;
+    const int w = (int)(v & 63), nbx = (S.tn[0] + 3) >> 2, nby = (S.tn[1] + 3) >> 2;
+    const long long bxy = brick % ((long long)nbx * nby);
+    const int xr = (int)(bxy % nbx) * 4 + (w & 3);
+    const int yr = (int)(bxy / nbx) * 4 + ((w >> 2) & 3);
+    const int zr = (int)(brick / ((long long)nbx * nby)) * 4 + (w >> 4);
+    if (xr >= S.tn[0] || yr >= S.tn[1] || zr >= S.tn[2]) return;
+    const float g = terma_grad[S.t_off + v];
+    if (g == 0.f) return;
+    const int x = S.t0[0] + xr, y = S.t0[1] + yr, z = S.t0[2] + zr;
+    const f3 src = ld3(S.src);
+    const int ss = P.ss, nsub = ss * ss * ss;
+    const float gs = g / (float)nsub;
+    const float sv0 = P.voxel[0] / (float)ss, sv1 = P.voxel[1] / (float)ss, sv2 = P.voxel[2] / (float)ss;
+    bool cap = false;
+    int cur = -1;
+    float acc = 0.f;
+    for (int ii = 0; ii < nsub; ii++) {
+        const int sx = ii % ss, sy = (ii / ss) % ss, sz = ii / (ss * ss);
+        const f3 p = mk(P.start[0] + ((float)x - 0.5f) * P.voxel[0] + ((float)sx + 0.5f) * sv0,
+                        P.start[1] + ((float)y - 0.5f) * P.voxel[1] + ((float)sy + 0.5f) * sv1,
+                        P.start[2] + ((float)z - 0.5f) * P.voxel[2] + ((float)sz + 0.5f) * sv2);
+        int bs = beamlet_of(S, p);
+        if (bs == -2) bs = beamlet_point_fp64(S, (double)p.x, (double)p.y, (double)p.z);
+        if (bs < 0) continue;
+        const float rpl = siddon_rpl(P, p, src, cap);
+        const float u = terma_per_fluence(P, rpl, p, src, S.sad);
+        if (bs != cur) {
+            if (cur >= 0 && acc != 0.f) atomicAdd(fgrad + S.fl_off + cur, acc);
+            cur = bs;
+            acc = 0.f;
+        }
+        acc = fmaf(gs, u, acc);
+    }
+    if (cur >= 0 && acc != 0.f) atomicAdd(fgrad + S.fl_off + cur, acc);
+}
+
 // TERMA adjoint: fluence_grad[beamlet(v)] += G_v * terma_grad[v].  A block
 // takes TT_VPT * 256 consecutive bricked voxels (a run of bricks along x) and
 // sums them per beamlet in a shared histogram of the beam's fluence map, then
@@ -2032,6 +2085,10 @@ cudaError_t ee_launch_terma_T(const EeParams& P, const EeBeamSpec* specs, const 
                               const float* unit_terma, const int* beamlet_idx, const float* terma_grad,
                               float* fluence_grad, int nbeams, long long max_tvol, cudaStream_t s) {
     (void)geoms;
+    if (P.ss > 1) {  // supersampled TERMA: recompute the sub-voxel beamlets
+        k_terma_T_ss<<<dim3(grid1(max_tvol, 256), 1, nbeams), 256, 0, s>>>(P, specs, terma_grad, fluence_grad);
+        return cudaGetLastError();
+    }
     dim3 grid(grid1(max_tvol, 256 * TT_VPT), 1, nbeams);
     k_terma_T<<<grid, 256, 0, s>>>(P, specs, unit_terma, beamlet_idx, terma_grad, fluence_grad);
     return cudaGetLastError();

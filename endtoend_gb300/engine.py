@@ -305,7 +305,7 @@ class Engine:
         self._check(self.lib.ee_set_kernel_mode(self.h, modes[mode]))
 
     def set_terma_supersampling(self, ss_factor: int):
-        """TERMA supersampling (omni-header ss_factor), forward dose only."""
+        """TERMA supersampling (omni-header ss_factor); the adjoint recomputes the sub-voxel beamlets."""
         self._check(self.lib.ee_set_terma_supersampling(self.h, int(ss_factor)))
 
     # -- forward dose

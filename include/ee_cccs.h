@@ -143,8 +143,9 @@ int ee_set_kernel_mode(ee_context *ctx, int mode);
 /* TERMA supersampling (the omni-header ss_factor; cudaSiddon.cu:248-306):
  * each calc-bbox voxel's TERMA is the mean over ss^3 sub-voxel centres, each
  * with its own beamlet lookup and ray trace.  1 (the default) = off; up to 8.
- * Forward dose only: adjoint and loss calls fail with EE_ERR_INVALID_ARG while
- * it is above 1 (a sub-sampled voxel draws on several beamlets). */
+ * Adjoint and loss calls recompute each sub-voxel centre's beamlet and unit
+ * TERMA in the TERMA adjoint (a supersampled voxel draws on several
+ * beamlets). */
 int ee_set_terma_supersampling(ee_context *ctx, int ss_factor);
 
 /* ---- forward dose (radconvolveTexture) ----
