@@ -138,3 +138,27 @@ def test_server_admission_and_errors():
         assert ei.value.code == engine.EE_ERR_NOMEM
         with pytest.raises(engine.EEError):
             srv.submit(7, beams)  # unknown volume
+
+
+def test_server_serving_workload_sizes():
+    """The serving workload at its stated sizes: head-and-neck phantoms of
+    96^3, 128^3, 160^3 and 256x256x192 voxels at 2 mm, requests of 1-40 beams
+    with fluence grids 16^2-64^2, dose or dose + gradient (the first 12
+    requests of the seeded 50/s stream, all queued at once on 2 slots): every
+    request equals its result alone (rtol 1e-5 dose, 1e-4 gradient)."""
+    vols, raw = inputs.serving_workload(12, 50.0, seed=9)
+    rng = np.random.default_rng(13)
+    grads = [rng.standard_normal(v.density.shape).astype(np.float32) for v in vols]
+    reqs = [(r["volume"], r["beams"], grads[r["volume"]] if r["grad"] else None) for r in raw]
+    assert {len(b) for _, b, _ in reqs} and max(len(b) for _, b, _ in reqs) > 20
+    phys = inputs.make_physics(seed=0, spacing_cm=0.2)
+    ref = _alone(vols, phys, reqs)
+    with engine.Server(0, slots=2, max_batch_beams=256) as srv:
+        srv.set_physics(phys, mode="exp")
+        for v in vols:
+            srv.add_volume(v)
+        tickets = [srv.submit(v, beams, grad) for v, beams, grad in reqs]
+        got = [srv.wait(t) for t in tickets]
+        st = srv.stats()
+    _check(reqs, ref, got)
+    assert st["completed"] == len(reqs)
