@@ -660,8 +660,8 @@ def main():
             "stage_ms": {k: round(v[0], 3) for k, v in prof.items()},
             "chain_frac": (2 * alg_bytes / (sum(step_ms) / len(step_ms) / 1e3) / 1e9) / peak}
     # kernels per graph replay: per chunk geom_init, terma, geometry, cone, gather,
-    # gather_T, cone_T, terma_T
-    gpu_launches = int(plan_info["chunks"]) * 8 * args.steps
+    # rev_zero, gather_T, cone_T, terma_T
+    gpu_launches = int(plan_info["chunks"]) * 9 * args.steps
 
     # accuracy vs the reference discretisation on one beam (FP64 oracle,
     # 24-radius table, texture 8-bit weights)
