@@ -1649,8 +1649,10 @@ __global__ void __launch_bounds__(ROW_WARPS * 32, 6) k_gather(EeParams P, const 
 constexpr int GT_TX = 8, GT_TY = 8, GT_TZ = 4;
 // floats per footprint buffer: an 8x8x4 tile spans at most |(7,7,3)| + 2 = 13
 // REV cells per axis when the REV spacing equals the voxel size (16 along i
-// after the quad alignment), 2704 < 4096; larger footprints (finer REV
-// spacing) take the direct-scatter path
+// after the quad alignment; 16 x 13 x 13 = 2704 < 4096).  A box clipped at
+// the array's end takes one cell more on that axis, which can pass 4096 only
+// for a tile at the array's corner under the widest rotation; such boxes and
+// larger footprints (finer REV spacing) take the direct-scatter path
 constexpr int GT_BUF = 4096;
 constexpr int GT_SMEM = 2 * GT_BUF;
 
@@ -1661,10 +1663,11 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
     extern __shared__ int acc_all[];  // two fixed-point footprint boxes
     // per cone: {l0 | n0 << 16, l1 | n1 << 16, l2 | n2 << 16, s0} (box origin
     // and extent along i, tY and tZ, the box's row stride along i; all below
-    // 2^16), read with one vector load before the scatter, and {sy, sz,
-    // offset lo, offset hi} (the REV gradient's brick strides and the cone's
-    // arena offset), read with one before the flush
-    __shared__ int4 s_p[EE_MAX_RAYS][2];
+    // 2^16) and {v0, v1, v2} (rev - l: the box cells inside the REV array),
+    // read with two vector loads before the scatter, and {sy, sz, offset lo,
+    // offset hi} (the REV gradient's brick strides and the cone's arena
+    // offset), read with one before the flush
+    __shared__ int4 s_p[EE_MAX_RAYS][3];
     __shared__ float4 s_A[EE_MAX_RAYS][3];
     const int b = blockIdx.z;
     const EeBeamGeom& G = geoms[b];
@@ -1712,9 +1715,16 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
         // REV axes: q.y -> rev[0] (along the line), q.z -> rev[1], q.x -> rev[2]
         const int dim = a == 1 ? R.rev[0] : (a == 2 ? R.rev[1] : R.rev[2]);
         int l = max(0, (int)floorf(lo - 1e-3f));
-        const int h = min(dim - 1, (int)floorf(hi + 1e-3f) + 1);
+        int h = min(dim - 1, (int)floorf(hi + 1e-3f) + 1);
+        // A voxel's corners are floor(q) - l and the cell above, and floor(q)
+        // <= floor(hi + 1e-3), so unclipped they stay inside [0, h - l].  Where
+        // the box is clipped at the array's last cell it gets one more, so the
+        // upper corner of a voxel in the last cell lands in the box; the flush
+        // drops it (the forward reads 0 past the array).
+        if (h == dim - 1 && h >= l) h++;
         int w = h - l + 1;
         int* sp = reinterpret_cast<int*>(s_p[r]);
+        sp[8 + (a == 1 ? 0 : (a == 2 ? 1 : 2))] = dim - (a == 1 ? (l & ~3) : l);
         if (a == 1) {
             int s0 = 0;
             if (w > 0) {
@@ -1725,7 +1735,7 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
                 l &= ~3;
                 // row stride 4 (mod 8) floats: the rows of adjacent voxels
                 // spread over the shared banks; the extra quad of a row is
-                // never scattered to (k0 < w), stays zero and is not sent
+                // never scattered to, stays zero and is not sent
                 s0 = (w & 7) == 0 ? w + 4 : w;
             }
             sp[3] = s0;
@@ -1778,38 +1788,32 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
                 const f3 q = mk(fmaf(a0.x, dx, fmaf(a0.y, dy, fmaf(a0.z, dz, a0.w))),
                                 fmaf(a1.x, dx, fmaf(a1.y, dy, fmaf(a1.z, dz, a1.w))),
                                 fmaf(a2.x, dx, fmaf(a2.y, dy, fmaf(a2.z, dz, a2.w))));
-                // the forward gather skips a cone where q is outside [0, rev):
-                // below 0 here; above, every corner lies past the box's end
-                // in tY and tZ (weight 0) or in the brick padding past rev[0]
+                // the forward gather skips a cone where q is outside [0, rev)
                 if (!(q.x < 0.f || q.y < 0.f || q.z < 0.f)) {
+                    const int4 pv = s_p[r][2];  // rev - l per axis
                     const float f0 = floorf(q.y), f1 = floorf(q.z), f2 = floorf(q.x);
                     const int j0 = (int)f0 - l0, j1 = (int)f1 - l1, j2 = (int)f2 - l2;
-                    const float a0 = q.y - f0, a1 = q.z - f1, a2 = q.x - f2;
-                    // Corners outside the box get weight 0 and a clamped
-                    // index inside it, so the eight adds need no tests.  The
-                    // box ends at the last REV cell in tY and tZ, so that is
-                    // the array edge there (tri_brick's border); in i it can
-                    // reach the brick padding past rev[0], cells outside
-                    // every segment, which the flush sends but nothing reads.
-                    const float w0[2] = {j0 >= 0 && j0 < n0 ? 1.f - a0 : 0.f, j0 + 1 >= 0 && j0 + 1 < n0 ? a0 : 0.f};
-                    const float w1[2] = {j1 >= 0 && j1 < n1 ? 1.f - a1 : 0.f, j1 + 1 >= 0 && j1 + 1 < n1 ? a1 : 0.f};
-                    const float w2[2] = {j2 >= 0 && j2 < n2 ? 1.f - a2 : 0.f, j2 + 1 >= 0 && j2 + 1 < n2 ? a2 : 0.f};
-                    const int c0[2] = {min(max(j0, 0), n0 - 1), min(max(j0 + 1, 0), n0 - 1)};
-                    const int c1[2] = {min(max(j1, 0), n1 - 1), min(max(j1 + 1, 0), n1 - 1)};
-                    const int c2[2] = {min(max(j2, 0), n2 - 1), min(max(j2 + 1, 0), n2 - 1)};
+                    if (j0 < pv.x && j1 < pv.y && j2 < pv.z) {
+                        const float a0 = q.y - f0, a1 = q.z - f1, a2 = q.x - f2;
+                        // all eight corners lie in the box (its set-up above);
+                        // those past the array's end are dropped by the flush
+                        const float w0[2] = {1.f - a0, a0}, w1[2] = {1.f - a1, a1}, w2[2] = {1.f - a2, a2};
+                        int* const c = acc + j0 + s0 * (j1 + n1p * j2);
+                        const int ss = s0 * n1p;
 #pragma unroll
-                    for (int d2 = 0; d2 < 2; d2++) {
-                        const float t2 = w2[d2] * gds;
+                        for (int d2 = 0; d2 < 2; d2++) {
+                            const float t2 = w2[d2] * gds;
 #pragma unroll
-                        for (int d1 = 0; d1 < 2; d1++) {
-                            const float t1 = w1[d1] * t2;
-                            // w * g * s rounded to an integer: the sum with
-                            // 1.5 * 2^23 has unit spacing, its low bits are
-                            // the integer (|w g s| < 2^22)
+                            for (int d1 = 0; d1 < 2; d1++) {
+                                const float t1 = w1[d1] * t2;
+                                // w * g * s rounded to an integer: the sum with
+                                // 1.5 * 2^23 has unit spacing, its low bits are
+                                // the integer (|w g s| < 2^22)
 #pragma unroll
-                            for (int d0 = 0; d0 < 2; d0++)
-                                atomicAdd(acc + c0[d0] + s0 * (c1[d1] + n1p * c2[d2]),
-                                          __float_as_int(fmaf(w0[d0], t1, 12582912.f)) - 0x4B400000);
+                                for (int d0 = 0; d0 < 2; d0++)
+                                    atomicAdd(c + d0 + d1 * s0 + d2 * ss,
+                                              __float_as_int(fmaf(w0[d0], t1, 12582912.f)) - 0x4B400000);
+                            }
                         }
                     }
                 }
@@ -1839,8 +1843,14 @@ __global__ void __launch_bounds__(GT_TX * GT_TY * GT_TZ) k_gather_T(EeParams P, 
                     const int kq = k - q1 * nq0;
                     const int k2 = __float2int_rd(((float)q1 + 0.5f) * inv1);
                     const int k1 = q1 - k2 * n1p;
-                    red_v4(rb + bk_x(l0 + 4 * kq) + bk_y(Bv, l1 + k1) + bk_z(Bv, l2 + k2), (float)v.x * fx_inv,
-                           (float)v.y * fx_inv, (float)v.z * fx_inv, (float)v.w * fx_inv);
+                    // rows and slabs past the array's end and quads that
+                    // start past it hold the forward's border corners (0):
+                    // cleared, not sent; a quad that starts inside the array
+                    // ends in its last brick, whose padding nothing reads
+                    const int4 pv = s_p[r][2];
+                    if (4 * kq < pv.x && k1 < pv.y && k2 < pv.z)
+                        red_v4(rb + bk_x(l0 + 4 * kq) + bk_y(Bv, l1 + k1) + bk_z(Bv, l2 + k2), (float)v.x * fx_inv,
+                               (float)v.y * fx_inv, (float)v.z * fx_inv, (float)v.w * fx_inv);
                 }
             }
         } else if (nbox > GT_BUF && gd != 0.f) {
