@@ -341,14 +341,14 @@ __device__ __forceinline__ void zero_outside_segment(float* out, const Brick& Bv
 // reference).
 __device__ __forceinline__ void gather_line(const EeParams& P, const EeBeamSpec& S, const EeBeamGeom& G,
                                             const EeRayGeom& R, const float* __restrict__ terma_b, int tY, int tZ,
-                                            int i0, int n, int lane, float* rho, float* T) {
+                                            int i0, int n, int lane, float* rho, float* T, int stride = 32) {
     const f3 bl = ld3(R.B0) + ld3(R.By) * (float)tY + ld3(R.Bz) * (float)tZ;
     const f3 gl = ld3(R.G0) + ld3(R.Gy) * (float)tY + ld3(R.Gz) * (float)tZ;
     const f3 bx = ld3(R.Bx), gx = ld3(R.Gx);
     const float bsx = (float)G.bev[0], bsy = (float)G.bev[1], bsz = (float)G.bev[2];
     const float b0x = (float)P.bb0[0], b0y = (float)P.bb0[1], b0z = (float)P.bb0[2];
     const float b1x = (float)(P.bb0[0] + P.bbs[0]), b1y = (float)(P.bb0[1] + P.bbs[1]), b1z = (float)(P.bb0[2] + P.bbs[2]);
-    for (int k = lane; k < n; k += 32) {
+    for (int k = lane; k < n; k += stride) {
         const float fi = (float)(i0 + k);
         f3 bev = bl + bx * fi;
         float r = -3.f, t = 0.f;
@@ -693,11 +693,14 @@ __device__ __forceinline__ TabRow tab_row(const float* t, bool fwd) {
                   o + 4 * EE_MAX_RADII};
 }
 
+// exclusive prefix sum over the W-lane group of `lane` (W = 32: the warp; W =
+// 16: each half separately); all 32 lanes take part
+template <int W = 32>
 __device__ __forceinline__ float warp_excl_scan(float x, int lane) {
     float s = x;
 #pragma unroll
-    for (int off = 1; off < 32; off <<= 1) {
-        const float y = __shfl_up_sync(FULL, s, off);
+    for (int off = 1; off < W; off <<= 1) {
+        const float y = __shfl_up_sync(FULL, s, off, W);
         if (lane >= off) s += y;
     }
     return s - x;
@@ -706,12 +709,13 @@ __device__ __forceinline__ float warp_excl_scan(float x, int lane) {
 template <bool FWD>
 __device__ __forceinline__ int wmap(int w, int n) { return FWD ? w : n - 1 - w; }
 
-// lane chunks of a line: the shortest length that covers it, so that as
-// many lanes as possible share a line (measured faster than odd lengths,
-// which spread the lanes' strided shared-memory accesses over all the banks
-// but leave up to a third of the lanes idle)
+// lane chunks of a line over the W lanes that share it: the shortest length
+// that covers it, so that as many lanes as possible work (measured faster
+// than odd lengths, which spread the lanes' strided shared-memory accesses
+// over all the banks but leave up to a third of the lanes idle)
+template <int W = 32>
 __device__ __forceinline__ void tab_chunk(int n, int lane, int& w0, int& w1) {
-    const int cs = max(1, (n + 31) >> 5);
+    const int cs = max(1, (n + W - 1) / W);
     w0 = min(n, lane * cs);
     w1 = min(n, w0 + cs);
 }
@@ -719,11 +723,11 @@ __device__ __forceinline__ void tab_chunk(int n, int lane, int& w0, int& w1) {
 // M_w, P_w, SV_w = T_{w-1} and SVM_w in walk order (separate arrays: lanes
 // reading scattered samples then spread over all the banks); T is 0 at
 // sentinels.
-template <bool FWD>
+template <bool FWD, int W = 32>
 __device__ __forceinline__ void tab_build(const float* rho, const float* T, int n, int lane, float delr, float* Mv,
                                           float* Pv, float* SVv, float* SVMv) {
     int w0, w1;
-    tab_chunk(n, lane, w0, w1);
+    tab_chunk<W>(n, lane, w0, w1);
     const float tp0 = (w0 > 0 && w0 < w1) ? T[wmap<FWD>(w0 - 1, n)] : 0.f;
     float sd = 0.f, svm = 0.f, tp = tp0;
     for (int w = w0; w < w1; w++) {  // chunk sums, P local to the chunk
@@ -734,8 +738,8 @@ __device__ __forceinline__ void tab_build(const float* rho, const float* T, int 
         sd += d;
         tp = t;
     }
-    const float Pst = warp_excl_scan(sd, lane);
-    float S = warp_excl_scan(fmaf(Pst, tp - tp0, svm), lane);
+    const float Pst = warp_excl_scan<W>(sd, lane);
+    float S = warp_excl_scan<W>(fmaf(Pst, tp - tp0, svm), lane);
     float Pw = Pst;
     tp = tp0;
     for (int w = w0; w < w1; w++) {
@@ -757,12 +761,12 @@ __device__ __forceinline__ void tab_build(const float* rho, const float* T, int 
 // adds its part, divides by nphi and zeroes sentinel samples.  X: this lane's
 // window ends, X[32 j] = x_j (shared memory, so the loops over the window
 // ends stay loops).
-template <bool FWD>
+template <bool FWD, int W = 32>
 __device__ __forceinline__ void tab_receivers(const float* Mv, const float* Pv, const float* SVv, const float* SVMv,
                                               const float* rho, int n, int lane, const TabRow& K, int* X, float* D,
                                               float nphi) {
     int w0, w1;
-    tab_chunk(n, lane, w0, w1);
+    tab_chunk<W>(n, lane, w0, w1);
     if (w0 >= w1) return;
     const float Rl = K.R[TAB_NR - 1];
     // window ends with R_j >= M_{n-1} - M_0 stay at 0 for every receiver
@@ -834,11 +838,11 @@ __device__ __forceinline__ void tab_receivers(const float* Mv, const float* Pv, 
 }
 
 // P_w, Sg_w, SgP_w (w = 0..n, P_n = +inf: pointer stop) and M_w in walk order.
-template <bool FWD>
+template <bool FWD, int W = 32>
 __device__ __forceinline__ void tab_build_T(const float* rho, const float* g, int n, int lane, float delr, float* Pv,
                                             float* Sgv, float* SgPv, float* Mv) {
     int w0, w1;
-    tab_chunk(n, lane, w0, w1);
+    tab_chunk<W>(n, lane, w0, w1);
     float sd = 0.f, sg = 0.f, sgp = 0.f;
     for (int w = w0; w < w1; w++) {
         const int i = wmap<FWD>(w, n);
@@ -847,9 +851,9 @@ __device__ __forceinline__ void tab_build_T(const float* rho, const float* g, in
         sg += gi;
         sd += r >= 0.f ? delr * r : 0.f;
     }
-    float Pw = warp_excl_scan(sd, lane);
-    float Sg = warp_excl_scan(sg, lane);
-    float SgP = warp_excl_scan(fmaf(Pw, sg, sgp), lane);
+    float Pw = warp_excl_scan<W>(sd, lane);
+    float Sg = warp_excl_scan<W>(sg, lane);
+    float SgP = warp_excl_scan<W>(fmaf(Pw, sg, sgp), lane);
     for (int w = w0; w < w1; w++) {
         const int i = wmap<FWD>(w, n);
         const float r = rho[i], gi = g[i];
@@ -872,11 +876,11 @@ __device__ __forceinline__ void tab_build_T(const float* rho, const float* g, in
 // Sources of one walk direction: W[k] = Phi_{b_k}(M_k), U[k] = Phi_{b_{k-1}}(M_k),
 // with the window ends y_j (Y[32 j], shared memory) clipped above at cap + 1
 // for each cap.
-template <bool FWD>
+template <bool FWD, int W = 32>
 __device__ __forceinline__ void tab_sources(const float* Pv, const float* Sgv, const float* SgPv, const float* Mv,
                                             int n, int lane, const TabRow& K, int* Y, float* Wk, float* Uk) {
     int w0, w1;
-    tab_chunk(n, lane, w0, w1);
+    tab_chunk<W>(n, lane, w0, w1);
     if (w0 >= w1) return;
     const float Rl = K.R[TAB_NR - 1], Rl2 = K.R[TAB_NR - 2];
     // window ends with R_j >= P_{n-1} - M_0 stay at n for every source
@@ -965,6 +969,56 @@ __host__ __device__ constexpr int tab_lp(int maxL) { return ((maxL + 3) & ~3) + 
 __host__ __device__ constexpr int tab_fwd_stride(int maxL) { return 7 * tab_lp(maxL) + 32 * TAB_NB; }
 __host__ __device__ constexpr int tab_adj_stride(int maxL) { return 9 * tab_lp(maxL) + 32 * TAB_NR; }
 
+// One line of k_cone_tab on the W lanes of its group (`lane` counts within
+// the group; W = 32: the whole warp, W = 16: half of it), with the group's
+// arrays at `arr`.  line < 0 or n <= 0: nothing to write, but the group still
+// takes part in the scans, which all 32 lanes execute.
+template <int W>
+__device__ __forceinline__ void tab_fwd_line(const EeParams& P, const EeBeamSpec& S, const EeBeamGeom& G,
+                                             const EeRayGeom& R, const float* __restrict__ terma_b,
+                                             float* __restrict__ rev_beam, int line, int i0, int n, int lane,
+                                             float* arr, int Lp, const float* tab, int* X) {
+    float* Mv = arr;
+    float* Pv = Mv + Lp;
+    float* SVv = Pv + Lp;
+    float* SVMv = SVv + Lp;
+    float* rho = SVMv + Lp;
+    float* T = rho + Lp;
+    float* D = T + Lp;
+    float* out = nullptr;
+    int nn = 0;
+    if (line >= 0) {
+        const int L = R.rev[0];
+        const int tY = line % R.rev[1], tZ = line / R.rev[1];
+        const Brick Bv = rev_brick(R.rev[0], R.rev[1], R.rev[2]);
+        out = rev_beam + R.offset + rev_line(Bv, tY, tZ);
+        int z0, z1;
+        line_read_span(G, R, tY, tZ, L, z0, z1);
+        zero_outside_segment(out, Bv, z0, z1, i0, n, lane, W);
+        if (n > 0) {
+            gather_line(P, S, G, R, terma_b, tY, tZ, i0, n, lane, rho, T, W);
+            nn = n;
+        }
+    }
+    __syncwarp();
+    const float nphi = (float)P.nphi;
+    tab_build<true, W>(rho, T, nn, lane, P.lng, Mv, Pv, SVv, SVMv);
+    __syncwarp();
+    tab_receivers<true, W>(Mv, Pv, SVv, SVMv, rho, nn, lane, tab_row(tab, true), X, D, nphi);
+    __syncwarp();
+    tab_build<false, W>(rho, T, nn, lane, P.lng, Mv, Pv, SVv, SVMv);
+    __syncwarp();
+    tab_receivers<false, W>(Mv, Pv, SVv, SVMv, rho, nn, lane, tab_row(tab, false), X, D, nphi);
+    __syncwarp();
+    for (int k = lane; k < nn; k += W) out[bk_x(i0 + k)] = D[k];
+}
+
+// A warp takes two neighbouring lines.  When both fit half of its arrays (n
+// below Lp / 2), each half-warp runs one of them, 16 lanes per line; else the
+// whole warp runs one after the other.  A lane's first receiver costs a
+// binary search per window end, so a lane that runs one chunk of a line
+// instead of two shorter chunks of two lines saves one set of searches, and
+// short lines keep more lanes busy.
 __global__ void __launch_bounds__(TAB_WARPS * 32) k_cone_tab(EeParams P, const EeBeamSpec* __restrict__ specs,
                                                              const EeBeamGeom* __restrict__ geoms,
                                                              const float* __restrict__ terma, float* __restrict__ rev,
@@ -981,40 +1035,96 @@ __global__ void __launch_bounds__(TAB_WARPS * 32) k_cone_tab(EeParams P, const E
     const EeBeamGeom& G = geoms[b];
     if (G.status != 0) return;
     const EeRayGeom& R = G.ray[ray];
-    const int line = blockIdx.x * TAB_WARPS + warp;
-    if (line >= R.nlines) return;
+    const int la = 2 * (blockIdx.x * TAB_WARPS + warp);
+    if (la >= R.nlines) return;
+    const int lb = la + 1 < R.nlines ? la + 1 : -1;
     const int L = R.rev[0];
-    const int tY = line % R.rev[1], tZ = line / R.rev[1];
-    float* Mv = sm + (size_t)warp * tab_fwd_stride(maxL);
-    float* Pv = Mv + Lp;
-    float* SVv = Pv + Lp;
-    float* SVMv = SVv + Lp;
-    float* rho = SVMv + Lp;
-    float* T = rho + Lp;
-    float* D = T + Lp;
-    int* X = reinterpret_cast<int*>(D + Lp) + lane;
-    const Brick Bv = rev_brick(R.rev[0], R.rev[1], R.rev[2]);
-    float* out = rev + G.arena_off + R.offset + rev_line(Bv, tY, tZ);
-    int i0, n, z0, z1;
-    line_segment(P, G, R, tY, tZ, L, i0, n);
-    line_read_span(G, R, tY, tZ, L, z0, z1);
-    zero_outside_segment(out, Bv, z0, z1, i0, n, lane, 32);
-    if (n <= 0) return;
-    gather_line(P, specs[b], G, R, terma + specs[b].t_off, tY, tZ, i0, n, lane, rho, T);
-    __syncwarp();
-    const float nphi = (float)P.nphi;
-    tab_build<true>(rho, T, n, lane, P.lng, Mv, Pv, SVv, SVMv);
-    __syncwarp();
-    tab_receivers<true>(Mv, Pv, SVv, SVMv, rho, n, lane, tab_row(tab, true), X, D, nphi);
-    __syncwarp();
-    tab_build<false>(rho, T, n, lane, P.lng, Mv, Pv, SVv, SVMv);
-    __syncwarp();
-    tab_receivers<false>(Mv, Pv, SVv, SVMv, rho, n, lane, tab_row(tab, false), X, D, nphi);
-    __syncwarp();
-    for (int k = lane; k < n; k += 32) out[bk_x(i0 + k)] = D[k];
+    int i0a, na, i0b = 0, nb = 0;
+    line_segment(P, G, R, la % R.rev[1], la / R.rev[1], L, i0a, na);
+    if (lb >= 0) line_segment(P, G, R, lb % R.rev[1], lb / R.rev[1], L, i0b, nb);
+    float* arr = sm + (size_t)warp * tab_fwd_stride(maxL);
+    int* X = reinterpret_cast<int*>(arr + 7 * Lp) + lane;
+    const EeBeamSpec& S = specs[b];
+    const float* terma_b = terma + S.t_off;
+    float* rev_beam = rev + G.arena_off;
+    const int half = Lp >> 1;
+    if (max(na, nb) < half) {
+        const int sub = lane >> 4;
+        tab_fwd_line<16>(P, S, G, R, terma_b, rev_beam, sub ? lb : la, sub ? i0b : i0a, sub ? nb : na, lane & 15,
+                         arr + sub * half, Lp, tab, X);
+    } else {
+        tab_fwd_line<32>(P, S, G, R, terma_b, rev_beam, la, i0a, na, lane, arr, Lp, tab, X);
+        if (lb >= 0) {
+            __syncwarp();
+            tab_fwd_line<32>(P, S, G, R, terma_b, rev_beam, lb, i0b, nb, lane, arr, Lp, tab, X);
+        }
+    }
 }
 
-// Its adjoint followed by the transpose of the REV TERMA resample.
+// One line of k_cone_T_tab on the W lanes of its group (as tab_fwd_line).
+template <int W>
+__device__ __forceinline__ void tab_adj_line(const EeParams& P, const EeBeamSpec& S, const EeBeamGeom& G,
+                                             const EeRayGeom& R, const float* __restrict__ grad_beam,
+                                             float* __restrict__ terma_grad, int line, int i0, int n, int lane,
+                                             float* arr, int Lp, const float* tab, int* Y) {
+    float* Pv = arr;
+    float* Sgv = Pv + Lp;
+    float* SgPv = Sgv + Lp;
+    float* Mv = SgPv + Lp;
+    float* rho = Mv + Lp;
+    float* g = rho + Lp;
+    float* Tb = g + Lp;
+    float* Wk = Tb + Lp;
+    float* Uk = Wk + Lp;
+    int nn = 0, tY = 0, tZ = 0;
+    if (line >= 0 && n > 0) {
+        tY = line % R.rev[1];
+        tZ = line / R.rev[1];
+        gather_line(P, S, G, R, nullptr, tY, tZ, i0, n, lane, rho, nullptr, W);
+        nn = n;
+    }
+    __syncwarp();
+    if (nn > 0) {
+        const Brick Bv = rev_brick(R.rev[0], R.rev[1], R.rev[2]);
+        const float* gin = grad_beam + R.offset + rev_line(Bv, tY, tZ);
+        const float inv_nphi = 1.f / (float)P.nphi;
+        for (int k = lane; k < nn; k += W) {
+            g[k] = rho[k] >= 0.f ? gin[bk_x(i0 + k)] * inv_nphi : 0.f;
+            Tb[k] = 0.f;
+        }
+    }
+    __syncwarp();
+#pragma unroll 1
+    for (int dir = 0; dir < 2; dir++) {
+        if (dir == 0) tab_build_T<true, W>(rho, g, nn, lane, P.lng, Pv, Sgv, SgPv, Mv);
+        else tab_build_T<false, W>(rho, g, nn, lane, P.lng, Pv, Sgv, SgPv, Mv);
+        __syncwarp();
+        if (dir == 0) tab_sources<true, W>(Pv, Sgv, SgPv, Mv, nn, lane, tab_row(tab, true), Y, Wk, Uk);
+        else tab_sources<false, W>(Pv, Sgv, SgPv, Mv, nn, lane, tab_row(tab, false), Y, Wk, Uk);
+        __syncwarp();
+        for (int w = lane; w < nn; w += W) {
+            const float v = Wk[w] - (w + 1 < nn ? Uk[w + 1] : 0.f);
+            Tb[dir == 0 ? w : nn - 1 - w] += v;
+        }
+        __syncwarp();
+    }
+    if (nn > 0) {
+        // transpose of the REV TERMA resample
+        const f3 gl = ld3(R.G0) + ld3(R.Gy) * (float)tY + ld3(R.Gz) * (float)tZ;
+        const f3 gx = ld3(R.Gx);
+        float* tg = terma_grad + S.t_off;
+        for (int k = lane; k < nn; k += W) {
+            const float v = Tb[k];
+            if (rho[k] < 0.f || v == 0.f) continue;
+            const f3 gp = gl + gx * (float)(i0 + k);
+            tri_brick_scatter(tg, brick_of(S.tn), gp.x - (float)S.t0[0], gp.y - (float)S.t0[1],
+                              gp.z - (float)S.t0[2], v);
+        }
+    }
+}
+
+// Its adjoint followed by the transpose of the REV TERMA resample; two lines
+// per warp as k_cone_tab.
 __global__ void __launch_bounds__(TAB_WARPS * 32) k_cone_T_tab(EeParams P, const EeBeamSpec* __restrict__ specs,
                                                                const EeBeamGeom* __restrict__ geoms,
                                                                const float* __restrict__ rev_grad,
@@ -1031,57 +1141,28 @@ __global__ void __launch_bounds__(TAB_WARPS * 32) k_cone_T_tab(EeParams P, const
     const EeBeamGeom& G = geoms[b];
     if (G.status != 0) return;
     const EeRayGeom& R = G.ray[ray];
-    const int line = blockIdx.x * TAB_WARPS + warp;
-    if (line >= R.nlines) return;
+    const int la = 2 * (blockIdx.x * TAB_WARPS + warp);
+    if (la >= R.nlines) return;
+    const int lb = la + 1 < R.nlines ? la + 1 : -1;
     const int L = R.rev[0];
-    const int tY = line % R.rev[1], tZ = line / R.rev[1];
-    float* Pv = sm + (size_t)warp * tab_adj_stride(maxL);
-    float* Sgv = Pv + Lp;
-    float* SgPv = Sgv + Lp;
-    float* Mv = SgPv + Lp;
-    float* rho = Mv + Lp;
-    float* g = rho + Lp;
-    float* Tb = g + Lp;
-    float* Wk = Tb + Lp;
-    float* Uk = Wk + Lp;
-    int* Y = reinterpret_cast<int*>(Uk + Lp) + lane;
+    int i0a, na, i0b = 0, nb = 0;
+    line_segment(P, G, R, la % R.rev[1], la / R.rev[1], L, i0a, na);
+    if (lb >= 0) line_segment(P, G, R, lb % R.rev[1], lb / R.rev[1], L, i0b, nb);
+    float* arr = sm + (size_t)warp * tab_adj_stride(maxL);
+    int* Y = reinterpret_cast<int*>(arr + 9 * Lp) + lane;
     const EeBeamSpec& S = specs[b];
-    int i0, n;
-    line_segment(P, G, R, tY, tZ, L, i0, n);
-    if (n <= 0) return;
-    gather_line(P, S, G, R, nullptr, tY, tZ, i0, n, lane, rho, nullptr);
-    const Brick Bv = rev_brick(R.rev[0], R.rev[1], R.rev[2]);
-    const float* gin = rev_grad + G.arena_off + R.offset + rev_line(Bv, tY, tZ);
-    const float inv_nphi = 1.f / (float)P.nphi;
-    __syncwarp();
-    for (int k = lane; k < n; k += 32) {
-        g[k] = rho[k] >= 0.f ? gin[bk_x(i0 + k)] * inv_nphi : 0.f;
-        Tb[k] = 0.f;
-    }
-    __syncwarp();
-#pragma unroll 1
-    for (int dir = 0; dir < 2; dir++) {
-        if (dir == 0) tab_build_T<true>(rho, g, n, lane, P.lng, Pv, Sgv, SgPv, Mv);
-        else tab_build_T<false>(rho, g, n, lane, P.lng, Pv, Sgv, SgPv, Mv);
-        __syncwarp();
-        if (dir == 0) tab_sources<true>(Pv, Sgv, SgPv, Mv, n, lane, tab_row(tab, true), Y, Wk, Uk);
-        else tab_sources<false>(Pv, Sgv, SgPv, Mv, n, lane, tab_row(tab, false), Y, Wk, Uk);
-        __syncwarp();
-        for (int w = lane; w < n; w += 32) {
-            const float v = Wk[w] - (w + 1 < n ? Uk[w + 1] : 0.f);
-            Tb[dir == 0 ? w : n - 1 - w] += v;
+    const float* grad_beam = rev_grad + G.arena_off;
+    const int half = Lp >> 1;
+    if (max(na, nb) < half) {
+        const int sub = lane >> 4;
+        tab_adj_line<16>(P, S, G, R, grad_beam, terma_grad, sub ? lb : la, sub ? i0b : i0a, sub ? nb : na,
+                         lane & 15, arr + sub * half, Lp, tab, Y);
+    } else {
+        tab_adj_line<32>(P, S, G, R, grad_beam, terma_grad, la, i0a, na, lane, arr, Lp, tab, Y);
+        if (lb >= 0) {
+            __syncwarp();
+            tab_adj_line<32>(P, S, G, R, grad_beam, terma_grad, lb, i0b, nb, lane, arr, Lp, tab, Y);
         }
-        __syncwarp();
-    }
-    // transpose of the REV TERMA resample
-    const f3 gl = ld3(R.G0) + ld3(R.Gy) * (float)tY + ld3(R.Gz) * (float)tZ;
-    const f3 gx = ld3(R.Gx);
-    float* tg = terma_grad + S.t_off;
-    for (int k = lane; k < n; k += 32) {
-        const float v = Tb[k];
-        if (rho[k] < 0.f || v == 0.f) continue;
-        const f3 gp = gl + gx * (float)(i0 + k);
-        tri_brick_scatter(tg, brick_of(S.tn), gp.x - (float)S.t0[0], gp.y - (float)S.t0[1], gp.z - (float)S.t0[2], v);
     }
 }
 
@@ -2060,7 +2141,7 @@ cudaError_t ee_launch_cone(const EeParams& P, const EeBeamSpec* specs, const EeB
         const size_t smem = sizeof(float) * ((size_t)TAB_WARPS * tab_fwd_stride(max_line) + TAB_SMEM);
         cudaError_t e = smem_attr((const void*)k_cone_tab, smem);
         if (e != cudaSuccess) return e;
-        dim3 grid(grid1(max_lines, TAB_WARPS), P.nrays, nbeams);
+        dim3 grid(grid1(max_lines, 2 * TAB_WARPS), P.nrays, nbeams);
         k_cone_tab<<<grid, TAB_WARPS * 32, smem, s>>>(P, specs, geoms, terma, rev, max_line);
         return cudaGetLastError();
     }
@@ -2112,7 +2193,7 @@ cudaError_t ee_launch_cone_T(const EeParams& P, const EeBeamSpec* specs, const E
         const size_t smem = sizeof(float) * ((size_t)TAB_WARPS * tab_adj_stride(max_line) + TAB_SMEM);
         cudaError_t e = smem_attr((const void*)k_cone_T_tab, smem);
         if (e != cudaSuccess) return e;
-        dim3 grid(grid1(max_lines, TAB_WARPS), P.nrays, nbeams);
+        dim3 grid(grid1(max_lines, 2 * TAB_WARPS), P.nrays, nbeams);
         k_cone_T_tab<<<grid, TAB_WARPS * 32, smem, s>>>(P, specs, geoms, rev_grad, terma_grad, max_line);
         return cudaGetLastError();
     }
