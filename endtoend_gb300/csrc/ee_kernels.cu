@@ -1014,7 +1014,7 @@ __device__ __forceinline__ void tab_fwd_line(const EeParams& P, const EeBeamSpec
 }
 
 // A warp takes two neighbouring lines.  When both fit half of its arrays (n
-// below Lp / 2), each half-warp runs one of them, 16 lanes per line; else the
+// below Lp / 2 - 1), each half-warp runs one of them, 16 lanes per line; else the
 // whole warp runs one after the other.  A lane's first receiver costs a
 // binary search per window end, so a lane that runs one chunk of a line
 // instead of two shorter chunks of two lines saves one set of searches, and
@@ -1047,11 +1047,13 @@ __global__ void __launch_bounds__(TAB_WARPS * 32) k_cone_tab(EeParams P, const E
     const EeBeamSpec& S = specs[b];
     const float* terma_b = terma + S.t_off;
     float* rev_beam = rev + G.arena_off;
+    // the second half-warp's arrays start one cell past the middle: an odd
+    // offset puts the two halves' strided accesses on different banks
     const int half = Lp >> 1;
-    if (max(na, nb) < half) {
+    if (max(na, nb) < half - 1) {
         const int sub = lane >> 4;
         tab_fwd_line<16>(P, S, G, R, terma_b, rev_beam, sub ? lb : la, sub ? i0b : i0a, sub ? nb : na, lane & 15,
-                         arr + sub * half, Lp, tab, X);
+                         arr + sub * (half + 1), Lp, tab, X);
     } else {
         tab_fwd_line<32>(P, S, G, R, terma_b, rev_beam, la, i0a, na, lane, arr, Lp, tab, X);
         if (lb >= 0) {
@@ -1152,11 +1154,11 @@ __global__ void __launch_bounds__(TAB_WARPS * 32) k_cone_T_tab(EeParams P, const
     int* Y = reinterpret_cast<int*>(arr + 9 * Lp) + lane;
     const EeBeamSpec& S = specs[b];
     const float* grad_beam = rev_grad + G.arena_off;
-    const int half = Lp >> 1;
-    if (max(na, nb) < half) {
+    const int half = Lp >> 1;  // second half-warp's arrays at an odd offset, as k_cone_tab
+    if (max(na, nb) < half - 1) {
         const int sub = lane >> 4;
         tab_adj_line<16>(P, S, G, R, grad_beam, terma_grad, sub ? lb : la, sub ? i0b : i0a, sub ? nb : na,
-                         lane & 15, arr + sub * half, Lp, tab, Y);
+                         lane & 15, arr + sub * (half + 1), Lp, tab, Y);
     } else {
         tab_adj_line<32>(P, S, G, R, grad_beam, terma_grad, la, i0a, na, lane, arr, Lp, tab, Y);
         if (lb >= 0) {
