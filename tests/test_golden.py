@@ -41,3 +41,29 @@ def test_golden_fixtures_reproduce_from_reference_source():
     vol, phys, beams, doses, _, _ = golden_cases.load("slab32")
     d, _, _ = ref_harness.ReferenceHarness(vol, phys, tex_emulate=True).beam_dose(beams[1])
     assert np.abs(d - doses[1]).max() <= 1e-6 * doses[1].max()
+
+
+def test_beamlet_cfg4_fixture_matches_its_problem():
+    """The config-4 beamlet fixture describes the problem that
+    golden_cases.cfg4_problem builds: same phantom (density digest), the 8
+    beams' active beamlets, 200 columns, and per-column summaries that are
+    consistent (top entries and block sums within the column maximum, the
+    reference's change non-negative)."""
+    vol, phys, beams, ke, max_rev, thresh, z = golden_cases.load_cfg4()
+    assert int(z["nbeams"]) == len(beams) == 8
+    ncol = 0
+    for k, b in enumerate(beams):
+        idx = z[f"beam{k}_beamlet_index"]
+        np.testing.assert_array_equal(idx, np.flatnonzero(b.fluence.ravel() > 0))
+        mx, noise = z[f"beam{k}_max"], z[f"beam{k}_ref_noise"]
+        assert len(mx) == len(idx) == len(noise) and (mx > 0).all() and (noise >= 0).all()
+        tv, tp = z[f"beam{k}_top_val"], z[f"beam{k}_top_key_ptr"]
+        bs, bp = z[f"beam{k}_blk_sum"], z[f"beam{k}_blk_key_ptr"]
+        assert len(tp) == len(bp) == len(idx) + 1
+        for c in range(len(idx)):
+            top = tv[tp[c]:tp[c + 1]]
+            assert 0 < len(top) <= golden_cases.CFG4_TOP
+            assert abs(top.max() - mx[c]) <= 1e-6 * mx[c]
+            assert bs[bp[c]:bp[c + 1]].sum() <= z[f"beam{k}_sum"][c] * (1 + 1e-6)
+        ncol += len(idx)
+    assert ncol == 200 and ke == 2.0 and thresh == 1e-4
