@@ -202,6 +202,11 @@ __device__ __forceinline__ void tri_brick_scatter(float* v, const Brick& B, floa
     const bool both = in0 && in1 && o != 3;     // corner i + 1 in the same row
     const int xa = in0 ? (i >> 2) << 6 : 0;     // brick row of corner i
     const int xb = in1 ? ((i + 1) >> 2) << 6 : 0;  // brick row of corner i + 1 (slot 0 unless both)
+    // the x weights in the four slots of corner i's brick row, the same for
+    // the four corner rows: each row's reduction is w times this pattern
+    const float a0 = 1.f - ax;
+    const float p0 = o == 0 ? a0 : 0.f, p1 = o == 1 ? a0 : (o == 0 && both ? ax : 0.f);
+    const float p2 = o == 2 ? a0 : (o == 1 && both ? ax : 0.f), p3 = o == 3 ? a0 : (o == 2 && both ? ax : 0.f);
 #pragma unroll
     for (int dk = 0; dk < 2; dk++) {
         int kk = k + dk;
@@ -213,13 +218,8 @@ __device__ __forceinline__ void tri_brick_scatter(float* v, const Brick& B, floa
             if (jj < 0 || jj >= B.n1) continue;
             float w = (dj ? ay : 1.f - ay) * wz * g;
             float* row = v + bk_y(B, jj) + bk_z(B, kk);
-            const float wa = (1.f - ax) * w, wb = ax * w;
-            if (in0) {
-                const float pb = both ? wb : 0.f;
-                red_v4(row + xa, o == 0 ? wa : 0.f, o == 1 ? wa : (o == 0 ? pb : 0.f),
-                       o == 2 ? wa : (o == 1 ? pb : 0.f), o == 3 ? wa : (o == 2 ? pb : 0.f));
-            }
-            if (in1 && !both) red_v4(row + xb, wb, 0.f, 0.f, 0.f);
+            if (in0) red_v4(row + xa, w * p0, w * p1, w * p2, w * p3);
+            if (in1 && !both) red_v4(row + xb, w * ax, 0.f, 0.f, 0.f);
         }
     }
 }
