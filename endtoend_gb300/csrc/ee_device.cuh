@@ -186,6 +186,29 @@ __device__ __forceinline__ float tri_brick(const float* __restrict__ v, const Br
     return acc;
 }
 
+// tri_brick for a point the caller has placed in [0, n0) x [0, n1) x [0, n2):
+// no entry test and no lower-bound tests; the same loads, weights and order.
+__device__ __forceinline__ float tri_brick_in(const float* __restrict__ v, const Brick& B, float x, float y, float z) {
+    const float fx = floorf(x), fy = floorf(y), fz = floorf(z);
+    const int i = (int)fx, j = (int)fy, k = (int)fz;
+    if (i + 1 < B.n0 && j + 1 < B.n1 && k + 1 < B.n2) {
+        const float ax = x - fx, ay = y - fy, az = z - fz;
+        const int x0 = bk_x(i), x1 = bk_x(i + 1), y0 = bk_y(B, j), y1 = bk_y(B, j + 1);
+        const int z0 = bk_z(B, k), z1 = bk_z(B, k + 1);
+        const float* p0 = v + z0;
+        const float* p1 = v + z1;
+        float c000 = __ldg(p0 + y0 + x0), c100 = __ldg(p0 + y0 + x1), c010 = __ldg(p0 + y1 + x0),
+              c110 = __ldg(p0 + y1 + x1);
+        float c001 = __ldg(p1 + y0 + x0), c101 = __ldg(p1 + y0 + x1), c011 = __ldg(p1 + y1 + x0),
+              c111 = __ldg(p1 + y1 + x1);
+        float c00 = c000 + ax * (c100 - c000), c10 = c010 + ax * (c110 - c010);
+        float c01 = c001 + ax * (c101 - c001), c11 = c011 + ax * (c111 - c011);
+        float c0 = c00 + ay * (c10 - c00), c1 = c01 + ay * (c11 - c01);
+        return c0 + az * (c1 - c0);
+    }
+    return tri_brick(v, B, x, y, z);  // the last cell of an axis: border corners
+}
+
 // Transpose of tri_brick (same weights as tri_border_scatter).  Each (y, z)
 // corner row takes one vector reduction on the 16-byte brick row of corner
 // i, holding both x corners unless the pair straddles a brick edge (i % 4 ==

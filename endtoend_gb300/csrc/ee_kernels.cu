@@ -1702,7 +1702,7 @@ __global__ void __launch_bounds__(ROW_WARPS * 32, 6) k_gather(EeParams P, const 
                 if (qy >= (float)n0 || qz >= (float)n1 || qx >= (float)n2 || qx < 0.f || qy < 0.f || qz < 0.f)
                     continue;
                 // bricked REV arrays over (i, tY, tZ): x = i (q.y), y = tY (q.z), z = tZ (q.x)
-                acc += tri_brick(base + __float_as_int(rv.w), rev_brick(n0, n1, n2), qy, qz, qx);
+                acc += tri_brick_in(base + __float_as_int(rv.w), rev_brick(n0, n1, n2), qy, qz, qx);
             }
         }
         if (mode == 2) out[rbase + x] = acc;
