@@ -186,21 +186,21 @@ __device__ __forceinline__ float tri_brick(const float* __restrict__ v, const Br
     return acc;
 }
 
-// tri_brick for a point the caller has placed in [0, n0) x [0, n1) x [0, n2):
-// no entry test and no lower-bound tests; the same loads, weights and order.
+// tri_brick for a point the caller has placed in [0, n0) x [0, n1) x [0, n2)
+// (B's sizes and brick strides): no entry or lower-bound tests, and the
+// corners addressed from the first one by per-axis steps (+1, +4, +16 inside
+// a brick; +61, +sy - 12, +sz - 48 across a brick face).  The same loads,
+// weights and order as tri_brick.
 __device__ __forceinline__ float tri_brick_in(const float* __restrict__ v, const Brick& B, float x, float y, float z) {
     const float fx = floorf(x), fy = floorf(y), fz = floorf(z);
     const int i = (int)fx, j = (int)fy, k = (int)fz;
     if (i + 1 < B.n0 && j + 1 < B.n1 && k + 1 < B.n2) {
         const float ax = x - fx, ay = y - fy, az = z - fz;
-        const int x0 = bk_x(i), x1 = bk_x(i + 1), y0 = bk_y(B, j), y1 = bk_y(B, j + 1);
-        const int z0 = bk_z(B, k), z1 = bk_z(B, k + 1);
-        const float* p0 = v + z0;
-        const float* p1 = v + z1;
-        float c000 = __ldg(p0 + y0 + x0), c100 = __ldg(p0 + y0 + x1), c010 = __ldg(p0 + y1 + x0),
-              c110 = __ldg(p0 + y1 + x1);
-        float c001 = __ldg(p1 + y0 + x0), c101 = __ldg(p1 + y0 + x1), c011 = __ldg(p1 + y1 + x0),
-              c111 = __ldg(p1 + y1 + x1);
+        const float* p = v + bk_x(i) + bk_y(B, j) + bk_z(B, k);
+        const int dx = (i & 3) == 3 ? 61 : 1, dy = (j & 3) == 3 ? B.sy - 12 : 4, dz = (k & 3) == 3 ? B.sz - 48 : 16;
+        float c000 = __ldg(p), c100 = __ldg(p + dx), c010 = __ldg(p + dy), c110 = __ldg(p + dy + dx);
+        float c001 = __ldg(p + dz), c101 = __ldg(p + dz + dx), c011 = __ldg(p + dz + dy),
+              c111 = __ldg(p + dz + dy + dx);
         float c00 = c000 + ax * (c100 - c000), c10 = c010 + ax * (c110 - c010);
         float c01 = c001 + ax * (c101 - c001), c11 = c011 + ax * (c111 - c011);
         float c0 = c00 + ay * (c10 - c00), c1 = c01 + ay * (c11 - c01);

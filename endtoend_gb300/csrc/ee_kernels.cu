@@ -1648,14 +1648,18 @@ __global__ void __launch_bounds__(ROW_WARPS * 32, 6) k_gather(EeParams P, const 
     const EeBeamGeom& G = geoms[b];
     if (G.status != 0) return;
     // the beam's cone maps, staged once per block: rows of [A | -q0] (REV
-    // from crop-box-relative patient index) and (rev sizes, arena offset)
-    __shared__ float4 s_ray[EE_MAX_RAYS][4];
-    for (int k = threadIdx.x; k < P.nrays * 4; k += blockDim.x) {
-        const int r = k >> 2, c = k & 3;
+    // from crop-box-relative patient index), (rev sizes, arena offset) and
+    // the REV array's brick strides
+    __shared__ float4 s_ray[EE_MAX_RAYS][5];
+    for (int k = threadIdx.x; k < P.nrays * 5; k += blockDim.x) {
+        const int r = k / 5, c = k - 5 * r;
         const EeRayGeom& R = G.ray[r];
         float4 v;
         if (c < 3) {
             v = make_float4(R.A[3 * c], R.A[3 * c + 1], R.A[3 * c + 2], -R.q0[c]);
+        } else if (c == 4) {
+            const Brick Bq = rev_brick(R.rev[0], R.rev[1], R.rev[2]);
+            v = make_float4(__int_as_float(Bq.sy), __int_as_float(Bq.sz), 0.f, 0.f);
         } else {
             v = make_float4(__int_as_float(R.rev[0]), __int_as_float(R.rev[1]), __int_as_float(R.rev[2]),
                             __int_as_float((int)R.offset));
@@ -1702,7 +1706,11 @@ __global__ void __launch_bounds__(ROW_WARPS * 32, 6) k_gather(EeParams P, const 
                 if (qy >= (float)n0 || qz >= (float)n1 || qx >= (float)n2 || qx < 0.f || qy < 0.f || qz < 0.f)
                     continue;
                 // bricked REV arrays over (i, tY, tZ): x = i (q.y), y = tY (q.z), z = tZ (q.x)
-                acc += tri_brick_in(base + __float_as_int(rv.w), rev_brick(n0, n1, n2), qy, qz, qx);
+                const float4 st = s_ray[r][4];
+                Brick Bq;
+                Bq.n0 = n0; Bq.n1 = n1; Bq.n2 = n2;
+                Bq.sy = __float_as_int(st.x); Bq.sz = __float_as_int(st.y);
+                acc += tri_brick_in(base + __float_as_int(rv.w), Bq, qy, qz, qx);
             }
         }
         if (mode == 2) out[rbase + x] = acc;
