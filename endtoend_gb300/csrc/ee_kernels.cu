@@ -1126,9 +1126,9 @@ __device__ __forceinline__ void tab_fwd_line(const EeParams& P, const EeBeamSpec
     for (int k = lane; k < nn; k += W) out[bk_x(i0 + k)] = D[k];
 }
 
-// A warp takes two neighbouring lines.  When both fit half of its arrays (n
-// below Lp / 2 - 1), each half-warp runs one of them, 16 lanes per line; else the
-// whole warp runs one after the other.  A lane's first receiver costs a
+// A warp takes two neighbouring lines.  When both fit half of its arrays
+// (n below Lp / 2 - 1), each half-warp runs one of them, 16 lanes per line;
+// else the whole warp runs one after the other.  A lane's first receiver costs a
 // binary search per window end, so a lane that runs one chunk of a line
 // instead of two shorter chunks of two lines saves one set of searches, and
 // short lines keep more lanes busy.
@@ -1843,8 +1843,9 @@ __global__ void __launch_bounds__(ROW_WARPS * 32, 6) k_gather(EeParams P, const 
 //
 // The shared boxes accumulate in 32-bit fixed point: integer adds are native
 // shared-memory atomics, while a float add to shared memory is a
-// compare-and-swap loop (measured: the scatter with float adds takes 1.41x as
-// long, and as long as non-atomic adds within 2 %).  Each tile scales its
+// compare-and-swap loop (measured on the whole kernel: 1.41x as long with
+// float adds; the integer form within 2 % of non-atomic adds, which give wrong
+// sums and served only as a bound).  Each tile scales its
 // gradients by a power of two s with max|g| * s in [2^21, 2^22), so one
 // contribution w * g * s (w <= 1) is below 2^22 in magnitude and rounds to
 // an integer exactly through the FP32 sum with 1.5 * 2^23; a box cell takes
