@@ -462,10 +462,10 @@ def run_reference(args, ws, rank):
 
 # DRAM bytes (read + write) per crop-box voxel of each stage, from ncu
 # captures of the chain kernels on eight beams of this workload (dram__bytes
-# of one call's launches / sum of V_beam = 12.37 M; k_gather_T captured again
-# with its fixed-point boxes); roofline.traffic scales the dominant stage's
-# figure to the profiled step.
-DRAM_BYTES_PER_VBEAM = {"terma": 1.0, "cone": 251.9, "gather": 51.7, "gather_T": 102.3, "cone_T": 196.1,
+# of one call's launches / sum of V_beam = 12.37 M; k_gather_T and
+# k_cone_T_lane captured again with their current forms); roofline.traffic
+# scales the dominant stage's figure to the profiled step.
+DRAM_BYTES_PER_VBEAM = {"terma": 1.0, "cone": 251.9, "gather": 51.7, "gather_T": 102.3, "cone_T": 230.3,
                         "terma_T": 3.5, "geometry": 0.0}
 
 
